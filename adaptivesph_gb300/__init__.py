@@ -1,0 +1,30 @@
+"""adaptivesph_gb300 — GB300-native (sm_103a) implementation of AdaptiveSph's per-step particle pipeline.
+
+The compute path is libasph_gb300.so (hand-written CUDA behind the C ABI of include/asph.h); this package is the
+Python mirror of the reference's simulation interface over that ABI, plus headless scene generators.
+"""
+from .parameters import (BoundaryMode, Criterion, DensityInfo, Domain, Parameters, RefinementParameters,
+                         ViscosityModel)
+from .simulation import (BoundaryParticlesDataImportedBuffer, FluidParticlesDataImportedBuffer, ImportedMemory,
+                         Simulation, StaticBoundaryDomain, allocate_buffer, create_simulation, import_buffer)
+from ._lib import AsphError, load as load_library
+
+__all__ = [
+    "AsphError",
+    "BoundaryMode",
+    "BoundaryParticlesDataImportedBuffer",
+    "Criterion",
+    "DensityInfo",
+    "Domain",
+    "FluidParticlesDataImportedBuffer",
+    "ImportedMemory",
+    "Parameters",
+    "RefinementParameters",
+    "Simulation",
+    "StaticBoundaryDomain",
+    "ViscosityModel",
+    "allocate_buffer",
+    "create_simulation",
+    "import_buffer",
+    "load_library",
+]

@@ -1,0 +1,82 @@
+// asph_kernels.cuh — kernel argument blocks and kernel declarations shared by the host code.
+#pragma once
+
+#include "asph_device.cuh"
+
+namespace asph {
+
+// Particle arrays of the current (cell-sorted) buffer set.
+struct StepArgs {
+    GridDev grid;
+    PhysDev phys;
+    uint32_t n;
+    float4* ph;   // x, y, z, h
+    float4* vm;   // vx, vy, vz, m
+    float4* acc;  // ax, ay, az, 0
+    float4* kc;   // 1/h, coef/h^3, dcoef/h^4, m
+    float2* rp;   // rho, p/rho^2
+    float* rad;
+    uint32_t* id;
+    uint32_t* err;
+};
+
+struct ReorderArgs {
+    const uint32_t* keys_sorted;
+    const uint32_t* vals_sorted;
+    const float4* ph_in;
+    const float4* vm_in;
+    const float4* acc_in;
+    const float* rad_in;
+    const uint32_t* id_in;
+    const float2* rp_in;  // may be null
+    uint32_t* start;
+    uint32_t* end;
+    float* hmax;
+    float* hmax_all;
+};
+
+__global__ void k_integrate_keys(StepArgs a, float dt, float pending_half, int has_pending, uint32_t* keys,
+                                 uint32_t* vals, unsigned long long* q3);
+__global__ void k_keys(StepArgs a, uint32_t* keys, uint32_t* vals, unsigned long long* q3);
+__global__ void k_boundary_keys(GridDev g, const float4* pos, uint32_t n, uint32_t* keys, uint32_t* vals,
+                                unsigned long long* q3);
+__global__ void k_excluded(const unsigned long long* q3, const uint32_t* n_ptr, uint32_t n_host, uint32_t* ex,
+                           int periodic);
+__global__ void k_reorder_cells(StepArgs a, ReorderArgs r);
+__global__ void k_cells_only(GridDev g, const uint32_t* keys, const uint32_t* n_ptr, uint32_t* start, uint32_t* end);
+__global__ void k_boundary_reorder(GridDev g, const float4* pos_in, const float* psi_in, float friction,
+                                   const uint32_t* keys_sorted, const uint32_t* vals_sorted, uint32_t n,
+                                   float4* pos_out, float* fric_out, uint32_t* start, uint32_t* end,
+                                   uint8_t* refflag);
+__global__ void k_density(StepArgs a, CellsDev c, BoundaryDev b);
+cudaError_t launch_forces(bool morris, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c, BoundaryDev b);
+__global__ void k_neighbor_counts(StepArgs a, CellsDev c, uint32_t* counts, unsigned long long* total);
+__global__ void k_export(StepArgs a, float pending_half, int has_pending, float4* pos_out, float4* vel_out,
+                         float* rho_out, float* rad_out, uint32_t* id_out);
+__global__ void k_totals(StepArgs a, float pending_half, int has_pending, double* out, unsigned int* cfl_min_bits);
+__global__ void k_density_info(StepArgs a, float threshold, float rest, double* sum, unsigned int* minmax,
+                               unsigned int* counts);
+
+// ------------------------------------------------------------------ radix sort (radix_sort.cu)
+// Stable LSD radix sort of (uint32 key, uint32 value) pairs, 8-bit digits, one onesweep pass per digit with
+// decoupled look-back. The item count is read from device memory so a sort can follow a device-side count.
+struct SortScratch {
+    uint32_t* keys_alt;
+    uint32_t* vals_alt;
+    uint32_t* hist;      // [4][256] digit counts, then exclusive offsets
+    uint32_t* lookback;  // [4][max_tiles][256]
+    uint32_t* counters;  // [4] tile counters
+    uint32_t max_items;
+    uint32_t max_tiles;
+};
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortThreads * kSortItems;
+size_t sort_scratch_bytes(uint32_t max_items);
+void sort_scratch_bind(SortScratch& s, void* base, uint32_t max_items);
+// Sorts keys/vals[0, *d_n) by bits [0, key_bits); n_max bounds *d_n. The result is in keys/vals (the
+// ping-pong buffers are swapped back if the number of passes is odd). Returns the number of kernels launched.
+int radix_sort_pairs(uint32_t*& keys, uint32_t*& vals, const uint32_t* d_n, uint32_t n_max, uint32_t key_bits,
+                     SortScratch& s, uint32_t* err, cudaStream_t stream);
+
+}  // namespace asph

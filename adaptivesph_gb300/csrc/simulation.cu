@@ -1,0 +1,1457 @@
+// simulation.cu — the host runtime behind the C ABI (include/asph.h): one simulation = device-resident
+// particle state + the per-step kernel sequence on one CUDA stream.
+//
+// Replaces SphSimulation / AdaptiveSphSimulation (cuda/src/simulation/SphSimulation.cu,
+// cuda/src/simulation/AdaptiveSphSimulation.cu), NeighborGrid (cuda/src/simulation/neighbors/NeighborGrid.cu),
+// ImportedParticleMemory (cuda/src/memory/ImportedParticleMemory.cu) and StaticBoundaryDomain
+// (cuda/src/simulation/physics/StaticBoundaryDomain.cu) behind the reference's interface.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/asph.h"
+#include "asph_kernels.cuh"
+#include "asph_refine.cuh"
+
+using namespace asph;
+
+// ------------------------------------------------------------------------------------------------ errors
+static thread_local std::string g_last_error;
+
+static asph_status fail(asph_status s, const std::string& msg) {
+    g_last_error = msg;
+    return s;
+}
+
+static asph_status cuda_fail(cudaError_t e, const char* what) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return ASPH_ERR_OUT_OF_MEMORY;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return ASPH_ERR_NO_DEVICE;
+    return ASPH_ERR_CUDA;
+}
+
+#define CK(call)                                                   \
+    do {                                                           \
+        cudaError_t e_ = (call);                                   \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);        \
+    } while (0)
+
+#define CK_LAUNCH(what)                                            \
+    do {                                                           \
+        cudaError_t e_ = cudaGetLastError();                       \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what);         \
+    } while (0)
+
+static inline uint32_t blocks_for(uint32_t n, uint32_t t = 256) { return n == 0 ? 1u : (n + t - 1) / t; }
+
+// ------------------------------------------------------------------------------------------------ memory
+struct asph_memory {
+    void* ptr = nullptr;
+    size_t size = 0;
+    cudaExternalMemory_t ext = nullptr;
+};
+
+// ------------------------------------------------------------------------------------------------ state kernels
+namespace {
+
+// Unpacks the SoA state into the reference's separate arrays.
+__global__ void k_read_state(StepArgs a, float4* pos, float4* vel, float4* acc, float* rho, float* rad, float* h,
+                             float* m, uint32_t* id) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const float4 ph = a.ph[i];
+    const float4 vm = a.vm[i];
+    pos[i] = make_float4(ph.x, ph.y, ph.z, 0.0f);
+    vel[i] = make_float4(vm.x, vm.y, vm.z, 0.0f);
+    acc[i] = a.acc[i];
+    rho[i] = a.rp[i].x;
+    rad[i] = a.rad[i];
+    h[i] = ph.w;
+    m[i] = vm.w;
+    id[i] = a.id[i];
+}
+
+__global__ void k_write_state(StepArgs a, const float4* pos, const float4* vel, const float4* acc, const float* rho,
+                              const float* rad, const float* h, const float* m, const uint32_t* id) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const float4 p = pos[i];
+    const float4 v = vel[i];
+    a.ph[i] = make_float4(p.x, p.y, p.z, h[i]);
+    a.vm[i] = make_float4(v.x, v.y, v.z, m[i]);
+    const float4 ac = acc[i];
+    a.acc[i] = make_float4(ac.x, ac.y, ac.z, 0.0f);
+    a.rp[i] = make_float2(rho[i], 0.0f);
+    a.rad[i] = rad[i];
+    a.id[i] = id[i];
+}
+
+// Initial state as the reference's constructor writes it (SphSimulation.cu:29-80): v = 0, a = (g, 0),
+// r = r0, h = h0, m = m0; the id is the array slot.
+__global__ void k_init_state(StepArgs a, const float4* pos, float r0, float h0, float m0) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const float4 p = pos[i];
+    a.ph[i] = make_float4(p.x, p.y, p.z, h0);
+    a.vm[i] = make_float4(0.0f, 0.0f, 0.0f, m0);
+    a.acc[i] = make_float4(a.phys.gravity[0], a.phys.gravity[1], a.phys.gravity[2], 0.0f);
+    a.rp[i] = make_float2(0.0f, 0.0f);
+    a.rad[i] = r0;
+    a.id[i] = i;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------------ simulation
+struct BufferSet {
+    float4* ph = nullptr;
+    float4* vm = nullptr;
+    float4* acc = nullptr;
+    float2* rp = nullptr;
+    float* rad = nullptr;
+    uint32_t* id = nullptr;
+};
+
+struct asph_simulation {
+    asph_parameters P{};
+    asph_refinement_parameters R{};
+    bool adaptive = false;
+    GridDev grid{};
+    PhysDev phys{};
+    uint32_t cap = 0, n = 0;
+    uint32_t bcap = 0, nb = 0;
+    uint32_t tpb = 256;
+
+    BufferSet set[2];
+    int cur = 0;
+    float4* kc = nullptr;
+    uint32_t* keys = nullptr;
+    uint32_t* vals = nullptr;
+    void* sort_mem = nullptr;
+    SortScratch ss{};
+    uint32_t* cell_start = nullptr;
+    uint32_t* cell_end = nullptr;
+    float* cell_hmax = nullptr;
+    uint32_t cells_alloc = 0;
+    float* hmax_all = nullptr;
+    uint32_t* ex = nullptr;
+    unsigned long long* q3 = nullptr;
+    uint32_t* err = nullptr;
+    uint32_t* d_count = nullptr;
+
+    // boundary
+    float4* bpos = nullptr;
+    float* bfric = nullptr;
+    uint32_t* bstart = nullptr;
+    uint32_t* bend = nullptr;
+    uint8_t* brefflag = nullptr;
+    uint32_t brefcells = 0;
+    uint32_t bex[2] = {kNone, kNone};
+
+    // refinement scratch
+    float* score = nullptr;
+    uint32_t* cand = nullptr;
+    uint32_t* flag = nullptr;
+    uint32_t* ctr = nullptr;
+    unsigned long long* slot0 = nullptr;
+    uint32_t* block_counts = nullptr;
+    uint32_t* rkeys = nullptr;    // [2 * cap] cell keys of the step and their compacted copy
+    uint32_t* dbg_ids = nullptr;  // [3 * cap] keep / removed / split id lists (when enabled)
+    bool record_ids = false;
+
+    // host-side state
+    uint32_t frame = 0;
+    uint32_t next_id = 0;
+    float pending_half = 0.0f;
+    bool has_pending = false;
+    bool grid_valid = false;
+    asph_refinement_report last_report{};
+    uint32_t last_pairs_listed = 0, last_splits_listed = 0;
+
+    // pinned host scratch
+    uint32_t* h_ctr = nullptr;
+    uint64_t* h_small = nullptr;
+
+    // export targets (imported memory)
+    asph_fluid_buffers fbuf{};
+    bool have_fbuf = false;
+    asph_boundary_buffers bbuf{};
+    bool have_bbuf = false;
+
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    uint64_t launches = 0;
+
+    // timing
+    bool timing = false;
+    struct Ev {
+        cudaEvent_t a, b;
+        int cls;
+    };
+    std::vector<Ev> events;
+    std::vector<cudaEvent_t> event_pool;
+    double ms[ASPH_KERNEL_COUNT] = {0};
+    uint32_t timed[ASPH_KERNEL_COUNT] = {0};
+
+    StepArgs args(int s) const {
+        StepArgs a;
+        a.grid = grid;
+        a.phys = phys;
+        a.n = n;
+        a.ph = set[s].ph;
+        a.vm = set[s].vm;
+        a.acc = set[s].acc;
+        a.rp = set[s].rp;
+        a.rad = set[s].rad;
+        a.id = set[s].id;
+        a.kc = kc;
+        a.err = err;
+        return a;
+    }
+
+    CellsDev cells() const { return CellsDev{cell_start, cell_end, cell_hmax, ex, hmax_all}; }
+
+    BoundaryDev boundary() const {
+        return BoundaryDev{bpos, bfric, bstart, bend, brefflag, bex[0], bex[1], nb};
+    }
+
+    cudaEvent_t take_event() {
+        if (!event_pool.empty()) {
+            cudaEvent_t e = event_pool.back();
+            event_pool.pop_back();
+            return e;
+        }
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        return e;
+    }
+    int tic() {
+        if (!timing) return -1;
+        Ev ev{take_event(), take_event(), 0};
+        cudaEventRecord(ev.a, stream);
+        events.push_back(ev);
+        return (int)events.size() - 1;
+    }
+    void toc(int h, int cls) {
+        if (h < 0) return;
+        events[h].cls = cls;
+        cudaEventRecord(events[h].b, stream);
+    }
+    void harvest() {
+        for (auto& e : events) {
+            float t = 0.f;
+            if (cudaEventElapsedTime(&t, e.a, e.b) == cudaSuccess) {
+                ms[e.cls] += t;
+                timed[e.cls] += 1;
+            }
+            event_pool.push_back(e.a);
+            event_pool.push_back(e.b);
+        }
+        events.clear();
+    }
+};
+
+namespace {
+
+template <class T>
+asph_status dalloc(T*& p, size_t count) {
+    p = nullptr;
+    if (count == 0) count = 1;
+    CK(cudaMalloc(reinterpret_cast<void**>(&p), sizeof(T) * count));
+    return ASPH_OK;
+}
+
+void dfree(void* p) {
+    if (p) cudaFree(p);
+}
+
+asph_status make_grid(const asph_parameters& P, GridDev& g) {
+    std::memset(&g, 0, sizeof(g));
+    const float cw = (2.0f * P.base_smoothing_radius) * 2.0f;
+    int32_t mx = 1;
+    uint64_t ncells = 1;
+    float maxscale = 0.0f;
+    for (int a = 0; a < 3; a++) {
+        g.dmin[a] = P.domain.min[a];
+        g.dmax[a] = P.domain.max[a];
+        g.scale[a] = P.domain.max[a] - P.domain.min[a];
+        if (!(g.scale[a] > 0.0f)) return fail(ASPH_ERR_INVALID_ARGUMENT, "domain max must exceed min on every axis");
+        const float q = std::ceil(g.scale[a] / cw);
+        if (!(q < 512.5f)) return fail(ASPH_ERR_UNSUPPORTED, "domain spans more than 512 cells of 4 h0 on an axis");
+        int32_t gs = (int32_t)q;
+        if (gs < 1) gs = 1;
+        if (P.boundary_mode == ASPH_BOUNDARY_PERIODIC && gs < 3)
+            return fail(ASPH_ERR_UNSUPPORTED, "a periodic box needs at least 3 cells of 4 h0 per axis");
+        g.gs[a] = gs;
+        g.cs[a] = g.scale[a] / (float)gs;
+        g.w[a] = g.cs[a] * 0.5f;
+        g.sgs[a] = 2 * gs;
+        mx = std::max(mx, g.sgs[a]);
+        ncells *= (uint64_t)g.sgs[a];
+        maxscale = std::max(maxscale, g.scale[a]);
+    }
+    uint32_t bits = 1;
+    while ((1 << bits) < mx) bits++;
+    g.bits = bits;
+    g.ncells = (uint32_t)ncells;
+    g.periodic = P.boundary_mode == ASPH_BOUNDARY_PERIODIC ? 1 : 0;
+    g.cull_margin = 1.0e-5f * maxscale;
+    return ASPH_OK;
+}
+
+void make_phys(const asph_parameters& P, PhysDev& ph) {
+    for (int a = 0; a < 3; a++) ph.gravity[a] = P.gravity[a];
+    ph.c0 = P.speed_of_sound;
+    ph.rho0 = P.rest_density;
+    ph.alpha = P.viscosity_constant;
+    ph.sigma = P.surface_tension_constant;
+    ph.max_velocity = P.max_velocity;
+    ph.h0 = P.base_smoothing_radius;
+    ph.r0 = P.base_particle_radius;
+    ph.m0 = P.base_particle_mass;
+    ph.nu = P.kinematic_viscosity;
+    ph.B = ((P.rest_density * P.speed_of_sound) * P.speed_of_sound) / 5.0f;
+    ph.morris = P.viscosity_model == ASPH_VISCOSITY_MORRIS ? 1 : 0;
+    ph.visc_on = ph.morris ? (P.kinematic_viscosity != 0.0f) : (P.viscosity_constant != 0.0f);
+    ph.sigma_on = P.surface_tension_constant != 0.0f;
+}
+
+asph_status alloc_cells(asph_simulation* s) {
+    if (s->grid.ncells <= s->cells_alloc) return ASPH_OK;
+    dfree(s->cell_start);
+    dfree(s->cell_end);
+    dfree(s->cell_hmax);
+    dfree(s->bstart);
+    dfree(s->bend);
+    s->cells_alloc = 0;
+    asph_status st;
+    if ((st = dalloc(s->cell_start, s->grid.ncells)) != ASPH_OK) return st;
+    if ((st = dalloc(s->cell_end, s->grid.ncells)) != ASPH_OK) return st;
+    if ((st = dalloc(s->cell_hmax, s->grid.ncells)) != ASPH_OK) return st;
+    if ((st = dalloc(s->bstart, s->grid.ncells)) != ASPH_OK) return st;
+    if ((st = dalloc(s->bend, s->grid.ncells)) != ASPH_OK) return st;
+    s->cells_alloc = s->grid.ncells;
+    return ASPH_OK;
+}
+
+// Uploads the boundary particles, sorts them by sub-cell and builds their tables; also writes the caller's
+// imported boundary buffers in the caller's order (initializeBoundaryParticles, SphSimulation.cu:287-333).
+asph_status setup_boundary(asph_simulation* s, const asph_boundary_particle* b, uint32_t nb) {
+    if (nb > s->bcap) {
+        dfree(s->bpos);
+        dfree(s->bfric);
+        s->bcap = 0;
+        asph_status st;
+        if ((st = dalloc(s->bpos, nb)) != ASPH_OK) return st;
+        if ((st = dalloc(s->bfric, nb)) != ASPH_OK) return st;
+        s->bcap = nb;
+    }
+    const uint32_t refcells = (uint32_t)(s->grid.gs[0] * s->grid.gs[1] * s->grid.gs[2]);
+    if (refcells > s->brefcells) {
+        dfree(s->brefflag);
+        s->brefcells = 0;
+        asph_status st;
+        if ((st = dalloc(s->brefflag, refcells)) != ASPH_OK) return st;
+        s->brefcells = refcells;
+    }
+    s->nb = nb;
+    CK(cudaMemsetAsync(s->bstart, 0xff, sizeof(uint32_t) * s->grid.ncells, s->stream));
+    CK(cudaMemsetAsync(s->bend, 0, sizeof(uint32_t) * s->grid.ncells, s->stream));
+    CK(cudaMemsetAsync(s->brefflag, 0, refcells, s->stream));
+    s->bex[0] = s->bex[1] = kNone;
+    if (nb == 0) return ASPH_OK;
+    std::vector<float4> pos(nb);
+    std::vector<float> psi(nb);
+    for (uint32_t i = 0; i < nb; i++) {
+        pos[i] = make_float4(b[i].position[0], b[i].position[1], b[i].position[2], b[i].position[3]);
+        psi[i] = b[i].psi;
+    }
+    float4* d_pos = nullptr;
+    float* d_psi = nullptr;
+    asph_status st;
+    if ((st = dalloc(d_pos, nb)) != ASPH_OK) return st;
+    if ((st = dalloc(d_psi, nb)) != ASPH_OK) {
+        dfree(d_pos);
+        return st;
+    }
+    CK(cudaMemcpyAsync(d_pos, pos.data(), sizeof(float4) * nb, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(d_psi, psi.data(), sizeof(float) * nb, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemsetAsync(s->q3, 0xff, 2 * sizeof(unsigned long long), s->stream));
+    k_boundary_keys<<<blocks_for(nb), 256, 0, s->stream>>>(s->grid, d_pos, nb, s->keys, s->vals, s->q3);
+    CK_LAUNCH("k_boundary_keys");
+    // the sort reads its item count from device memory
+    s->h_ctr[0] = nb;
+    CK(cudaMemcpyAsync(s->d_count + 1, s->h_ctr, sizeof(uint32_t), cudaMemcpyHostToDevice, s->stream));
+    s->launches += 1 + radix_sort_pairs(s->keys, s->vals, s->d_count + 1, nb, 3 * s->grid.bits, s->ss, s->err,
+                                        s->stream);
+    CK_LAUNCH("boundary sort");
+    k_excluded<<<1, 1, 0, s->stream>>>(s->q3, nullptr, nb, s->ex + 2, s->grid.periodic);
+    k_boundary_reorder<<<blocks_for(nb), 256, 0, s->stream>>>(s->grid, d_pos, d_psi, s->P.domain.friction, s->keys,
+                                                              s->vals, nb, s->bpos, s->bfric, s->bstart, s->bend,
+                                                              s->brefflag);
+    CK_LAUNCH("k_boundary_reorder");
+    s->launches += 2;
+    CK(cudaMemcpyAsync(s->h_ctr, s->ex + 2, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    s->bex[0] = s->h_ctr[0];
+    s->bex[1] = s->h_ctr[1];
+    dfree(d_pos);
+    dfree(d_psi);
+    if (s->have_bbuf) {
+        std::vector<float4> colors(nb, make_float4(0.3f, 0.3f, 0.3f, 0.2f));
+        std::vector<float> radii(nb, s->P.base_particle_radius);
+        const asph_memory* mp = s->bbuf.positions;
+        const asph_memory* mr = s->bbuf.radii;
+        const asph_memory* mc = s->bbuf.colors;
+        if (mp && mp->size >= sizeof(float4) * nb)
+            CK(cudaMemcpyAsync(mp->ptr, pos.data(), sizeof(float4) * nb, cudaMemcpyHostToDevice, s->stream));
+        if (mr && mr->size >= sizeof(float) * nb)
+            CK(cudaMemcpyAsync(mr->ptr, radii.data(), sizeof(float) * nb, cudaMemcpyHostToDevice, s->stream));
+        if (mc && mc->size >= sizeof(float4) * nb)
+            CK(cudaMemcpyAsync(mc->ptr, colors.data(), sizeof(float4) * nb, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
+    return ASPH_OK;
+}
+
+asph_status upload_count(asph_simulation* s) {
+    s->h_ctr[0] = s->n;
+    CK(cudaMemcpyAsync(s->d_count, s->h_ctr, sizeof(uint32_t), cudaMemcpyHostToDevice, s->stream));
+    return ASPH_OK;
+}
+
+// Sort the current particles by sub-cell, gather into the other buffer set, build the cell tables.
+asph_status build_grid(asph_simulation* s, bool integrate, float dt, bool carry_rho) {
+    const uint32_t n = s->n;
+    StepArgs a = s->args(s->cur);
+    CK(cudaMemsetAsync(s->q3, 0xff, 2 * sizeof(unsigned long long), s->stream));
+    int h = s->tic();
+    if (integrate) {
+        k_integrate_keys<<<blocks_for(n), 256, 0, s->stream>>>(a, dt, s->pending_half, s->has_pending ? 1 : 0,
+                                                               s->keys, s->vals, s->q3);
+        CK_LAUNCH("k_integrate_keys");
+        s->has_pending = false;
+    } else {
+        k_keys<<<blocks_for(n), 256, 0, s->stream>>>(a, s->keys, s->vals, s->q3);
+        CK_LAUNCH("k_keys");
+    }
+    s->toc(h, ASPH_KERNEL_INTEGRATE);
+    s->launches++;
+    h = s->tic();
+    s->launches += radix_sort_pairs(s->keys, s->vals, s->d_count, n, 3 * s->grid.bits, s->ss, s->err, s->stream);
+    CK_LAUNCH("radix sort");
+    s->toc(h, ASPH_KERNEL_SORT);
+    CK(cudaMemsetAsync(s->cell_start, 0xff, sizeof(uint32_t) * s->grid.ncells, s->stream));
+    CK(cudaMemsetAsync(s->cell_end, 0, sizeof(uint32_t) * s->grid.ncells, s->stream));
+    CK(cudaMemsetAsync(s->cell_hmax, 0, sizeof(float) * s->grid.ncells, s->stream));
+    CK(cudaMemsetAsync(s->hmax_all, 0, sizeof(float), s->stream));
+    k_excluded<<<1, 1, 0, s->stream>>>(s->q3, nullptr, n, s->ex, s->grid.periodic);
+    CK_LAUNCH("k_excluded");
+    ReorderArgs r;
+    r.keys_sorted = s->keys;
+    r.vals_sorted = s->vals;
+    r.ph_in = s->set[s->cur].ph;
+    r.vm_in = s->set[s->cur].vm;
+    r.acc_in = s->set[s->cur].acc;
+    r.rad_in = s->set[s->cur].rad;
+    r.id_in = s->set[s->cur].id;
+    r.rp_in = carry_rho ? s->set[s->cur].rp : nullptr;
+    r.start = s->cell_start;
+    r.end = s->cell_end;
+    r.hmax = s->cell_hmax;
+    r.hmax_all = s->hmax_all;
+    const int nxt = 1 - s->cur;
+    StepArgs b = s->args(nxt);
+    h = s->tic();
+    k_reorder_cells<<<blocks_for(n), 256, 0, s->stream>>>(b, r);
+    CK_LAUNCH("k_reorder_cells");
+    s->toc(h, ASPH_KERNEL_REORDER);
+    s->launches += 2;
+    s->cur = nxt;
+    s->grid_valid = true;
+    return ASPH_OK;
+}
+
+asph_status run_density(asph_simulation* s) {
+    StepArgs a = s->args(s->cur);
+    int h = s->tic();
+    k_density<<<blocks_for(s->n), 256, 0, s->stream>>>(a, s->cells(), s->boundary());
+    CK_LAUNCH("k_density");
+    s->toc(h, ASPH_KERNEL_DENSITY);
+    s->launches++;
+    return ASPH_OK;
+}
+
+asph_status run_forces(asph_simulation* s) {
+    StepArgs a = s->args(s->cur);
+    int h = s->tic();
+    CK(launch_forces(s->phys.morris != 0, blocks_for(s->n), s->stream, a, s->cells(), s->boundary()));
+    s->toc(h, ASPH_KERNEL_FORCES);
+    s->launches++;
+    return ASPH_OK;
+}
+
+RefineArgs refine_args(asph_simulation* s) {
+    RefineArgs r;
+    r.score = s->score;
+    r.cand = s->cand;
+    r.flag = s->flag;
+    r.ctr = s->ctr;
+    r.slot0 = s->slot0;
+    r.keep_ids = s->record_ids ? s->dbg_ids : nullptr;
+    r.removed_ids = s->record_ids ? s->dbg_ids + s->cap : nullptr;
+    r.split_ids = s->record_ids ? s->dbg_ids + 2 * (size_t)s->cap : nullptr;
+    r.err = s->err;
+    const asph_refinement_parameters& R = s->R;
+    r.min_mass = R.min_mass_ratio * s->P.base_particle_mass;
+    r.max_mass = R.max_mass_ratio * s->P.base_particle_mass;
+    r.max_batch_ratio = R.max_batch_ratio;
+    r.eps = R.split_epsilon;
+    r.alpha = R.split_alpha;
+    r.center_ratio = R.split_center_mass_ratio;
+    r.vertex_ratio = R.split_vertex_mass_ratio;
+    r.vel_split = R.velocity_split_min_speed;
+    r.vel_merge = R.velocity_merge_max_speed;
+    r.vort_split = R.vorticity_split_min;
+    r.vort_merge = R.vorticity_merge_max;
+    r.iface_split = R.interface_split_distance_ratio;
+    r.iface_merge = R.interface_merge_distance_ratio;
+    r.r0 = s->P.base_particle_radius;
+    r.m0 = s->P.base_particle_mass;
+    r.criterion = R.criterion;
+    return r;
+}
+
+uint32_t id_bits(uint32_t next_id) {
+    uint32_t b = 1;
+    while (b < 32 && (1ull << b) < (uint64_t)next_id) b++;
+    return b;
+}
+
+// One refinement pass (performAdaptiveRefinement, AdaptiveSphSimulation.cu:102-252); one read-back at the end.
+asph_status run_refine(asph_simulation* s) {
+    const uint32_t n = s->n;
+    s->last_report = asph_refinement_report{};
+    s->last_report.frame = s->frame;
+    s->last_report.count_before = n;
+    s->last_report.count_after = n;
+    if (n <= 1) return ASPH_OK;  // identifyAndMergeParticles returns early (AdaptiveSphSimulation.cu:197-200)
+    int h = s->tic();
+    RefineArgs r = refine_args(s);
+    std::memset(s->h_ctr, 0, sizeof(uint32_t) * kCtrNum);
+    s->h_ctr[kCtrNextId] = s->next_id;
+    CK(cudaMemcpyAsync(s->ctr, s->h_ctr, sizeof(uint32_t) * kCtrNum, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemsetAsync(s->slot0, 0xff, sizeof(unsigned long long), s->stream));
+    if (s->R.criterion == ASPH_CRITERION_VORTICITY) {
+        // keep the cell keys of this step: the selection sorts reuse the sort buffers
+        CK(cudaMemcpyAsync(s->rkeys, s->keys, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s->stream));
+    }
+    StepArgs a = s->args(s->cur);
+    const uint32_t nbk = blocks_for(n);
+    // merge selection
+    k_merge_score<<<nbk, 256, 0, s->stream>>>(a, s->cells(), r);
+    k_merge_limits<<<1, 1, 0, s->stream>>>(r, n);
+    k_select_ids<<<nbk, 256, 0, s->stream>>>(a, s->ctr + kCtrSortN, s->keys, s->vals);
+    CK_LAUNCH("merge selection");
+    s->launches += 3;
+    s->launches += radix_sort_pairs(s->keys, s->vals, s->ctr + kCtrSortN, n, id_bits(s->next_id), s->ss, s->err,
+                                    s->stream);
+    k_select_scores<<<nbk, 256, 0, s->stream>>>(s->score, s->ctr + kCtrSortN, 0, s->vals, s->keys);
+    s->launches += 1 + radix_sort_pairs(s->keys, s->vals, s->ctr + kCtrSortN, n, 32, s->ss, s->err, s->stream);
+    // candidates, pairs + merges
+    k_cand_init<<<nbk, 256, 0, s->stream>>>(r, n);
+    k_merge_candidates<<<nbk, 256, 0, s->stream>>>(a, s->cells(), r, s->vals);
+    k_merge_pairs<<<nbk, 256, 0, s->stream>>>(a, r);
+    CK_LAUNCH("merge");
+    // stable compaction into the other buffer set (also carries the cell keys for the vorticity split pass)
+    k_compact_count<<<nbk, 256, 0, s->stream>>>(s->flag, n, s->block_counts);
+    k_compact_scan<<<1, 1024, 0, s->stream>>>(s->block_counts, nbk, n, r);
+    const int nxt = 1 - s->cur;
+    StepArgs b = s->args(nxt);
+    const bool vort = s->R.criterion == ASPH_CRITERION_VORTICITY;
+    uint32_t* keys_c = s->rkeys + s->cap;
+    k_compact_scatter<<<nbk, 256, 0, s->stream>>>(a, b, s->flag, s->block_counts, vort ? s->rkeys : nullptr,
+                                                   keys_c);
+    CK_LAUNCH("compaction");
+    s->launches += 6;
+    s->cur = nxt;
+    StepArgs c = s->args(s->cur);
+    if (vort) {
+        // the compacted keys are still cell-sorted: rebuild the tables for the split criterion's search
+        CK(cudaMemsetAsync(s->cell_start, 0xff, sizeof(uint32_t) * s->grid.ncells, s->stream));
+        CK(cudaMemsetAsync(s->cell_end, 0, sizeof(uint32_t) * s->grid.ncells, s->stream));
+        k_cells_only<<<nbk, 256, 0, s->stream>>>(s->grid, keys_c, s->ctr + kCtrCount2, s->cell_start, s->cell_end);
+        s->launches++;
+    }
+    // split selection (skipped on the device when nothing was removed)
+    k_split_score<<<nbk, 256, 0, s->stream>>>(c, s->cells(), r);
+    k_split_limits<<<1, 1, 0, s->stream>>>(r, s->cap, s->tpb);
+    k_select_ids<<<nbk, 256, 0, s->stream>>>(c, s->ctr + kCtrSortN, s->keys, s->vals);
+    CK_LAUNCH("split selection");
+    s->launches += 3;
+    s->launches += radix_sort_pairs(s->keys, s->vals, s->ctr + kCtrSortN, n, id_bits(s->next_id), s->ss, s->err,
+                                    s->stream);
+    k_select_scores<<<nbk, 256, 0, s->stream>>>(s->score, s->ctr + kCtrSortN, 1, s->vals, s->keys);
+    s->launches += 1 + radix_sort_pairs(s->keys, s->vals, s->ctr + kCtrSortN, n, 32, s->ss, s->err, s->stream);
+    k_split_apply<<<nbk, 256, 0, s->stream>>>(c, r, s->vals);
+    k_refine_finish<<<1, 1, 0, s->stream>>>(r);
+    CK_LAUNCH("split");
+    s->launches += 2;
+    CK(cudaMemcpyAsync(s->d_count, s->ctr + kCtrCountOut, sizeof(uint32_t), cudaMemcpyDeviceToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->h_ctr, s->ctr, sizeof(uint32_t) * kCtrNum, cudaMemcpyDeviceToHost, s->stream));
+    s->toc(h, ASPH_KERNEL_REFINE);
+    CK(cudaStreamSynchronize(s->stream));
+    const uint32_t* c2 = s->h_ctr;
+    s->n = c2[kCtrCountOut];
+    s->next_id = c2[kCtrNextId];
+    s->last_report.merge_eligible = c2[kCtrEligible];
+    s->last_report.merge_pairs = c2[kCtrPairs];
+    s->last_report.removed = c2[kCtrRemoved];
+    s->last_report.split_candidates = c2[kCtrSplitCand];
+    s->last_report.split_budget = c2[kCtrSplitBudget];
+    s->last_report.splits = c2[kCtrSplits];
+    s->last_report.count_after = s->n;
+    s->last_pairs_listed = c2[kCtrPairs];
+    s->last_splits_listed = c2[kCtrSplits];
+    s->grid_valid = false;
+    return ASPH_OK;
+}
+
+bool refinement_due(const asph_simulation* s) {
+    if (!s->adaptive) return false;
+    const uint32_t f = s->frame, i0 = s->R.initial_cooldown, cd = s->R.cooldown;
+    return f == i0 || (f > i0 && f % cd == 0);
+}
+
+asph_status run_step(asph_simulation* s, float dt, uint32_t last_stage) {
+    if (!(std::isfinite(dt))) return fail(ASPH_ERR_INVALID_ARGUMENT, "delta time must be finite");
+    if (s->n == 0) {
+        // nothing to integrate; bookkeeping as the reference (kernels with zero threads)
+        if (last_stage >= ASPH_STAGE_ALL) {
+            s->pending_half = dt / 2.0f;
+            s->has_pending = true;
+            s->frame++;
+        }
+        return ASPH_OK;
+    }
+    asph_status st;
+    if (last_stage < ASPH_STAGE_GRID) {
+        // integrate only: keys are computed but the state is not reordered
+        StepArgs a = s->args(s->cur);
+        CK(cudaMemsetAsync(s->q3, 0xff, 2 * sizeof(unsigned long long), s->stream));
+        k_integrate_keys<<<blocks_for(s->n), 256, 0, s->stream>>>(a, dt, s->pending_half, s->has_pending ? 1 : 0,
+                                                                  s->keys, s->vals, s->q3);
+        CK_LAUNCH("k_integrate_keys");
+        s->launches++;
+        s->has_pending = false;
+        s->grid_valid = false;
+        return ASPH_OK;
+    }
+    if ((st = build_grid(s, true, dt, false)) != ASPH_OK) return st;
+    if (last_stage < ASPH_STAGE_DENSITY) return ASPH_OK;
+    if ((st = run_density(s)) != ASPH_OK) return st;
+    if (last_stage < ASPH_STAGE_FORCES) return ASPH_OK;
+    if ((st = run_forces(s)) != ASPH_OK) return st;
+    if (last_stage < ASPH_STAGE_ALL) return ASPH_OK;
+    if (refinement_due(s)) {
+        if ((st = run_refine(s)) != ASPH_OK) return st;
+    }
+    s->pending_half = dt / 2.0f;
+    s->has_pending = true;
+    s->frame++;
+    return ASPH_OK;
+}
+
+asph_status check_errors(asph_simulation* s, bool sync) {
+    if (sync) CK(cudaStreamSynchronize(s->stream));
+    CK(cudaMemcpy(s->h_ctr, s->err, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    const uint32_t e = s->h_ctr[0] & ~0x4u;
+    if (e != 0) {
+        char buf[128];
+        std::snprintf(buf, sizeof(buf), "device error word 0x%x", e);
+        return fail(ASPH_ERR_DEVICE_CHECK, buf);
+    }
+    return ASPH_OK;
+}
+
+asph_status ensure_grid(asph_simulation* s) {
+    if (s->grid_valid || s->n == 0) return ASPH_OK;
+    return build_grid(s, false, 0.0f, true);
+}
+
+void destroy(asph_simulation* s) {
+    if (!s) return;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    for (int k = 0; k < 2; k++) {
+        dfree(s->set[k].ph);
+        dfree(s->set[k].vm);
+        dfree(s->set[k].acc);
+        dfree(s->set[k].rp);
+        dfree(s->set[k].rad);
+        dfree(s->set[k].id);
+    }
+    dfree(s->kc);
+    dfree(s->keys);
+    dfree(s->vals);
+    dfree(s->sort_mem);
+    dfree(s->cell_start);
+    dfree(s->cell_end);
+    dfree(s->cell_hmax);
+    dfree(s->hmax_all);
+    dfree(s->ex);
+    dfree(s->q3);
+    dfree(s->err);
+    dfree(s->d_count);
+    dfree(s->bpos);
+    dfree(s->bfric);
+    dfree(s->bstart);
+    dfree(s->bend);
+    dfree(s->brefflag);
+    dfree(s->score);
+    dfree(s->cand);
+    dfree(s->flag);
+    dfree(s->ctr);
+    dfree(s->slot0);
+    dfree(s->block_counts);
+    dfree(s->rkeys);
+    dfree(s->dbg_ids);
+    if (s->h_ctr) cudaFreeHost(s->h_ctr);
+    if (s->h_small) cudaFreeHost(s->h_small);
+    for (auto& e : s->events) {
+        cudaEventDestroy(e.a);
+        cudaEventDestroy(e.b);
+    }
+    for (auto e : s->event_pool) cudaEventDestroy(e);
+    if (s->own_stream) cudaStreamDestroy(s->own_stream);
+    delete s;
+}
+
+}  // namespace
+
+// ================================================================================================ C ABI
+extern "C" {
+
+uint32_t asph_abi_version(void) { return ASPH_ABI_VERSION; }
+
+const char* asph_status_string(asph_status s) {
+    switch (s) {
+        case ASPH_OK: return "ok";
+        case ASPH_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case ASPH_ERR_CUDA: return "CUDA error";
+        case ASPH_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case ASPH_ERR_CAPACITY: return "capacity exceeded";
+        case ASPH_ERR_DEVICE_CHECK: return "device check failed";
+        case ASPH_ERR_UNSUPPORTED: return "unsupported";
+        case ASPH_ERR_NO_DEVICE: return "no CUDA device";
+    }
+    return "unknown status";
+}
+
+const char* asph_last_error(void) { return g_last_error.c_str(); }
+
+void asph_refinement_parameters_default(asph_refinement_parameters* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->enabled = 0;
+    p->min_mass_ratio = 0.3f;
+    p->max_mass_ratio = 8.0f;
+    p->max_particle_count = 1000000;
+    p->max_batch_ratio = 0.2f;
+    p->initial_cooldown = 10;
+    p->cooldown = 10;
+    p->criterion = ASPH_CRITERION_VELOCITY;
+    p->split_epsilon = 0.65f;
+    p->split_alpha = 0.70f;
+    p->split_center_mass_ratio = 0.077f;
+    p->split_vertex_mass_ratio = 0.077f;
+    p->velocity_split_min_speed = 2.0f;
+    p->velocity_merge_max_speed = 0.1f;
+    p->vorticity_split_min = 1.0f;
+    p->vorticity_merge_max = 0.3f;
+    p->curvature_split_min = 2.0f;
+    p->curvature_merge_max = 0.6f;
+    p->interface_split_distance_ratio = 0.05f;
+    p->interface_merge_distance_ratio = 0.15f;
+}
+
+// ---------------------------------------------------------------------------------------------- memory
+asph_status asph_import_buffer_fd(int fd, size_t size, asph_memory** out) {
+    if (!out || fd < 0 || size == 0) return fail(ASPH_ERR_INVALID_ARGUMENT, "import needs an fd, a size and out");
+    *out = nullptr;
+    cudaExternalMemoryHandleDesc hd;
+    std::memset(&hd, 0, sizeof(hd));
+    hd.type = cudaExternalMemoryHandleTypeOpaqueFd;
+    hd.handle.fd = fd;
+    hd.size = size;
+    cudaExternalMemory_t ext = nullptr;
+    CK(cudaImportExternalMemory(&ext, &hd));
+    cudaExternalMemoryBufferDesc bd;
+    std::memset(&bd, 0, sizeof(bd));
+    bd.offset = 0;
+    bd.size = size;
+    void* ptr = nullptr;
+    cudaError_t e = cudaExternalMemoryGetMappedBuffer(&ptr, ext, &bd);
+    if (e != cudaSuccess) {
+        cudaDestroyExternalMemory(ext);
+        return cuda_fail(e, "cudaExternalMemoryGetMappedBuffer");
+    }
+    asph_memory* m = new (std::nothrow) asph_memory;
+    if (!m) {
+        cudaFree(ptr);
+        cudaDestroyExternalMemory(ext);
+        return fail(ASPH_ERR_OUT_OF_MEMORY, "host allocation failed");
+    }
+    m->ptr = ptr;
+    m->size = size;
+    m->ext = ext;
+    *out = m;
+    return ASPH_OK;
+}
+
+asph_status asph_memory_allocate(size_t size, asph_memory** out) {
+    if (!out || size == 0) return fail(ASPH_ERR_INVALID_ARGUMENT, "allocation needs a size and out");
+    *out = nullptr;
+    void* p = nullptr;
+    CK(cudaMalloc(&p, size));
+    CK(cudaMemset(p, 0, size));
+    asph_memory* m = new (std::nothrow) asph_memory;
+    if (!m) {
+        cudaFree(p);
+        return fail(ASPH_ERR_OUT_OF_MEMORY, "host allocation failed");
+    }
+    m->ptr = p;
+    m->size = size;
+    *out = m;
+    return ASPH_OK;
+}
+
+asph_status asph_memory_device_pointer(const asph_memory* mem, void** out) {
+    if (!mem || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
+    *out = mem->ptr;
+    return ASPH_OK;
+}
+
+asph_status asph_memory_size(const asph_memory* mem, size_t* out) {
+    if (!mem || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
+    *out = mem->size;
+    return ASPH_OK;
+}
+
+void asph_memory_release(asph_memory* mem) {
+    if (!mem) return;
+    if (mem->ptr) cudaFree(mem->ptr);
+    if (mem->ext) cudaDestroyExternalMemory(mem->ext);
+    delete mem;
+}
+
+// ---------------------------------------------------------------------------------------------- simulation
+asph_status asph_simulation_create(const asph_parameters* parameters, const float* positions, uint32_t count,
+                                   const asph_fluid_buffers* fluid_buffers,
+                                   const asph_boundary_buffers* boundary_buffers,
+                                   const asph_boundary_particle* boundary, uint32_t boundary_count,
+                                   const asph_refinement_parameters* refinement, uint32_t max_fluid_capacity,
+                                   uint32_t max_boundary_capacity, asph_simulation** out) {
+    if (!parameters || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "parameters and out are required");
+    *out = nullptr;
+    if (count > 0 && !positions) return fail(ASPH_ERR_INVALID_ARGUMENT, "positions are required");
+    if (boundary_count > 0 && !boundary) return fail(ASPH_ERR_INVALID_ARGUMENT, "boundary particles are required");
+    const asph_parameters& P = *parameters;
+    if (!(P.base_smoothing_radius > 0.0f) || !(P.rest_density > 0.0f) || !(P.speed_of_sound > 0.0f) ||
+        !(P.base_particle_mass > 0.0f))
+        return fail(ASPH_ERR_INVALID_ARGUMENT, "smoothing radius, rest density, speed of sound and mass must be > 0");
+    if (P.viscosity_model > 1u || P.boundary_mode > 1u)
+        return fail(ASPH_ERR_INVALID_ARGUMENT, "unknown viscosity model or boundary mode");
+    const bool adaptive = refinement && refinement->enabled;
+    if (adaptive) {
+        if (refinement->cooldown == 0) return fail(ASPH_ERR_INVALID_ARGUMENT, "refinement cooldown must be > 0");
+        if (refinement->criterion > 2u) return fail(ASPH_ERR_INVALID_ARGUMENT, "unknown refinement criterion");
+        if (P.boundary_mode == ASPH_BOUNDARY_PERIODIC)
+            return fail(ASPH_ERR_UNSUPPORTED, "refinement in a periodic box is not supported");
+    }
+    // AdaptiveSphSimulation sizes the fluid arrays by maxParticleCount (AdaptiveSphSimulation.cu:37)
+    const uint32_t cap = adaptive ? refinement->max_particle_count : std::max(max_fluid_capacity, count);
+    if (count > cap) return fail(ASPH_ERR_CAPACITY, "more particles than the fluid capacity");
+    if (cap > (1u << 30)) return fail(ASPH_ERR_UNSUPPORTED, "fluid capacity above 2^30");
+    asph_simulation* s = new (std::nothrow) asph_simulation;
+    if (!s) return fail(ASPH_ERR_OUT_OF_MEMORY, "host allocation failed");
+    s->P = P;
+    if (adaptive) s->R = *refinement;
+    s->adaptive = adaptive;
+    s->tpb = P.threads_per_block ? P.threads_per_block : 256u;
+    s->cap = std::max(cap, 1u);
+    s->n = count;
+    s->next_id = count;
+    asph_status st = make_grid(P, s->grid);
+    if (st != ASPH_OK) {
+        delete s;
+        return st;
+    }
+    make_phys(P, s->phys);
+    if (fluid_buffers) {
+        s->fbuf = *fluid_buffers;
+        s->have_fbuf = true;
+    }
+    if (boundary_buffers) {
+        s->bbuf = *boundary_buffers;
+        s->have_bbuf = true;
+    }
+    cudaError_t e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        destroy(s);
+        return cuda_fail(e, "cudaStreamCreate");
+    }
+    s->stream = s->own_stream;
+#define TRY(x)                     \
+    if ((st = (x)) != ASPH_OK) {   \
+        destroy(s);                \
+        return st;                 \
+    }
+    const uint32_t C = s->cap;
+    for (int k = 0; k < 2; k++) {
+        TRY(dalloc(s->set[k].ph, C));
+        TRY(dalloc(s->set[k].vm, C));
+        TRY(dalloc(s->set[k].acc, C));
+        TRY(dalloc(s->set[k].rp, C));
+        TRY(dalloc(s->set[k].rad, C));
+        TRY(dalloc(s->set[k].id, C));
+    }
+    TRY(dalloc(s->kc, C));
+    const uint32_t sort_items = std::max(C, std::max(boundary_count, max_boundary_capacity));
+    TRY(dalloc(s->keys, sort_items));
+    TRY(dalloc(s->vals, sort_items));
+    {
+        uint8_t* mem = nullptr;
+        TRY(dalloc(mem, sort_scratch_bytes(sort_items)));
+        s->sort_mem = mem;
+        sort_scratch_bind(s->ss, mem, sort_items);
+    }
+    TRY(dalloc(s->hmax_all, 1));
+    TRY(dalloc(s->ex, 4));
+    TRY(dalloc(s->q3, 2));
+    TRY(dalloc(s->err, 1));
+    TRY(dalloc(s->d_count, 2));
+    TRY(alloc_cells(s));
+    if (adaptive) {
+        TRY(dalloc(s->score, C));
+        TRY(dalloc(s->cand, C));
+        TRY(dalloc(s->flag, C));
+        TRY(dalloc(s->ctr, kCtrNum));
+        TRY(dalloc(s->slot0, 1));
+        TRY(dalloc(s->block_counts, blocks_for(C)));
+        TRY(dalloc(s->rkeys, 2 * (size_t)C));
+    }
+    e = cudaMallocHost(reinterpret_cast<void**>(&s->h_ctr), sizeof(uint32_t) * 64);
+    if (e != cudaSuccess) {
+        destroy(s);
+        return cuda_fail(e, "cudaMallocHost");
+    }
+    e = cudaMallocHost(reinterpret_cast<void**>(&s->h_small), sizeof(uint64_t) * 16);
+    if (e != cudaSuccess) {
+        destroy(s);
+        return cuda_fail(e, "cudaMallocHost");
+    }
+    CK(cudaMemsetAsync(s->err, 0, sizeof(uint32_t), s->stream));
+    CK(cudaMemsetAsync(s->hmax_all, 0, sizeof(float), s->stream));
+    s->bcap = 0;
+    TRY(setup_boundary(s, boundary, boundary_count));
+    if (count > 0) {
+        float4* d_pos = nullptr;
+        TRY(dalloc(d_pos, count));
+        e = cudaMemcpyAsync(d_pos, positions, sizeof(float4) * count, cudaMemcpyHostToDevice, s->stream);
+        if (e == cudaSuccess) {
+            k_init_state<<<blocks_for(count), 256, 0, s->stream>>>(s->args(s->cur), d_pos, P.base_particle_radius,
+                                                                   P.base_smoothing_radius, P.base_particle_mass);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        dfree(d_pos);
+        if (e != cudaSuccess) {
+            destroy(s);
+            return cuda_fail(e, "initial upload");
+        }
+        s->launches++;
+    }
+    TRY(upload_count(s));
+    e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) {
+        destroy(s);
+        return cuda_fail(e, "create");
+    }
+#undef TRY
+    *out = s;
+    return ASPH_OK;
+}
+
+void asph_simulation_destroy(asph_simulation* sim) { destroy(sim); }
+
+asph_status asph_simulation_step_async(asph_simulation* sim, float delta_time) {
+    if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
+    return run_step(sim, delta_time, ASPH_STAGE_ALL);
+}
+
+asph_status asph_simulation_update(asph_simulation* sim, float delta_time) {
+    asph_status st = asph_simulation_step_async(sim, delta_time);
+    if (st != ASPH_OK) return st;
+    return check_errors(sim, true);
+}
+
+asph_status asph_simulation_run_stages(asph_simulation* sim, float delta_time, uint32_t last_stage) {
+    if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
+    if (last_stage < ASPH_STAGE_INTEGRATE || last_stage > ASPH_STAGE_ALL)
+        return fail(ASPH_ERR_INVALID_ARGUMENT, "unknown stage");
+    asph_status st = run_step(sim, delta_time, last_stage);
+    if (st != ASPH_OK) return st;
+    return check_errors(sim, true);
+}
+
+asph_status asph_simulation_synchronize(asph_simulation* sim) {
+    if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
+    return check_errors(sim, true);
+}
+
+asph_status asph_simulation_totals(asph_simulation* sim, asph_totals* out) {
+    if (!sim || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
+    std::memset(out, 0, sizeof(*out));
+    out->count = sim->n;
+    if (sim->n == 0) return ASPH_OK;
+    double* d = nullptr;
+    asph_status st;
+    if ((st = dalloc(d, 6)) != ASPH_OK) return st;
+    CK(cudaMemsetAsync(d, 0, sizeof(double) * 6, sim->stream));
+    k_totals<<<blocks_for(sim->n), 256, 0, sim->stream>>>(sim->args(sim->cur), sim->pending_half,
+                                                          sim->has_pending ? 1 : 0, d, nullptr);
+    CK_LAUNCH("k_totals");
+    sim->launches++;
+    double h[6];
+    CK(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, sim->stream));
+    CK(cudaStreamSynchronize(sim->stream));
+    dfree(d);
+    out->mass = h[0];
+    out->momentum[0] = h[1];
+    out->momentum[1] = h[2];
+    out->momentum[2] = h[3];
+    out->kinetic_energy = h[4];
+    out->volume = h[5];
+    return ASPH_OK;
+}
+
+asph_status asph_simulation_step_cfl(asph_simulation* sim, float cfl, float dt_max, float* dt_used) {
+    if (!sim || !(cfl > 0.0f)) return fail(ASPH_ERR_INVALID_ARGUMENT, "simulation and cfl > 0 required");
+    float dt = dt_max > 0.0f ? dt_max : 3.402823466e38f;
+    if (sim->n > 0) {
+        double* d = nullptr;
+        asph_status st;
+        if ((st = dalloc(d, 8)) != ASPH_OK) return st;
+        CK(cudaMemsetAsync(d, 0, sizeof(double) * 8, sim->stream));
+        unsigned int* bits = reinterpret_cast<unsigned int*>(d + 6);
+        CK(cudaMemsetAsync(bits, 0x7f, sizeof(unsigned int), sim->stream));
+        k_totals<<<blocks_for(sim->n), 256, 0, sim->stream>>>(sim->args(sim->cur), sim->pending_half,
+                                                              sim->has_pending ? 1 : 0, d, bits);
+        CK_LAUNCH("k_totals");
+        sim->launches++;
+        unsigned int hb = 0;
+        CK(cudaMemcpyAsync(&hb, bits, sizeof(hb), cudaMemcpyDeviceToHost, sim->stream));
+        CK(cudaStreamSynchronize(sim->stream));
+        dfree(d);
+        float m;
+        std::memcpy(&m, &hb, sizeof(m));
+        const float c = cfl * m;
+        if (c < dt) dt = c;
+    }
+    if (!(dt < 3.0e38f)) return fail(ASPH_ERR_INVALID_ARGUMENT, "no particles and no dt_max");
+    if (dt_used) *dt_used = dt;
+    return asph_simulation_step_async(sim, dt);
+}
+
+asph_status asph_simulation_update_domain(asph_simulation* sim, const asph_domain* domain,
+                                          const asph_boundary_particle* boundary, uint32_t boundary_count) {
+    if (!sim || !domain) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
+    if (boundary_count > 0 && !boundary) return fail(ASPH_ERR_INVALID_ARGUMENT, "boundary particles are required");
+    CK(cudaStreamSynchronize(sim->stream));
+    asph_parameters P = sim->P;
+    P.domain = *domain;
+    GridDev g;
+    asph_status st = make_grid(P, g);
+    if (st != ASPH_OK) return st;
+    if (boundary_count > sim->ss.max_items)
+        return fail(ASPH_ERR_CAPACITY, "more boundary particles than the sort capacity of this simulation");
+    sim->P = P;
+    sim->grid = g;
+    if ((st = alloc_cells(sim)) != ASPH_OK) return st;
+    if ((st = setup_boundary(sim, boundary, boundary_count)) != ASPH_OK) return st;
+    sim->grid_valid = false;
+    return check_errors(sim, true);
+}
+
+asph_status asph_simulation_fluid_count(const asph_simulation* sim, uint32_t* out) {
+    if (!sim || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
+    *out = sim->n;
+    return ASPH_OK;
+}
+
+asph_status asph_simulation_boundary_count(const asph_simulation* sim, uint32_t* out) {
+    if (!sim || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
+    *out = sim->nb;
+    return ASPH_OK;
+}
+
+asph_status asph_simulation_neighbor_counts(asph_simulation* sim, uint32_t* counts, uint32_t capacity) {
+    if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
+    if (counts && capacity < sim->n) return fail(ASPH_ERR_CAPACITY, "counts array too small");
+    if (sim->n == 0) return ASPH_OK;
+    asph_status st;
+    if ((st = ensure_grid(sim)) != ASPH_OK) return st;
+    uint32_t* d = nullptr;
+    unsigned long long* tot = nullptr;
+    if ((st = dalloc(d, sim->n)) != ASPH_OK) return st;
+    if ((st = dalloc(tot, 1)) != ASPH_OK) {
+        dfree(d);
+        return st;
+    }
+    CK(cudaMemsetAsync(tot, 0, sizeof(unsigned long long), sim->stream));
+    k_neighbor_counts<<<blocks_for(sim->n), 256, 0, sim->stream>>>(sim->args(sim->cur), sim->cells(), d, tot);
+    CK_LAUNCH("k_neighbor_counts");
+    sim->launches++;
+    if (counts) CK(cudaMemcpyAsync(counts, d, sizeof(uint32_t) * sim->n, cudaMemcpyDeviceToHost, sim->stream));
+    CK(cudaStreamSynchronize(sim->stream));
+    dfree(d);
+    dfree(tot);
+    return ASPH_OK;
+}
+
+asph_status asph_simulation_average_neighbor_count(asph_simulation* sim, float* out) {
+    if (!sim || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
+    *out = 0.0f;
+    if (sim->n == 0) return ASPH_OK;
+    asph_status st;
+    if ((st = ensure_grid(sim)) != ASPH_OK) return st;
+    unsigned long long* tot = nullptr;
+    if ((st = dalloc(tot, 1)) != ASPH_OK) return st;
+    CK(cudaMemsetAsync(tot, 0, sizeof(unsigned long long), sim->stream));
+    k_neighbor_counts<<<blocks_for(sim->n), 256, 0, sim->stream>>>(sim->args(sim->cur), sim->cells(), nullptr, tot);
+    CK_LAUNCH("k_neighbor_counts");
+    sim->launches++;
+    unsigned long long h = 0;
+    CK(cudaMemcpyAsync(&h, tot, sizeof(h), cudaMemcpyDeviceToHost, sim->stream));
+    CK(cudaStreamSynchronize(sim->stream));
+    dfree(tot);
+    // the reference accumulates a uint32 total (SphSimulation.cu:237-247)
+    *out = (float)(uint32_t)h / (float)sim->n;
+    return ASPH_OK;
+}
+
+asph_status asph_simulation_density_info(asph_simulation* sim, float threshold, asph_density_info* out) {
+    if (!sim || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
+    std::memset(out, 0, sizeof(*out));
+    out->rest_density = sim->P.rest_density;
+    out->min_density = 3.402823466e38f;
+    out->max_density = -3.402823466e38f;
+    if (sim->n == 0) {
+        out->average_density = NAN;  // 0 / 0 as in the reference (SphSimulation.cu:283)
+        return ASPH_OK;
+    }
+    uint8_t* d = nullptr;
+    asph_status st;
+    if ((st = dalloc(d, 64)) != ASPH_OK) return st;
+    double* sum = reinterpret_cast<double*>(d);
+    unsigned int* mm = reinterpret_cast<unsigned int*>(d + 8);
+    unsigned int* cnt = reinterpret_cast<unsigned int*>(d + 16);
+    CK(cudaMemsetAsync(d, 0, 64, sim->stream));
+    CK(cudaMemsetAsync(mm, 0xff, sizeof(unsigned int), sim->stream));
+    k_density_info<<<blocks_for(sim->n), 256, 0, sim->stream>>>(sim->args(sim->cur), threshold, sim->P.rest_density,
+                                                                sum, mm, cnt);
+    CK_LAUNCH("k_density_info");
+    sim->launches++;
+    uint8_t h[64];
+    CK(cudaMemcpyAsync(h, d, 64, cudaMemcpyDeviceToHost, sim->stream));
+    CK(cudaStreamSynchronize(sim->stream));
+    dfree(d);
+    double hs;
+    unsigned int hm[2], hc[3];
+    std::memcpy(&hs, h, 8);
+    std::memcpy(hm, h + 8, 8);
+    std::memcpy(hc, h + 16, 12);
+    auto unmap = [](unsigned int s) {
+        const uint32_t u = (s & 0x80000000u) ? (s & 0x7fffffffu) : ~s;
+        float f;
+        std::memcpy(&f, &u, 4);
+        return f;
+    };
+    out->min_density = unmap(hm[0]);
+    out->max_density = unmap(hm[1]);
+    out->average_density = (float)(hs / (double)sim->n);
+    out->under_density_count = hc[0];
+    out->normal_density_count = hc[1];
+    out->over_density_count = hc[2];
+    return ASPH_OK;
+}
+
+asph_status asph_simulation_enable_adaptive_refinement(asph_simulation* sim) {
+    if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
+    if (sim->adaptive) sim->frame = sim->R.initial_cooldown;
+    return ASPH_OK;
+}
+
+asph_status asph_simulation_export(asph_simulation* sim) {
+    if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
+    if (!sim->have_fbuf) return ASPH_OK;
+    const asph_fluid_buffers& f = sim->fbuf;
+    const size_t n = sim->n;
+    auto ptr_if = [&](const asph_memory* m, size_t bytes) -> void* {
+        return (m && m->ptr && m->size >= bytes) ? m->ptr : nullptr;
+    };
+    if (n > 0) {
+        k_export<<<blocks_for(sim->n), 256, 0, sim->stream>>>(
+            sim->args(sim->cur), sim->pending_half, sim->has_pending ? 1 : 0,
+            static_cast<float4*>(ptr_if(f.positions, 16 * n)), static_cast<float4*>(ptr_if(f.velocities, 16 * n)),
+            static_cast<float*>(ptr_if(f.densities, 4 * n)), static_cast<float*>(ptr_if(f.radii, 4 * n)), nullptr);
+        CK_LAUNCH("k_export");
+        sim->launches++;
+    }
+    return check_errors(sim, true);
+}
+
+asph_status asph_simulation_export_host(asph_simulation* sim, float* positions, float* velocities, float* densities,
+                                        float* radii, uint32_t* ids, uint32_t capacity) {
+    if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
+    const uint32_t n = sim->n;
+    if (capacity < n) return fail(ASPH_ERR_CAPACITY, "host arrays too small");
+    if (n == 0) return ASPH_OK;
+    // stage through the spare half of the sort buffers' neighbours: a dedicated staging allocation
+    uint8_t* stage = nullptr;
+    const size_t bytes = (size_t)n * (16 + 16 + 4 + 4 + 4);
+    asph_status st;
+    if ((st = dalloc(stage, bytes)) != ASPH_OK) return st;
+    float4* dp = reinterpret_cast<float4*>(stage);
+    float4* dv = dp + n;
+    float* dr = reinterpret_cast<float*>(dv + n);
+    float* dd = dr + n;
+    uint32_t* di = reinterpret_cast<uint32_t*>(dd + n);
+    k_export<<<blocks_for(n), 256, 0, sim->stream>>>(sim->args(sim->cur), sim->pending_half, sim->has_pending ? 1 : 0,
+                                                      positions ? dp : nullptr, velocities ? dv : nullptr,
+                                                      densities ? dr : nullptr, radii ? dd : nullptr,
+                                                      ids ? di : nullptr);
+    CK_LAUNCH("k_export");
+    sim->launches++;
+    if (positions) CK(cudaMemcpyAsync(positions, dp, 16 * (size_t)n, cudaMemcpyDeviceToHost, sim->stream));
+    if (velocities) CK(cudaMemcpyAsync(velocities, dv, 16 * (size_t)n, cudaMemcpyDeviceToHost, sim->stream));
+    if (densities) CK(cudaMemcpyAsync(densities, dr, 4 * (size_t)n, cudaMemcpyDeviceToHost, sim->stream));
+    if (radii) CK(cudaMemcpyAsync(radii, dd, 4 * (size_t)n, cudaMemcpyDeviceToHost, sim->stream));
+    if (ids) CK(cudaMemcpyAsync(ids, di, 4 * (size_t)n, cudaMemcpyDeviceToHost, sim->stream));
+    CK(cudaStreamSynchronize(sim->stream));
+    dfree(stage);
+    return check_errors(sim, false);
+}
+
+asph_status asph_simulation_device_errors(asph_simulation* sim, uint32_t* out, int clear) {
+    if (!sim || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
+    CK(cudaStreamSynchronize(sim->stream));
+    CK(cudaMemcpy(sim->h_ctr, sim->err, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    *out = sim->h_ctr[0];
+    if (clear) CK(cudaMemset(sim->err, 0, sizeof(uint32_t)));
+    return ASPH_OK;
+}
+
+asph_status asph_simulation_set_stream(asph_simulation* sim, void* cuda_stream) {
+    if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
+    CK(cudaStreamSynchronize(sim->stream));
+    sim->stream = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : sim->own_stream;
+    return ASPH_OK;
+}
+
+asph_status asph_simulation_state_info(asph_simulation* sim, asph_state_info* out) {
+    if (!sim || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
+    out->count = sim->n;
+    out->capacity = sim->cap;
+    out->frame = sim->frame;
+    out->next_id = sim->next_id;
+    out->pending_half_dt = sim->pending_half;
+    out->has_pending = sim->has_pending ? 1u : 0u;
+    return ASPH_OK;
+}
+
+asph_status asph_simulation_read_fluid(asph_simulation* sim, float* positions, float* velocities,
+                                       float* accelerations, float* densities, float* radii, float* smoothing_radii,
+                                       float* masses, uint32_t* ids, uint32_t capacity) {
+    if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
+    const uint32_t n = sim->n;
+    if (capacity < n) return fail(ASPH_ERR_CAPACITY, "host arrays too small");
+    if (n == 0) return ASPH_OK;
+    uint8_t* stage = nullptr;
+    const size_t bytes = (size_t)n * (16 * 3 + 4 * 5);
+    asph_status st;
+    if ((st = dalloc(stage, bytes)) != ASPH_OK) return st;
+    float4* p = reinterpret_cast<float4*>(stage);
+    float4* v = p + n;
+    float4* a = v + n;
+    float* rho = reinterpret_cast<float*>(a + n);
+    float* rad = rho + n;
+    float* h = rad + n;
+    float* m = h + n;
+    uint32_t* id = reinterpret_cast<uint32_t*>(m + n);
+    k_read_state<<<blocks_for(n), 256, 0, sim->stream>>>(sim->args(sim->cur), p, v, a, rho, rad, h, m, id);
+    CK_LAUNCH("k_read_state");
+    sim->launches++;
+    struct Item {
+        void* dst;
+        const void* src;
+        size_t b;
+    } items[] = {{positions, p, 16}, {velocities, v, 16}, {accelerations, a, 16}, {densities, rho, 4},
+                 {radii, rad, 4},    {smoothing_radii, h, 4}, {masses, m, 4},    {ids, id, 4}};
+    for (auto& it : items)
+        if (it.dst) CK(cudaMemcpyAsync(it.dst, it.src, it.b * n, cudaMemcpyDeviceToHost, sim->stream));
+    CK(cudaStreamSynchronize(sim->stream));
+    dfree(stage);
+    return ASPH_OK;
+}
+
+asph_status asph_simulation_write_fluid(asph_simulation* sim, const asph_state_info* info, const float* positions,
+                                        const float* velocities, const float* accelerations, const float* densities,
+                                        const float* radii, const float* smoothing_radii, const float* masses,
+                                        const uint32_t* ids) {
+    if (!sim || !info) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
+    const uint32_t n = info->count;
+    if (n > sim->cap) return fail(ASPH_ERR_CAPACITY, "more particles than the fluid capacity");
+    if (n > 0 && (!positions || !velocities || !accelerations || !densities || !radii || !smoothing_radii ||
+                  !masses || !ids))
+        return fail(ASPH_ERR_INVALID_ARGUMENT, "all state arrays are required");
+    CK(cudaStreamSynchronize(sim->stream));
+    sim->n = n;
+    if (n > 0) {
+        uint8_t* stage = nullptr;
+        const size_t bytes = (size_t)n * (16 * 3 + 4 * 5);
+        asph_status st;
+        if ((st = dalloc(stage, bytes)) != ASPH_OK) return st;
+        float4* p = reinterpret_cast<float4*>(stage);
+        float4* v = p + n;
+        float4* a = v + n;
+        float* rho = reinterpret_cast<float*>(a + n);
+        float* rad = rho + n;
+        float* h = rad + n;
+        float* m = h + n;
+        uint32_t* id = reinterpret_cast<uint32_t*>(m + n);
+        struct Item {
+            void* dst;
+            const void* src;
+            size_t b;
+        } items[] = {{p, positions, 16}, {v, velocities, 16}, {a, accelerations, 16}, {rho, densities, 4},
+                     {rad, radii, 4},    {h, smoothing_radii, 4}, {m, masses, 4},     {id, ids, 4}};
+        for (auto& it : items) CK(cudaMemcpyAsync(it.dst, it.src, it.b * n, cudaMemcpyHostToDevice, sim->stream));
+        k_write_state<<<blocks_for(n), 256, 0, sim->stream>>>(sim->args(sim->cur), p, v, a, rho, rad, h, m, id);
+        CK_LAUNCH("k_write_state");
+        sim->launches++;
+        CK(cudaStreamSynchronize(sim->stream));
+        dfree(stage);
+    }
+    sim->frame = info->frame;
+    sim->next_id = info->next_id;
+    sim->pending_half = info->pending_half_dt;
+    sim->has_pending = info->has_pending != 0;
+    sim->grid_valid = false;
+    asph_status st = upload_count(sim);
+    if (st != ASPH_OK) return st;
+    return check_errors(sim, true);
+}
+
+asph_status asph_simulation_grid_info(asph_simulation* sim, asph_grid_info* out) {
+    if (!sim || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
+    for (int a = 0; a < 3; a++) {
+        out->reference_cells[a] = sim->grid.gs[a];
+        out->reference_cell_size[a] = sim->grid.cs[a];
+        out->sub_cells[a] = sim->grid.sgs[a];
+    }
+    out->cell_count = sim->grid.ncells;
+    out->key_bits = 3 * sim->grid.bits;
+    CK(cudaStreamSynchronize(sim->stream));
+    uint32_t ex[2];
+    CK(cudaMemcpy(ex, sim->ex, sizeof(ex), cudaMemcpyDeviceToHost));
+    out->excluded_cells[0] = ex[0];
+    out->excluded_cells[1] = ex[1];
+    out->boundary_excluded_cells[0] = sim->bex[0];
+    out->boundary_excluded_cells[1] = sim->bex[1];
+    return ASPH_OK;
+}
+
+asph_status asph_simulation_read_grid(asph_simulation* sim, uint32_t* keys, uint32_t key_capacity,
+                                      uint32_t* cell_start, uint32_t* cell_end, uint32_t cell_capacity) {
+    if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
+    CK(cudaStreamSynchronize(sim->stream));
+    if (keys) {
+        if (key_capacity < sim->n) return fail(ASPH_ERR_CAPACITY, "keys array too small");
+        if (sim->n) CK(cudaMemcpy(keys, sim->keys, sizeof(uint32_t) * sim->n, cudaMemcpyDeviceToHost));
+    }
+    if (cell_start || cell_end) {
+        if (cell_capacity < sim->grid.ncells) return fail(ASPH_ERR_CAPACITY, "cell arrays too small");
+        if (cell_start)
+            CK(cudaMemcpy(cell_start, sim->cell_start, sizeof(uint32_t) * sim->grid.ncells, cudaMemcpyDeviceToHost));
+        if (cell_end)
+            CK(cudaMemcpy(cell_end, sim->cell_end, sizeof(uint32_t) * sim->grid.ncells, cudaMemcpyDeviceToHost));
+    }
+    return ASPH_OK;
+}
+
+asph_status asph_simulation_last_refinement(asph_simulation* sim, asph_refinement_report* out) {
+    if (!sim || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
+    *out = sim->last_report;
+    return ASPH_OK;
+}
+
+asph_status asph_simulation_enable_timing(asph_simulation* sim, int enable) {
+    if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
+    CK(cudaStreamSynchronize(sim->stream));
+    sim->harvest();
+    for (int k = 0; k < (int)ASPH_KERNEL_COUNT; k++) {
+        sim->ms[k] = 0.0;
+        sim->timed[k] = 0;
+    }
+    sim->timing = enable != 0;
+    return ASPH_OK;
+}
+
+asph_status asph_simulation_kernel_times(asph_simulation* sim, double* ms, uint32_t* launches, uint32_t n) {
+    if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
+    CK(cudaStreamSynchronize(sim->stream));
+    sim->harvest();
+    for (uint32_t k = 0; k < n && k < ASPH_KERNEL_COUNT; k++) {
+        if (ms) ms[k] = sim->ms[k];
+        if (launches) launches[k] = sim->timed[k];
+    }
+    return ASPH_OK;
+}
+
+asph_status asph_simulation_launch_count(const asph_simulation* sim, uint64_t* out) {
+    if (!sim || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
+    *out = sim->launches;
+    return ASPH_OK;
+}
+
+}  // extern "C"
+
+// Records the ids of merged and split particles of each refinement pass (test hook, not in asph.h).
+extern "C" asph_status asph_debug_record_refinement(asph_simulation* sim, int enable) {
+    if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
+    if (enable && !sim->dbg_ids) {
+        asph_status st = dalloc(sim->dbg_ids, 3 * (size_t)sim->cap);
+        if (st != ASPH_OK) return st;
+    }
+    sim->record_ids = enable != 0 && sim->adaptive;
+    return ASPH_OK;
+}
+
+extern "C" asph_status asph_debug_refinement_ids(asph_simulation* sim, uint32_t* keep, uint32_t* removed,
+                                                 uint32_t* split, uint32_t capacity) {
+    if (!sim || !sim->dbg_ids) return fail(ASPH_ERR_INVALID_ARGUMENT, "recording not enabled");
+    CK(cudaStreamSynchronize(sim->stream));
+    const uint32_t np = sim->last_pairs_listed, ns = sim->last_splits_listed;
+    if (capacity < np || capacity < ns) return fail(ASPH_ERR_CAPACITY, "arrays too small");
+    if (keep && np) CK(cudaMemcpy(keep, sim->dbg_ids, 4 * (size_t)np, cudaMemcpyDeviceToHost));
+    if (removed && np) CK(cudaMemcpy(removed, sim->dbg_ids + sim->cap, 4 * (size_t)np, cudaMemcpyDeviceToHost));
+    if (split && ns) CK(cudaMemcpy(split, sim->dbg_ids + 2 * (size_t)sim->cap, 4 * (size_t)ns, cudaMemcpyDeviceToHost));
+    return ASPH_OK;
+}

@@ -1,0 +1,1209 @@
+/*
+ * asph_oracle.c — CPU restatement of AdaptiveSph's per-step particle pipeline.
+ * TEST INFRASTRUCTURE ONLY (the checker); see asph_oracle.h for scope and parity status.
+ *
+ * Build: gcc -O2 -fopenmp -ffp-contract=off -fno-fast-math -shared -fPIC (oracle/build.py). Contraction must
+ * stay off: the FP32 variant reproduces the CUDA kernels' explicit fmaf/mul/add sequence operation for
+ * operation.
+ */
+#include "asph_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ------------------------------------------------------------------ threads */
+void orc_set_threads(int n)
+{
+#ifdef _OPENMP
+    if (n > 0) {
+        omp_set_num_threads(n);
+    }
+#else
+    (void)n;
+#endif
+}
+
+int orc_get_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* ------------------------------------------------------------------ grid geometry */
+/* NeighborGrid::createGrid / calculateGridSize (cuda/src/simulation/neighbors/NeighborGrid.cu:108-121); cell
+ * width 2 * h0 * wendlandRangeRatio (cuda/src/simulation/SphSimulation.cu:46-49). Each reference cell is split
+ * into 2x2x2 sub-cells for the sort and the cell tables; the reference cells still define the candidate set. */
+void orc_grid_make(const orc_params* P, orc_grid* g)
+{
+    const float cw = (2.0f * P->h0) * 2.0f;
+    int32_t mx = 1;
+    g->ncells = 1;
+    for (int a = 0; a < 3; a++) {
+        g->dmin[a] = P->dmin[a];
+        g->dmax[a] = P->dmax[a];
+        g->scale[a] = P->dmax[a] - P->dmin[a];
+        int32_t gs = (int32_t)ceilf(g->scale[a] / cw);
+        if (gs < 1) {
+            gs = 1;
+        }
+        g->gs[a] = gs;
+        g->cs[a] = g->scale[a] / (float)gs;
+        g->sgs[a] = 2 * gs;
+        if (g->sgs[a] > mx) {
+            mx = g->sgs[a];
+        }
+        g->ncells *= (uint32_t)g->sgs[a];
+    }
+    uint32_t bits = 1;
+    while ((1 << bits) < mx) {
+        bits++;
+    }
+    g->bits = bits;
+    g->periodic = P->periodic;
+}
+
+static uint32_t part1by2(uint32_t x)
+{
+    x &= 0x3ffu;
+    x = (x | (x << 16)) & 0x030000ffu;
+    x = (x | (x << 8)) & 0x0300f00fu;
+    x = (x | (x << 4)) & 0x030c30c3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+
+static uint32_t compact1by2(uint32_t x)
+{
+    x &= 0x09249249u;
+    x = (x ^ (x >> 2)) & 0x030c30c3u;
+    x = (x ^ (x >> 4)) & 0x0300f00fu;
+    x = (x ^ (x >> 8)) & 0xff0000ffu;
+    x = (x ^ (x >> 16)) & 0x000003ffu;
+    return x;
+}
+
+uint32_t orc_morton3(uint32_t x, uint32_t y, uint32_t z)
+{
+    return part1by2(x) | (part1by2(y) << 1) | (part1by2(z) << 2);
+}
+
+static uint32_t lin_of_key(const orc_grid* g, uint32_t key)
+{
+    const uint32_t x = compact1by2(key), y = compact1by2(key >> 1), z = compact1by2(key >> 2);
+    return x + (uint32_t)g->sgs[0] * (y + (uint32_t)g->sgs[1] * z);
+}
+
+/* calculateCellIndex (cuda/src/simulation/neighbors/NeighborGrid.cuh:166-172) and flattenCellIndex (:174-177);
+ * the sub-cell index is floor(2 f) of the same f = clamp(x - min) / cellSize, so it always lies inside the
+ * reference cell floor(f). */
+void orc_cell_of(const orc_grid* g, const float* p, uint32_t* key, uint32_t* refkey, uint32_t* lin)
+{
+    int32_t rc[3], sc[3];
+    for (int a = 0; a < 3; a++) {
+        const float rel = p[a] - g->dmin[a];
+        float cl = rel < 0.0f ? 0.0f : rel;
+        cl = cl > g->scale[a] ? g->scale[a] : cl;
+        const float f = cl / g->cs[a];
+        int32_t c = (int32_t)f;
+        if (c > g->gs[a] - 1) {
+            c = g->gs[a] - 1;
+        }
+        int32_t s2 = (int32_t)(f * 2.0f);
+        if (s2 > g->sgs[a] - 1) {
+            s2 = g->sgs[a] - 1;
+        }
+        rc[a] = c;
+        sc[a] = s2;
+    }
+    if (key) {
+        *key = orc_morton3((uint32_t)sc[0], (uint32_t)sc[1], (uint32_t)sc[2]);
+    }
+    if (refkey) {
+        *refkey = (uint32_t)(rc[0] + g->gs[0] * (rc[1] + g->gs[1] * rc[2]));
+    }
+    if (lin) {
+        *lin = (uint32_t)(sc[0] + g->sgs[0] * (sc[1] + g->sgs[1] * sc[2]));
+    }
+}
+
+/* ------------------------------------------------------------------ neighbour-cell iterator */
+/* forEachFluidNeighbor / forEachBoundaryNeighbor (cuda/src/simulation/neighbors/NeighborGrid.cuh:90-164): the
+ * candidate cells are the reference cells overlapping [x - R, x + R] (truncated toward zero, clamped to the
+ * grid), minus the cells the reference's boundary pass leaves unset. They are visited here as their sub-cells
+ * in z, y, x order; members of a sub-cell in cell-sorted order. */
+typedef struct orc_iter {
+    const orc_grid* g;
+    const uint32_t *start, *end;
+    uint32_t ex0, ex1;
+    int32_t lo[3], hi[3], s[3];
+    int empty;
+} orc_iter;
+
+static float clampf(float x, float lo, float hi)
+{
+    x = x < lo ? lo : x;
+    return x > hi ? hi : x;
+}
+
+static void it_init(orc_iter* it, const orc_grid* g, const uint32_t* start, const uint32_t* end,
+                    const uint32_t ex[2], const float* p, float R)
+{
+    it->g = g;
+    it->start = start;
+    it->end = end;
+    it->ex0 = ex[0];
+    it->ex1 = ex[1];
+    it->empty = 0;
+    for (int a = 0; a < 3; a++) {
+        const float rel = p[a] - g->dmin[a];
+        const float lof = clampf((rel - R) / g->cs[a], -1.0e7f, 1.0e7f);
+        const float hif = clampf((rel + R) / g->cs[a], -1.0e7f, 1.0e7f);
+        int32_t l, h;
+        if (!g->periodic) {
+            l = (int32_t)lof;
+            h = (int32_t)hif;
+            if (l < 0) {
+                l = 0;
+            }
+            if (h > g->gs[a] - 1) {
+                h = g->gs[a] - 1;
+            }
+        } else {
+            l = (int32_t)floorf(lof);
+            h = (int32_t)floorf(hif);
+            if (h - l + 1 > g->gs[a]) {
+                h = l + g->gs[a] - 1;
+            }
+        }
+        if (l > h) {
+            it->empty = 1;
+        }
+        it->lo[a] = 2 * l;
+        it->hi[a] = 2 * h + 1;
+    }
+    it->s[0] = it->lo[0] - 1;
+    it->s[1] = it->lo[1];
+    it->s[2] = it->lo[2];
+}
+
+static int it_next(orc_iter* it, uint32_t* b, uint32_t* e, float sh[3])
+{
+    const orc_grid* g = it->g;
+    if (it->empty) {
+        return 0;
+    }
+    for (;;) {
+        if (++it->s[0] > it->hi[0]) {
+            it->s[0] = it->lo[0];
+            if (++it->s[1] > it->hi[1]) {
+                it->s[1] = it->lo[1];
+                if (++it->s[2] > it->hi[2]) {
+                    it->empty = 1;
+                    return 0;
+                }
+            }
+        }
+        int32_t c[3];
+        for (int a = 0; a < 3; a++) {
+            c[a] = it->s[a];
+            sh[a] = 0.0f;
+            if (g->periodic) {
+                if (c[a] < 0) {
+                    c[a] += g->sgs[a];
+                    sh[a] = -g->scale[a];
+                } else if (c[a] >= g->sgs[a]) {
+                    c[a] -= g->sgs[a];
+                    sh[a] = g->scale[a];
+                }
+            }
+        }
+        if (!g->periodic) {
+            const uint32_t rk =
+                (uint32_t)((c[0] >> 1) + g->gs[0] * ((c[1] >> 1) + g->gs[1] * (c[2] >> 1)));
+            if (rk == it->ex0 || rk == it->ex1) {
+                continue;
+            }
+        } else if (c[0] < 0 || c[0] >= g->sgs[0] || c[1] < 0 || c[1] >= g->sgs[1] || c[2] < 0 ||
+                   c[2] >= g->sgs[2]) {
+            continue;
+        }
+        const uint32_t lin = (uint32_t)(c[0] + g->sgs[0] * (c[1] + g->sgs[1] * c[2]));
+        if (it->start[lin] == ORC_EMPTY) {
+            continue;
+        }
+        *b = it->start[lin];
+        *e = it->end[lin];
+        return 1;
+    }
+}
+
+/* ------------------------------------------------------------------ sort, cells, quirk */
+/* Stable LSD radix sort, 8-bit digits (thrust::sort_by_key on int keys is a stable radix sort,
+ * cuda/src/simulation/neighbors/NeighborGrid.cu:139-145). */
+void orc_sort_stable(uint32_t n, const uint32_t* key, uint32_t bits, uint32_t* perm)
+{
+    uint32_t* tmp = (uint32_t*)malloc(sizeof(uint32_t) * (n ? n : 1));
+    for (uint32_t i = 0; i < n; i++) {
+        perm[i] = i;
+    }
+    for (uint32_t shift = 0; shift < bits; shift += 8) {
+        uint32_t cnt[257];
+        memset(cnt, 0, sizeof(cnt));
+        for (uint32_t i = 0; i < n; i++) {
+            cnt[((key[perm[i]] >> shift) & 0xffu) + 1]++;
+        }
+        for (int d = 0; d < 256; d++) {
+            cnt[d + 1] += cnt[d];
+        }
+        for (uint32_t i = 0; i < n; i++) {
+            tmp[cnt[(key[perm[i]] >> shift) & 0xffu]++] = perm[i];
+        }
+        memcpy(perm, tmp, sizeof(uint32_t) * n);
+    }
+    free(tmp);
+}
+
+/* calculateCellStartAndEndIndices (cuda/src/algorithm/neighbors/NeighborKernels.cu:17-44): thread 0 returns
+ * before comparing key[0] with key[1], so when the first two particles of the reference's sorted order lie in
+ * different cells, neither cell gets a valid [start, end] and both are skipped by every neighbour query; with
+ * one particle its cell is skipped. The reference sorts (cell, array slot); slot order is id order here. */
+void orc_excluded_cells(uint32_t n, const uint32_t* refkey, const uint32_t* slot, uint32_t ex[2])
+{
+    ex[0] = ORC_NONE;
+    ex[1] = ORC_NONE;
+    if (n == 0) {
+        return;
+    }
+    uint64_t S = ~0ull, T = ~0ull;
+    for (uint32_t i = 0; i < n; i++) {
+        const uint64_t v = ((uint64_t)refkey[i] << 32) | slot[i];
+        if (v < S) {
+            T = S;
+            S = v;
+        } else if (v < T) {
+            T = v;
+        }
+    }
+    if (n == 1) {
+        ex[0] = (uint32_t)(S >> 32);
+        return;
+    }
+    if ((S >> 32) != (T >> 32)) {
+        ex[0] = (uint32_t)(S >> 32);
+        ex[1] = (uint32_t)(T >> 32);
+    }
+}
+
+void orc_cells_from_keys(const orc_grid* g, uint32_t n, const uint32_t* keys, uint32_t* start, uint32_t* end)
+{
+    for (uint32_t c = 0; c < g->ncells; c++) {
+        start[c] = ORC_EMPTY;
+        end[c] = 0;
+    }
+    for (uint32_t k = 0; k < n; k++) {
+        const uint32_t lin = lin_of_key(g, keys[k]);
+        if (k == 0 || keys[k] != keys[k - 1]) {
+            start[lin] = k;
+        }
+        if (k + 1 == n || keys[k] != keys[k + 1]) {
+            end[lin] = k + 1;
+        }
+    }
+}
+
+static void permute_f(float* a, const uint32_t* perm, uint32_t n, int width, float* tmp)
+{
+    for (uint32_t k = 0; k < n; k++) {
+        memcpy(tmp + (size_t)width * k, a + (size_t)width * perm[k], sizeof(float) * width);
+    }
+    memcpy(a, tmp, sizeof(float) * width * n);
+}
+
+void orc_grid_build(const orc_grid* g, orc_state* s, orc_cells* c)
+{
+    const uint32_t n = s->n;
+    const size_t nn = n ? n : 1;
+    uint32_t* keys = (uint32_t*)malloc(sizeof(uint32_t) * nn);
+    uint32_t* refk = (uint32_t*)malloc(sizeof(uint32_t) * nn);
+    uint32_t* perm = (uint32_t*)malloc(sizeof(uint32_t) * nn);
+    float* tmp = (float*)malloc(sizeof(float) * 4 * nn);
+    for (uint32_t i = 0; i < n; i++) {
+        orc_cell_of(g, s->pos + 4 * (size_t)i, &keys[i], &refk[i], NULL);
+    }
+    if (!g->periodic) {
+        orc_excluded_cells(n, refk, s->id, c->ex);
+    } else {
+        c->ex[0] = c->ex[1] = ORC_NONE;
+    }
+    orc_sort_stable(n, keys, 3 * g->bits, perm);
+    permute_f(s->pos, perm, n, 4, tmp);
+    permute_f(s->vel, perm, n, 4, tmp);
+    permute_f(s->acc, perm, n, 4, tmp);
+    permute_f(s->rho, perm, n, 1, tmp);
+    permute_f(s->rad, perm, n, 1, tmp);
+    permute_f(s->h, perm, n, 1, tmp);
+    permute_f(s->m, perm, n, 1, tmp);
+    {
+        uint32_t* t = (uint32_t*)tmp;
+        for (uint32_t k = 0; k < n; k++) {
+            t[k] = s->id[perm[k]];
+        }
+        memcpy(s->id, t, sizeof(uint32_t) * n);
+    }
+    for (uint32_t k = 0; k < n; k++) {
+        c->keys[k] = keys[perm[k]];
+    }
+    orc_cells_from_keys(g, n, c->keys, c->start, c->end);
+    free(keys);
+    free(refk);
+    free(perm);
+    free(tmp);
+}
+
+void orc_boundary_setup(const orc_grid* g, uint32_t n, const float* pos4, const float* psi, float friction,
+                        orc_boundary* b)
+{
+    const size_t nn = n ? n : 1;
+    uint32_t* keys = (uint32_t*)malloc(sizeof(uint32_t) * nn);
+    uint32_t* refk = (uint32_t*)malloc(sizeof(uint32_t) * nn);
+    uint32_t* slot = (uint32_t*)malloc(sizeof(uint32_t) * nn);
+    uint32_t* perm = (uint32_t*)malloc(sizeof(uint32_t) * nn);
+    for (uint32_t i = 0; i < n; i++) {
+        orc_cell_of(g, pos4 + 4 * (size_t)i, &keys[i], &refk[i], NULL);
+        slot[i] = i;
+    }
+    if (!g->periodic) {
+        orc_excluded_cells(n, refk, slot, b->ex);
+    } else {
+        b->ex[0] = b->ex[1] = ORC_NONE;
+    }
+    orc_sort_stable(n, keys, 3 * g->bits, perm);
+    for (uint32_t k = 0; k < n; k++) {
+        memcpy(b->pos + 4 * (size_t)k, pos4 + 4 * (size_t)perm[k], sizeof(float) * 4);
+        b->psi[k] = psi[perm[k]];
+        b->fric[k] = friction;
+        slot[k] = keys[perm[k]];
+    }
+    b->n = n;
+    orc_cells_from_keys(g, n, slot, b->start, b->end);
+    free(keys);
+    free(refk);
+    free(slot);
+    free(perm);
+}
+
+/* ------------------------------------------------------------------ cube root */
+/* Cube root by Newton-Raphson on y^3 = a in double precision: x = m * 2^e with the exponent split as
+ * e = 3k + r, six iterations y <- (2y + a/y^2)/3 from y = 1 on a = m * 2^r in [0.5, 4), then y * 2^k rounded
+ * to float. Only basic IEEE operations, so the CUDA kernels and this oracle produce the same bits. */
+float orc_cbrtf(float xf)
+{
+    if (xf == 0.0f || !(xf == xf) || xf == INFINITY || xf == -INFINITY) {
+        return xf;
+    }
+    const int neg = xf < 0.0f;
+    double x = neg ? -(double)xf : (double)xf;
+    int e;
+    double m = frexp(x, &e);
+    int k = e >= 0 ? e / 3 : -((-e + 2) / 3);
+    int r = e - 3 * k;
+    const double a = ldexp(m, r);
+    double y = 1.0;
+    for (int it = 0; it < 6; it++) {
+        y = ((y + y) + a / (y * y)) / 3.0;
+    }
+    y = ldexp(y, k);
+    const float out = (float)y;
+    return neg ? -out : out;
+}
+
+/* ------------------------------------------------------------------ FP32 / FP64 bodies */
+static const float ORC_PI_F = 3.141592653589793f;
+
+#define REAL float
+#define F(name) name##_f32
+#define FMA fmaf
+#define SQRT sqrtf
+#define WCOEF (21.0f / (16.0f * ORC_PI_F))
+#define DCOEF (-5.0f * (21.0f / (16.0f * ORC_PI_F)))
+#include "oracle_body.h"
+#undef REAL
+#undef F
+#undef FMA
+#undef SQRT
+#undef WCOEF
+#undef DCOEF
+#undef NBR
+
+#define REAL double
+#define F(name) name##_f64
+#define FMA fma
+#define SQRT sqrt
+#define WCOEF (21.0 / (16.0 * 3.14159265358979323846))
+#define DCOEF (-5.0 * (21.0 / (16.0 * 3.14159265358979323846)))
+#include "oracle_body.h"
+#undef REAL
+#undef F
+#undef FMA
+#undef SQRT
+#undef WCOEF
+#undef DCOEF
+#undef NBR
+
+void orc32_density(const orc_grid* g, const orc_params* P, const orc_state* s, const orc_cells* c,
+                   const orc_boundary* b, float* rho_out)
+{
+    orc_density_impl_f32(g, P, s, c, b, rho_out);
+}
+
+void orc64_density(const orc_grid* g, const orc_params* P, const orc_state* s, const orc_cells* c,
+                   const orc_boundary* b, double* rho_out)
+{
+    orc_density_impl_f64(g, P, s, c, b, rho_out);
+}
+
+void orc32_forces(const orc_grid* g, const orc_params* P, const orc_state* s, const orc_cells* c,
+                  const orc_boundary* b, float* acc_out)
+{
+    orc_forces_impl_f32(g, P, s, c, b, s->rho, acc_out, NULL);
+}
+
+void orc64_forces(const orc_grid* g, const orc_params* P, const orc_state* s, const orc_cells* c,
+                  const orc_boundary* b, double* acc_out, double* scale_out)
+{
+    orc_forces_impl_f64(g, P, s, c, b, s->rho, acc_out, scale_out);
+}
+
+/* sumAllNeighbors per particle (cuda/src/algorithm/Algorithm.cu:234-268) */
+void orc_neighbor_counts(const orc_grid* g, const orc_state* s, const orc_cells* c, uint32_t* counts)
+{
+    const int64_t n = s->n;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < n; i++) {
+        const float* pi = s->pos + 4 * i;
+        const float R = s->h[i] + s->h[i];
+        uint32_t cnt = 0;
+        orc_iter it;
+        uint32_t jb, je;
+        float sh[3];
+        it_init(&it, g, c->start, c->end, c->ex, pi, R);
+        while (it_next(&it, &jb, &je, sh)) {
+            for (uint32_t j = jb; j < je; j++) {
+                if ((int64_t)j == i) {
+                    continue;
+                }
+                const float* pj = s->pos + 4 * (size_t)j;
+                const float dx = (g->periodic ? pj[0] + sh[0] : pj[0]) - pi[0];
+                const float dy = (g->periodic ? pj[1] + sh[1] : pj[1]) - pi[1];
+                const float dz = (g->periodic ? pj[2] + sh[2] : pj[2]) - pi[2];
+                const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                const float twoh = s->h[j] + s->h[j];
+                if (r2 <= twoh * twoh) {
+                    cnt++;
+                }
+            }
+        }
+        counts[i] = cnt;
+    }
+}
+
+/* ------------------------------------------------------------------ integrator */
+/* halfKickVelocities (cuda/src/algorithm/Algorithm.cu:270-284) */
+static void kick32(float* v, const float* a, float hdt, float maxv)
+{
+    v[0] = fmaf(a[0], hdt, v[0]);
+    v[1] = fmaf(a[1], hdt, v[1]);
+    v[2] = fmaf(a[2], hdt, v[2]);
+    const float len = sqrtf(fmaf(v[2], v[2], fmaf(v[1], v[1], v[0] * v[0])));
+    if (len > maxv) {
+        const float sc = maxv / len;
+        v[0] = v[0] * sc;
+        v[1] = v[1] * sc;
+        v[2] = v[2] * sc;
+    }
+}
+
+/* The closing half-kick of the previous step is applied here, just before the opening half-kick of this
+ * step, then the drift and the domain clamp (updatePositions, Algorithm.cu:286-298); the reference runs the
+ * same two kicks as separate kernels at the end and the start of consecutive steps. */
+void orc32_integrate(orc_state* s, const orc_params* P, float dt)
+{
+    const float half = dt / 2.0f;
+    const int64_t n = s->n;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; i++) {
+        float* v = s->vel + 4 * i;
+        const float* a = s->acc + 4 * i;
+        float* x = s->pos + 4 * i;
+        if (s->has_pending) {
+            kick32(v, a, s->pending_half, P->max_velocity);
+        }
+        kick32(v, a, half, P->max_velocity);
+        v[3] = 0.0f;
+        for (int c = 0; c < 3; c++) {
+            float xc = fmaf(v[c], dt, x[c]);
+            if (!P->periodic) {
+                xc = xc < P->dmin[c] ? P->dmin[c] : xc;
+                xc = xc > P->dmax[c] ? P->dmax[c] : xc;
+            } else {
+                const float L = P->dmax[c] - P->dmin[c];
+                if (xc < P->dmin[c]) {
+                    xc = xc + L;
+                } else if (xc >= P->dmax[c]) {
+                    xc = xc - L;
+                }
+            }
+            x[c] = xc;
+        }
+    }
+    s->has_pending = 0;
+}
+
+void orc32_export_velocities(const orc_params* P, const orc_state* s, float* vel4_out)
+{
+    for (uint32_t i = 0; i < s->n; i++) {
+        float v[4] = {s->vel[4 * i], s->vel[4 * i + 1], s->vel[4 * i + 2], 0.0f};
+        if (s->has_pending) {
+            kick32(v, s->acc + 4 * (size_t)i, s->pending_half, P->max_velocity);
+        }
+        memcpy(vel4_out + 4 * (size_t)i, v, sizeof(v));
+    }
+}
+
+void orc_totals(const orc_params* P, const orc_state* s, double out[6])
+{
+    double M = 0, px = 0, py = 0, pz = 0, ke = 0;
+    for (uint32_t i = 0; i < s->n; i++) {
+        float v[4] = {s->vel[4 * i], s->vel[4 * i + 1], s->vel[4 * i + 2], 0.0f};
+        if (s->has_pending) {
+            kick32(v, s->acc + 4 * (size_t)i, s->pending_half, P->max_velocity);
+        }
+        const double m = s->m[i];
+        M += m;
+        px += m * v[0];
+        py += m * v[1];
+        pz += m * v[2];
+        ke += 0.5 * m * ((double)v[0] * v[0] + (double)v[1] * v[1] + (double)v[2] * v[2]);
+    }
+    out[0] = M;
+    out[1] = px;
+    out[2] = py;
+    out[3] = pz;
+    out[4] = ke;
+    out[5] = (double)s->n;
+}
+
+/* ------------------------------------------------------------------ refinement */
+static uint32_t sortable_f(float f)
+{
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+static int cmp_u64(const void* a, const void* b)
+{
+    const uint64_t x = *(const uint64_t*)a, y = *(const uint64_t*)b;
+    return x < y ? -1 : (x > y ? 1 : 0);
+}
+
+/* checkIfParticleCanBeSplitInsideDomain (cuda/src/simulation/refinement/criteria/Common.cuh:6-20) */
+static int inside_domain(const orc_params* P, const float* p, float h, float eps)
+{
+    const float mo = eps * h;
+    if (p[0] - mo < P->dmin[0] || p[0] + mo > P->dmax[0] || p[1] - mo < P->dmin[1] || p[1] + mo > P->dmax[1] ||
+        p[2] - mo < P->dmin[2] || p[2] + mo > P->dmax[2]) {
+        return 0;
+    }
+    return 1;
+}
+
+/* velocity-gradient sum of VorticityCriterion.cuh:198-229 (search radius h_i); returns |curl v| or -1 when
+ * fewer than 4 neighbours qualify */
+static float vorticity_mag(const orc_grid* g, const orc_state* s, const orc_cells* c, uint32_t i)
+{
+    const float* pi = s->pos + 4 * (size_t)i;
+    const float* vi = s->vel + 4 * (size_t)i;
+    const float hi = s->h[i];
+    float invh, wc, dwc;
+    kernel_consts_f32(hi, &invh, &wc, &dwc);
+    float d[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    int valid = 0;
+    orc_iter it;
+    uint32_t jb, je;
+    float sh[3];
+    it_init(&it, g, c->start, c->end, c->ex, pi, hi);
+    while (it_next(&it, &jb, &je, sh)) {
+        for (uint32_t j = jb; j < je; j++) {
+            if (j == i) {
+                continue;
+            }
+            const float* pj = s->pos + 4 * (size_t)j;
+            const float rx = pj[0] - pi[0], ry = pj[1] - pi[1], rz = pj[2] - pi[2];
+            const float dist = sqrtf(fmaf(rz, rz, fmaf(ry, ry, rx * rx)));
+            if (dist < hi && dist > 1e-6f) {
+                const float* vj = s->vel + 4 * (size_t)j;
+                const float vd[3] = {vj[0] - vi[0], vj[1] - vi[1], vj[2] - vi[2]};
+                const float gw = kernel_dw_f32(dist, invh, dwc);
+                const float w = s->m[j] / s->rho[j];
+                const float gd[3] = {rx / dist, ry / dist, rz / dist};
+                for (int a = 0; a < 3; a++) {
+                    for (int bb = 0; bb < 3; bb++) {
+                        d[3 * a + bb] = fmaf((w * vd[a]) * gd[bb], gw, d[3 * a + bb]);
+                    }
+                }
+                valid++;
+            }
+        }
+    }
+    if (valid < 4) {
+        return -1.0f;
+    }
+    /* d[3a+b] = dv_a/dx_b ; omega = (dvz/dy - dvy/dz, dvx/dz - dvz/dx, dvy/dx - dvx/dy) */
+    const float ox = d[7] - d[5], oy = d[2] - d[6], oz = d[3] - d[1];
+    return sqrtf(fmaf(oz, oz, fmaf(oy, oy, ox * ox)));
+}
+
+/* calculateMinSurfaceDistance (InterfaceCriterion.cuh:52-67) */
+static void min_surface_distance(const orc_params* P, const float* p, float out[3])
+{
+    for (int a = 0; a < 3; a++) {
+        const float lo = p[a] - P->dmin[a];
+        const float hi = P->dmax[a] - p[a];
+        const float m = hi < lo ? hi : lo;
+        out[a] = m < 0.0f ? 0.0f : m;
+    }
+}
+
+static float compmin3(const float v[3])
+{
+    float m = v[0];
+    m = v[1] < m ? v[1] : m;
+    m = v[2] < m ? v[2] : m;
+    return m;
+}
+
+/* merge criterion generators: VelocityCriterion.cuh:208-227, InterfaceCriterion.cuh:97-115,
+ * VorticityCriterion.cuh:248-312 */
+static float merge_score(const orc_grid* g, const orc_params* P, const orc_refine* R, const orc_state* s,
+                         const orc_cells* c, uint32_t i, float maxMass)
+{
+    if (s->m[i] > maxMass) {
+        return -1.0f;
+    }
+    const float* p = s->pos + 4 * (size_t)i;
+    if (R->criterion == 1u) {
+        float md[3], nd[3];
+        min_surface_distance(P, p, md);
+        for (int a = 0; a < 3; a++) {
+            nd[a] = md[a] / (R->iface_merge * (P->dmax[a] - P->dmin[a]));
+        }
+        return compmin3(nd) - 1.0f;
+    }
+    if (R->criterion == 2u) {
+        const float mag = vorticity_mag(g, s, c, i);
+        if (mag < 0.0f) {
+            return -1.0f;
+        }
+        if (mag < R->vort_merge) {
+            return mag / R->vort_merge;
+        }
+        return -1.0f;
+    }
+    const float* v = s->vel + 4 * (size_t)i;
+    const float sp = sqrtf(fmaf(v[2], v[2], fmaf(v[1], v[1], v[0] * v[0])));
+    if (sp < R->vel_merge) {
+        return sp / R->vel_merge;
+    }
+    return -1.0f;
+}
+
+/* split criterion generators: VelocityCriterion.cuh:180-206, InterfaceCriterion.cuh:69-95,
+ * VorticityCriterion.cuh:170-246 */
+static float split_score(const orc_grid* g, const orc_params* P, const orc_refine* R, const orc_state* s,
+                         const orc_cells* c, uint32_t i, float minMass)
+{
+    if (s->m[i] < minMass) {
+        return -1.0f;
+    }
+    const float* p = s->pos + 4 * (size_t)i;
+    const float h = s->h[i];
+    if (R->criterion == 1u) {
+        float md[3], nd[3];
+        min_surface_distance(P, p, md);
+        if (compmin3(md) < R->eps * h) {
+            return -1.0f;
+        }
+        for (int a = 0; a < 3; a++) {
+            nd[a] = md[a] / (R->iface_split * (P->dmax[a] - P->dmin[a]));
+        }
+        return 1.0f - compmin3(nd);
+    }
+    if (!inside_domain(P, p, h, R->eps)) {
+        return -1.0f;
+    }
+    if (R->criterion == 2u) {
+        const float mag = vorticity_mag(g, s, c, i);
+        if (mag < 0.0f) {
+            return -1.0f;
+        }
+        return mag > R->vort_split ? mag : -1.0f;
+    }
+    const float* v = s->vel + 4 * (size_t)i;
+    const float sp = sqrtf(fmaf(v[2], v[2], fmaf(v[1], v[1], v[0] * v[0])));
+    if (sp < R->vel_split) {
+        return -1.0f;
+    }
+    return sp;
+}
+
+/* identifyMergeCandidates (cuda/src/algorithm/AdaptiveAlgorithm.cu:159-206): nearest neighbour with
+ * r^2 < min(h_i,h_j)^2 and m_j < maxMass within the cells of [x - h_i, x + h_i]. Exact r^2 ties go to the
+ * smaller id (the reference keeps the first one its loop meets). */
+static uint32_t merge_candidate(const orc_grid* g, const orc_state* s, const orc_cells* c, uint32_t e,
+                                float maxMass)
+{
+    const float* pe = s->pos + 4 * (size_t)e;
+    const float he = s->h[e];
+    float best = 3.402823466e38f;
+    uint32_t bj = ORC_NONE;
+    orc_iter it;
+    uint32_t jb, je;
+    float sh[3];
+    it_init(&it, g, c->start, c->end, c->ex, pe, he);
+    while (it_next(&it, &jb, &je, sh)) {
+        for (uint32_t j = jb; j < je; j++) {
+            if (j == e) {
+                continue;
+            }
+            const float* pj = s->pos + 4 * (size_t)j;
+            const float dx = pj[0] - pe[0], dy = pj[1] - pe[1], dz = pj[2] - pe[2];
+            const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            const float hj = s->h[j];
+            const float hm = hj < he ? hj : he;
+            if (r2 < hm * hm && s->m[j] < maxMass) {
+                if (r2 < best || (r2 == best && s->id[j] < s->id[bj])) {
+                    best = r2;
+                    bj = j;
+                }
+            }
+        }
+    }
+    return bj;
+}
+
+static const float ORC_PHI_F = 1.6180339887498949f;
+static const float ORC_INVNORM_F = 0.5257311121f;
+
+/* icosahedronVertices (cuda/src/algorithm/AdaptiveAlgorithm.cu:35-48), same order */
+static void icosahedron(float v[12][3])
+{
+    const float A = ORC_PHI_F * ORC_INVNORM_F, B = ORC_INVNORM_F;
+    const float t[12][3] = {{0.0f, A, B},  {0.0f, A, -B},  {0.0f, -A, -B}, {0.0f, -A, B},
+                            {B, 0.0f, A},  {-B, 0.0f, A},  {B, 0.0f, -A},  {-B, 0.0f, -A},
+                            {A, B, 0.0f},  {A, -B, 0.0f},  {-A, B, 0.0f},  {-A, -B, 0.0f}};
+    memcpy(v, t, sizeof(t));
+}
+
+/* performMerges + calculateMergedSmoothingLength (cuda/src/algorithm/AdaptiveAlgorithm.cu:50-67, 236-275) */
+static void merge_pair(const orc_params* P, orc_state* s, uint32_t i, uint32_t c)
+{
+    const float m1 = s->m[i], m2 = s->m[c];
+    const float M = m1 + m2;
+    float np[3], nv[3], na[3];
+    for (int a = 0; a < 3; a++) {
+        np[a] = fmaf(m1, s->pos[4 * (size_t)i + a], m2 * s->pos[4 * (size_t)c + a]) / M;
+        nv[a] = fmaf(m1, s->vel[4 * (size_t)i + a], m2 * s->vel[4 * (size_t)c + a]) / M;
+        na[a] = fmaf(m1, s->acc[4 * (size_t)i + a], m2 * s->acc[4 * (size_t)c + a]) / M;
+    }
+    float d[2], W[2];
+    const uint32_t idx[2] = {i, c};
+    for (int k = 0; k < 2; k++) {
+        const float* p = s->pos + 4 * (size_t)idx[k];
+        const float dx = p[0] - np[0], dy = p[1] - np[1], dz = p[2] - np[2];
+        d[k] = sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
+        float invh, wc, dwc;
+        kernel_consts_f32(s->h[idx[k]], &invh, &wc, &dwc);
+        W[k] = kernel_w_f32(d[k], invh, wc);
+    }
+    const float denom = fmaf(m1, W[0], m2 * W[1]);
+    const float coef = (16.0f * ORC_PI_F) / 21.0f;
+    const float hn = orc_cbrtf((coef * M) / denom);
+    const float rn = P->r0 * orc_cbrtf(M / P->m0);
+    for (int a = 0; a < 3; a++) {
+        s->pos[4 * (size_t)i + a] = np[a];
+        s->vel[4 * (size_t)i + a] = nv[a];
+        s->acc[4 * (size_t)i + a] = na[a];
+    }
+    s->pos[4 * (size_t)i + 3] = 0.0f;
+    s->vel[4 * (size_t)i + 3] = 0.0f;
+    s->acc[4 * (size_t)i + 3] = 0.0f;
+    s->m[i] = M;
+    s->rad[i] = rn;
+    s->h[i] = hn;
+    s->rho[i] = 0.0f;
+}
+
+/* splitParticles (cuda/src/algorithm/AdaptiveAlgorithm.cu:69-117) with daughters at base .. base+11 */
+static void split_one(const orc_refine* R, orc_state* s, uint32_t p, uint32_t base, uint32_t base_id)
+{
+    float ico[12][3];
+    icosahedron(ico);
+    const float m = s->m[p], r = s->rad[p], h = s->h[p];
+    const float dm = m * R->vertex_ratio, cm = m * R->center_ratio;
+    const float nr = r * orc_cbrtf(dm / m);
+    const float nh = R->alpha * h;
+    float x[4], v[4], a[4];
+    memcpy(x, s->pos + 4 * (size_t)p, sizeof(x));
+    memcpy(v, s->vel + 4 * (size_t)p, sizeof(v));
+    memcpy(a, s->acc + 4 * (size_t)p, sizeof(a));
+    s->m[p] = cm;
+    s->rad[p] = r * orc_cbrtf(cm / m);
+    s->h[p] = nh;
+    for (uint32_t k = 0; k < 12; k++) {
+        const size_t q = base + k;
+        for (int c = 0; c < 3; c++) {
+            s->pos[4 * q + c] = x[c] + (ico[k][c] * R->eps) * h;
+        }
+        s->pos[4 * q + 3] = x[3];
+        memcpy(s->vel + 4 * q, v, sizeof(v));
+        memcpy(s->acc + 4 * q, a, sizeof(a));
+        s->m[q] = dm;
+        s->rad[q] = nr;
+        s->h[q] = nh;
+        s->rho[q] = 0.0f;
+        s->id[q] = base_id + k;
+    }
+}
+
+/* One refinement pass: performAdaptiveRefinement (cuda/src/simulation/AdaptiveSphSimulation.cu:102-113) with
+ * identifyAndMergeParticles (:195-252) then, if particles were removed, identifyAndSplitParticles (:135-193).
+ * Selection follows findTopParticlesToMerge/ToSplit (AdaptiveAlgorithm.cuh:56-131): stable sort of
+ * (score, array slot) ascending for merge, descending for split; k = min(#score > 0, round(N*maxBatchRatio)).
+ * Merge: non-eligible particles keep the reset candidate value 0, i.e. the particle in slot 0; pairs are
+ * mutual candidates, the lower slot keeps. Split: the device count k bounds the kernel while the launch covers
+ * ceil(budget/threadsPerBlock) blocks, budget = min(k, removed/12). Daughters are appended in split order. */
+void orc32_refine(const orc_grid* g, const orc_params* P, const orc_refine* R, orc_state* s, orc_cells* c,
+                  orc_report* rep)
+{
+    orc_report local;
+    if (rep == NULL) {
+        memset(&local, 0, sizeof(local));
+        rep = &local;
+    }
+    const uint32_t n = s->n;
+    rep->frame = s->frame;
+    rep->count_before = n;
+    rep->merge_eligible = rep->merge_pairs = rep->removed = 0;
+    rep->split_candidates = rep->split_budget = rep->splits = 0;
+    rep->capacity_hit = 0;
+    rep->count_after = n;
+    if (n <= 1) {
+        return;
+    }
+    const float minMass = R->min_mass_ratio * P->m0;
+    const float maxMass = R->max_mass_ratio * P->m0;
+    float* score = (float*)malloc(sizeof(float) * n);
+    uint32_t* cand = (uint32_t*)malloc(sizeof(uint32_t) * n);
+    uint8_t* flag = (uint8_t*)calloc(n, 1);
+
+    uint32_t cpos = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        score[i] = merge_score(g, P, R, s, c, i, maxMass);
+        cpos += score[i] > 0.0f;
+    }
+    const uint32_t lim = (uint32_t)roundf((float)n * R->max_batch_ratio);
+    const uint32_t k = cpos < lim ? cpos : lim;
+    rep->merge_eligible = k;
+    uint32_t pairs = 0;
+    if (k > 0) {
+        /* (score, slot) ascending; ids are unique, so (sortable score, id) is a total order */
+        uint32_t* sel = (uint32_t*)malloc(sizeof(uint32_t) * n);
+        {
+            uint64_t* tmp = (uint64_t*)malloc(sizeof(uint64_t) * n * 2);
+            for (uint32_t i = 0; i < n; i++) {
+                tmp[2 * i] = ((uint64_t)sortable_f(score[i]) << 32) | s->id[i];
+                tmp[2 * i + 1] = i;
+            }
+            qsort(tmp, n, sizeof(uint64_t) * 2, cmp_u64);
+            for (uint32_t i = 0; i < n; i++) {
+                sel[i] = (uint32_t)tmp[2 * i + 1];
+            }
+            free(tmp);
+        }
+        uint32_t slot0 = 0;
+        for (uint32_t i = 1; i < n; i++) {
+            if (s->id[i] < s->id[slot0]) {
+                slot0 = i;
+            }
+        }
+        for (uint32_t i = 0; i < n; i++) {
+            cand[i] = slot0;
+        }
+        for (uint32_t q = 0; q < k; q++) {
+            const uint32_t e = sel[q];
+            cand[e] = merge_candidate(g, s, c, e, maxMass);
+        }
+        free(sel);
+        for (uint32_t i = 0; i < n; i++) {
+            const uint32_t cc = cand[i];
+            if (cc == ORC_NONE) {
+                continue;
+            }
+            if (cand[cc] == i && s->id[i] < s->id[cc]) {
+                if (rep->keep_ids) {
+                    rep->keep_ids[pairs] = s->id[i];
+                }
+                if (rep->removed_ids) {
+                    rep->removed_ids[pairs] = s->id[cc];
+                }
+                merge_pair(P, s, i, cc);
+                flag[cc] = 1;
+                pairs++;
+            }
+        }
+    }
+    rep->merge_pairs = pairs;
+    if (pairs > 0) {
+        /* stable compaction (compactParticles, AdaptiveAlgorithm.cu:130-157, done out of place) */
+        uint32_t w = 0;
+        for (uint32_t i = 0; i < n; i++) {
+            if (flag[i]) {
+                continue;
+            }
+            if (w != i) {
+                memcpy(s->pos + 4 * (size_t)w, s->pos + 4 * (size_t)i, 16);
+                memcpy(s->vel + 4 * (size_t)w, s->vel + 4 * (size_t)i, 16);
+                memcpy(s->acc + 4 * (size_t)w, s->acc + 4 * (size_t)i, 16);
+                s->rho[w] = s->rho[i];
+                s->rad[w] = s->rad[i];
+                s->h[w] = s->h[i];
+                s->m[w] = s->m[i];
+                s->id[w] = s->id[i];
+                c->keys[w] = c->keys[i];
+            }
+            w++;
+        }
+        const uint32_t removed = n - w;
+        rep->removed = removed;
+        s->n = w;
+        const uint32_t n2 = w;
+        if (R->criterion == 2u) {
+            orc_cells_from_keys(g, n2, c->keys, c->start, c->end);
+        }
+        uint32_t cs = 0;
+        for (uint32_t i = 0; i < n2; i++) {
+            score[i] = split_score(g, P, R, s, c, i, minMass);
+            cs += score[i] > 0.0f;
+        }
+        const uint32_t lim2 = (uint32_t)roundf((float)n2 * R->max_batch_ratio);
+        const uint32_t ks = cs < lim2 ? cs : lim2;
+        rep->split_candidates = ks;
+        const uint32_t budget = ks < removed / 12u ? ks : removed / 12u;
+        rep->split_budget = budget;
+        if (budget > 0) {
+            const uint32_t tpb = P->threads_per_block ? P->threads_per_block : 256u;
+            uint64_t launched = (uint64_t)((budget + tpb - 1) / tpb) * tpb;
+            const uint32_t M = (uint64_t)ks < launched ? ks : (uint32_t)launched;
+            uint64_t* tmp = (uint64_t*)malloc(sizeof(uint64_t) * n2 * 2);
+            for (uint32_t i = 0; i < n2; i++) {
+                tmp[2 * i] = ((uint64_t)(~sortable_f(score[i])) << 32) | s->id[i];
+                tmp[2 * i + 1] = i;
+            }
+            qsort(tmp, n2, sizeof(uint64_t) * 2, cmp_u64);
+            uint32_t done = 0;
+            for (uint32_t r = 0; r < M; r++) {
+                const uint64_t end = (uint64_t)n2 + 12ull * (r + 1);
+                if (end > s->cap) {
+                    rep->capacity_hit = 1;
+                    break;
+                }
+                const uint32_t p = (uint32_t)tmp[2 * r + 1];
+                if (rep->split_ids) {
+                    rep->split_ids[r] = s->id[p];
+                }
+                split_one(R, s, p, n2 + 12u * r, s->next_id + 12u * r);
+                done++;
+            }
+            free(tmp);
+            rep->splits = done;
+            s->n = n2 + 12u * done;
+            s->next_id += 12u * done;
+        }
+    }
+    rep->count_after = s->n;
+    free(score);
+    free(cand);
+    free(flag);
+}
+
+int orc32_step(const orc_grid* g, const orc_params* P, const orc_refine* R, orc_state* s, orc_cells* c,
+               const orc_boundary* b, float dt, orc_report* rep)
+{
+    orc32_integrate(s, P, dt);
+    orc_grid_build(g, s, c);
+    orc32_density(g, P, s, c, b, s->rho);
+    orc32_forces(g, P, s, c, b, s->acc);
+    int refined = 0;
+    if (R != NULL && R->enabled && R->cooldown > 0) {
+        const uint32_t f = s->frame;
+        if (f == R->initial_cooldown || (f > R->initial_cooldown && f % R->cooldown == 0)) {
+            orc32_refine(g, P, R, s, c, rep);
+            refined = 1;
+        }
+    }
+    s->pending_half = dt / 2.0f;
+    s->has_pending = 1;
+    s->frame++;
+    return refined;
+}
+
+/* ------------------------------------------------------------------ boundary generation */
+/* Reference kernel in its own operation order (WendlandKernel.cuh:39-52), as StaticBoundaryDomain uses it. */
+static float ref_wendland(float r, float h)
+{
+    const float q = r / h;
+    if (q > 2.0f) {
+        return 0.0f;
+    }
+    const float h3 = (h * h) * h;
+    const float t = 1.0f - 0.5f * q;
+    const float t4 = (t * t) * (t * t);
+    return ((21.0f / (16.0f * ORC_PI_F)) / h3) * t4 * (2.0f * q + 1.0f);
+}
+
+/* generateWallParticles (StaticBoundaryDomain.cu:88-147) and computePsi (:149-174): psi = rho0 / sum_b W over
+ * walls with |d|^2 < (2h)^2 (self included). The reference sums in KD-tree order; this sums in index order. */
+uint32_t orc_boundary_generate(const float dmin[3], const float dmax[3], float spacing, float rho0, float h,
+                               float* pos4, float* psi, uint32_t cap)
+{
+    float mn[3], mx[3];
+    for (int a = 0; a < 3; a++) {
+        mn[a] = dmin[a] - 0.05f;
+        mx[a] = dmax[a] + 0.05f;
+    }
+    size_t n = 0, cap_all = 0;
+    float* tmp = NULL;
+#define ORC_PUSH(X, Y, Z)                                          \
+    do {                                                           \
+        if (n == cap_all) {                                        \
+            cap_all = cap_all ? cap_all * 2 : 4096;                \
+            tmp = (float*)realloc(tmp, sizeof(float) * 4 * cap_all); \
+        }                                                          \
+        tmp[4 * n] = (X);                                          \
+        tmp[4 * n + 1] = (Y);                                      \
+        tmp[4 * n + 2] = (Z);                                      \
+        tmp[4 * n + 3] = 0.0f;                                     \
+        n++;                                                       \
+    } while (0)
+    for (float x = mn[0]; x < mx[0]; x += spacing)
+        for (float z = mn[2]; z < mx[2]; z += spacing) ORC_PUSH(x, mn[1], z);
+    for (float x = mn[0]; x < mx[0]; x += spacing)
+        for (float z = mn[2]; z < mx[2]; z += spacing) ORC_PUSH(x, mx[1], z);
+    for (float y = mn[1] + spacing; y < mx[1]; y += spacing)
+        for (float z = mn[2]; z < mx[2]; z += spacing) ORC_PUSH(mn[0], y, z);
+    for (float y = mn[1] + spacing; y < mx[1]; y += spacing)
+        for (float z = mn[2]; z < mx[2]; z += spacing) ORC_PUSH(mx[0], y, z);
+    for (float x = mn[0] + spacing; x < mx[0]; x += spacing)
+        for (float y = mn[1] + spacing; y < mx[1]; y += spacing) ORC_PUSH(x, y, mn[2]);
+    for (float x = mn[0] + spacing; x < mx[0]; x += spacing)
+        for (float y = mn[1] + spacing; y < mx[1]; y += spacing) ORC_PUSH(x, y, mx[2]);
+#undef ORC_PUSH
+    if (pos4 == NULL || psi == NULL || n > cap || n == 0) {
+        free(tmp);
+        return (uint32_t)n;
+    }
+    /* exact radius search through a uniform grid of cell 2h */
+    const float R = 2.0f * h;
+    const float R2 = R * R;
+    int gd[3];
+    float lo[3];
+    for (int a = 0; a < 3; a++) {
+        lo[a] = mn[a] - R;
+        gd[a] = (int)((mx[a] + R - lo[a]) / R) + 1;
+    }
+    const size_t ncell = (size_t)gd[0] * gd[1] * gd[2];
+    uint32_t* head = (uint32_t*)malloc(sizeof(uint32_t) * (ncell + 1));
+    uint32_t* list = (uint32_t*)malloc(sizeof(uint32_t) * n);
+    int* cid = (int*)malloc(sizeof(int) * 3 * n);
+    memset(head, 0, sizeof(uint32_t) * (ncell + 1));
+    for (size_t i = 0; i < n; i++) {
+        int cc[3];
+        for (int a = 0; a < 3; a++) {
+            cc[a] = (int)((tmp[4 * i + a] - lo[a]) / R);
+            cid[3 * i + a] = cc[a];
+        }
+        head[(size_t)cc[0] + gd[0] * ((size_t)cc[1] + gd[1] * (size_t)cc[2]) + 1]++;
+    }
+    for (size_t c = 0; c < ncell; c++) {
+        head[c + 1] += head[c];
+    }
+    {
+        uint32_t* fill = (uint32_t*)malloc(sizeof(uint32_t) * ncell);
+        memcpy(fill, head, sizeof(uint32_t) * ncell);
+        for (size_t i = 0; i < n; i++) {
+            const size_t c = (size_t)cid[3 * i] + gd[0] * ((size_t)cid[3 * i + 1] + gd[1] * (size_t)cid[3 * i + 2]);
+            list[fill[c]++] = (uint32_t)i;
+        }
+        free(fill);
+    }
+    const int64_t nn = (int64_t)n;
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t i = 0; i < nn; i++) {
+        float sum = 0.0f;
+        /* index-ordered sum: walk all 27 cells, collect, then sum in ascending index order */
+        uint32_t buf[4096];
+        int nb = 0;
+        for (int dz = -1; dz <= 1; dz++)
+            for (int dy = -1; dy <= 1; dy++)
+                for (int dx = -1; dx <= 1; dx++) {
+                    const int x = cid[3 * i] + dx, y = cid[3 * i + 1] + dy, z = cid[3 * i + 2] + dz;
+                    if (x < 0 || y < 0 || z < 0 || x >= gd[0] || y >= gd[1] || z >= gd[2]) {
+                        continue;
+                    }
+                    const size_t c = (size_t)x + gd[0] * ((size_t)y + gd[1] * (size_t)z);
+                    for (uint32_t q = head[c]; q < head[c + 1] && nb < 4096; q++) {
+                        const uint32_t j = list[q];
+                        const float ddx = tmp[4 * i] - tmp[4 * (size_t)j];
+                        const float ddy = tmp[4 * i + 1] - tmp[4 * (size_t)j + 1];
+                        const float ddz = tmp[4 * i + 2] - tmp[4 * (size_t)j + 2];
+                        const float d2 = (ddx * ddx + ddy * ddy) + ddz * ddz;
+                        if (d2 < R2) {
+                            buf[nb++] = j;
+                        }
+                    }
+                }
+        /* insertion sort of the (short) candidate list by index */
+        for (int a = 1; a < nb; a++) {
+            const uint32_t v = buf[a];
+            int b = a - 1;
+            while (b >= 0 && buf[b] > v) {
+                buf[b + 1] = buf[b];
+                b--;
+            }
+            buf[b + 1] = v;
+        }
+        for (int a = 0; a < nb; a++) {
+            const uint32_t j = buf[a];
+            const float ddx = tmp[4 * i] - tmp[4 * (size_t)j];
+            const float ddy = tmp[4 * i + 1] - tmp[4 * (size_t)j + 1];
+            const float ddz = tmp[4 * i + 2] - tmp[4 * (size_t)j + 2];
+            const float d2 = (ddx * ddx + ddy * ddy) + ddz * ddz;
+            sum += ref_wendland(sqrtf(d2), h);
+        }
+        psi[i] = rho0 * (1.0f / sum);
+        memcpy(pos4 + 4 * i, tmp + 4 * i, sizeof(float) * 4);
+    }
+    free(head);
+    free(list);
+    free(cid);
+    free(tmp);
+    return (uint32_t)n;
+}

@@ -1,0 +1,316 @@
+/*
+ * oracle_body.h — precision-generic part of the oracle (TEST INFRASTRUCTURE ONLY, see asph_oracle.h).
+ * Included twice by asph_oracle.c: with REAL=float (FP32 canonical mirror, suffix 32) and REAL=double
+ * (FP64 restatement, suffix 64). Requires: REAL, F(name), FMA, SQRT, WCOEF, DCOEF.
+ *
+ * Formulas (reference file:line):
+ *   Wendland C2 kernel and derivative ........ cuda/src/algorithm/WendlandKernel.cuh:39-52, 69-84
+ *   Tait equation of state, gamma = 5 ........ cuda/src/algorithm/Common.cuh:6-12
+ *   density ................................... cuda/src/algorithm/Algorithm.cu:17-54
+ *   boundary density .......................... cuda/src/algorithm/BoundaryAlgorithm.cu:15-51
+ *   gravity / pressure / viscosity / cohesion . cuda/src/algorithm/Algorithm.cu:56-232
+ *   boundary pressure / friction .............. cuda/src/algorithm/BoundaryAlgorithm.cu:53-162
+ *
+ * Canonical operation order (shared with the CUDA kernels, documented where it departs from the
+ * reference): squared distances are fma(dz,dz,fma(dy,dy,dx*dx)); q = r * (1/h) instead of r / h;
+ * the kernel prefactors coef/h^3 and dcoef/h^4 are formed once per particle; the Tait pressure is
+ * B*d*(5+d*(10+d*(10+d*(5+d)))) with d = (rho-rho0)/rho0, algebraically (rho/rho0)^5-1 without
+ * the cancellation of powf(...)-1; directions are offset * (1/r); per-pair force terms are a scalar
+ * s times the direction, accumulated with fma.
+ */
+
+/* W(r, h) with precomputed 1/h and coef/h^3 */
+static inline REAL F(kernel_w)(REAL r, REAL invh, REAL wc)
+{
+    const REAL q = r * invh;
+    if (q > (REAL)2) {
+        return (REAL)0;
+    }
+    const REAL t = FMA((REAL)-0.5, q, (REAL)1);
+    const REAL t2 = t * t;
+    return (wc * (t2 * t2)) * FMA((REAL)2, q, (REAL)1);
+}
+
+/* dW/dr(r, h) with precomputed 1/h and dcoef/h^4 */
+static inline REAL F(kernel_dw)(REAL r, REAL invh, REAL dwc)
+{
+    const REAL q = r * invh;
+    if (q > (REAL)2) {
+        return (REAL)0;
+    }
+    const REAL t = FMA((REAL)-0.5, q, (REAL)1);
+    const REAL t3 = (t * t) * t;
+    return (dwc * q) * t3;
+}
+
+static inline void F(kernel_consts)(REAL h, REAL* invh, REAL* wc, REAL* dwc)
+{
+    const REAL h3 = (h * h) * h;
+    *invh = (REAL)1 / h;
+    *wc = WCOEF / h3;
+    *dwc = DCOEF / (h3 * h);
+}
+
+/* p / rho^2 with the Tait equation (Common.cuh:6-12) */
+static inline REAL F(pressure_term)(REAL rho, REAL rho0, REAL c0)
+{
+    const REAL B = ((rho0 * c0) * c0) / (REAL)5;
+    const REAL d = (rho - rho0) / rho0;
+    REAL u = (REAL)5 + d;
+    u = FMA(d, u, (REAL)10);
+    u = FMA(d, u, (REAL)10);
+    u = FMA(d, u, (REAL)5);
+    const REAL p = B * (d * u);
+    return p / (rho * rho);
+}
+
+/* neighbour coordinate a of p, shifted by the periodic image offset of its cell (sh) */
+#define NBR(p, a) (g->periodic ? (REAL)(p)[a] + (REAL)sh[a] : (REAL)(p)[a])
+
+static inline REAL F(dist2)(REAL dx, REAL dy, REAL dz)
+{
+    return FMA(dz, dz, FMA(dy, dy, dx * dx));
+}
+
+void F(orc_density_impl)(const orc_grid* g, const orc_params* P, const orc_state* s, const orc_cells* c,
+                         const orc_boundary* b, REAL* rho_out)
+{
+    const int64_t n = s->n;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < n; i++) {
+        const float* pi = s->pos + 4 * i;
+        const REAL xi = pi[0], yi = pi[1], zi = pi[2];
+        const REAL hi = s->h[i];
+        const float R = s->h[i] + s->h[i];
+        REAL rho = 0;
+        orc_iter it;
+        uint32_t jb, je;
+        float sh[3];
+        it_init(&it, g, c->start, c->end, c->ex, pi, R);
+        while (it_next(&it, &jb, &je, sh)) {
+            for (uint32_t j = jb; j < je; j++) {
+                const float* pj = s->pos + 4 * (size_t)j;
+                const REAL dx = NBR(pj, 0) - xi;
+                const REAL dy = NBR(pj, 1) - yi;
+                const REAL dz = NBR(pj, 2) - zi;
+                const REAL r2 = F(dist2)(dx, dy, dz);
+                const REAL hj = s->h[j];
+                const REAL twoh = hj + hj;
+                if (r2 > twoh * twoh) {
+                    continue;
+                }
+                REAL invh, wc, dwc;
+                F(kernel_consts)(hj, &invh, &wc, &dwc);
+                const REAL w = F(kernel_w)(SQRT(r2), invh, wc);
+                rho = FMA((REAL)s->m[j], w, rho);
+            }
+        }
+        REAL rb = 0;
+        if (b != NULL && b->n > 0) {
+            REAL invh, wc, dwc;
+            F(kernel_consts)(hi, &invh, &wc, &dwc);
+            const REAL twoh = hi + hi;
+            const REAL cut = twoh * twoh;
+            it_init(&it, g, b->start, b->end, b->ex, pi, R);
+            while (it_next(&it, &jb, &je, sh)) {
+                for (uint32_t k = jb; k < je; k++) {
+                    const float* pb = b->pos + 4 * (size_t)k;
+                    const REAL dx = NBR(pb, 0) - xi;
+                    const REAL dy = NBR(pb, 1) - yi;
+                    const REAL dz = NBR(pb, 2) - zi;
+                    const REAL r2 = F(dist2)(dx, dy, dz);
+                    if (r2 > cut) {
+                        continue;
+                    }
+                    const REAL w = F(kernel_w)(SQRT(r2), invh, wc);
+                    rb = FMA((REAL)b->psi[k], w, rb);
+                }
+            }
+        }
+        rho_out[i] = rho + rb;
+    }
+}
+
+/* Force pass. rho: densities of the state (FP32 values, as the GPU holds them). */
+void F(orc_forces_impl)(const orc_grid* g, const orc_params* P, const orc_state* s, const orc_cells* c,
+                        const orc_boundary* b, const float* rho_in, REAL* acc_out, double* scale_out)
+{
+    const int64_t n = s->n;
+    const REAL rho0 = P->rho0, c0 = P->c0;
+    const REAL alpha = P->alpha, sigma = P->sigma, nu_k = P->nu;
+    const int morris = P->viscosity_model == 1u;
+    const int visc_on = morris ? (P->nu != 0.0f) : (P->alpha != 0.0f);
+    const int sigma_on = P->sigma != 0.0f;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < n; i++) {
+        const float* pi = s->pos + 4 * i;
+        const float* vi4 = s->vel + 4 * i;
+        const REAL xi = pi[0], yi = pi[1], zi = pi[2];
+        const REAL vxi = vi4[0], vyi = vi4[1], vzi = vi4[2];
+        const REAL hi = s->h[i], mi = s->m[i];
+        const REAL rhoi = rho_in[i];
+        const REAL pti = F(pressure_term)(rhoi, rho0, c0);
+        const REAL Ki = (((REAL)2 * alpha) * hi) * c0;
+        const REAL ei = ((REAL)0.01 * hi) * hi;
+        const float R = s->h[i] + s->h[i];
+        REAL apx = 0, apy = 0, apz = 0, avx = 0, avy = 0, avz = 0, asx = 0, asy = 0, asz = 0;
+        double scale = 0.0;
+        orc_iter it;
+        uint32_t jb, je;
+        float sh[3];
+        it_init(&it, g, c->start, c->end, c->ex, pi, R);
+        while (it_next(&it, &jb, &je, sh)) {
+            for (uint32_t j = jb; j < je; j++) {
+                if ((int64_t)j == i) {
+                    continue;
+                }
+                const float* pj = s->pos + 4 * (size_t)j;
+                const REAL dx = xi - NBR(pj, 0);
+                const REAL dy = yi - NBR(pj, 1);
+                const REAL dz = zi - NBR(pj, 2);
+                const REAL r2 = F(dist2)(dx, dy, dz);
+                const REAL hj = s->h[j];
+                const REAL twoh = hj + hj;
+                if (r2 > twoh * twoh) {
+                    continue;
+                }
+                REAL invh, wc, dwc;
+                F(kernel_consts)(hj, &invh, &wc, &dwc);
+                const REAL r = SQRT(r2);
+                REAL ux, uy, uz;
+                if (r > (REAL)0) {
+                    const REAL ir = (REAL)1 / r;
+                    ux = dx * ir;
+                    uy = dy * ir;
+                    uz = dz * ir;
+                } else {
+                    ux = 0;
+                    uy = 1;
+                    uz = 0;
+                }
+                const REAL dw = F(kernel_dw)(r, invh, dwc);
+                const REAL mj = s->m[j];
+                const REAL rhoj = rho_in[j];
+                const REAL ptj = F(pressure_term)(rhoj, rho0, c0);
+                {
+                    const REAL sp = (mj * dw) * (pti + ptj);
+                    apx = FMA(-sp, ux, apx);
+                    apy = FMA(-sp, uy, apy);
+                    apz = FMA(-sp, uz, apz);
+                    scale += fabs((double)sp);
+                }
+                if (visc_on) {
+                    const float* vj4 = s->vel + 4 * (size_t)j;
+                    const REAL vdx = vxi - (REAL)vj4[0];
+                    const REAL vdy = vyi - (REAL)vj4[1];
+                    const REAL vdz = vzi - (REAL)vj4[2];
+                    if (!morris) {
+                        const REAL comp = FMA(vdz, dz, FMA(vdy, dy, vdx * dx));
+                        if (comp < (REAL)0) {
+                            const REAL nuij = Ki / (rhoi + rhoj);
+                            const REAL piv = (-nuij * comp) / (r2 + ei);
+                            const REAL sv = (mj * piv) * dw;
+                            avx = FMA(-sv, ux, avx);
+                            avy = FMA(-sv, uy, avy);
+                            avz = FMA(-sv, uz, avz);
+                            scale += fabs((double)sv);
+                        }
+                    } else {
+                        const REAL coef = ((mj * nu_k) * (rhoi + rhoj)) / (rhoi * rhoj);
+                        const REAL sv = coef * ((r * dw) / (r2 + ei));
+                        avx = FMA(sv, vdx, avx);
+                        avy = FMA(sv, vdy, avy);
+                        avz = FMA(sv, vdz, avz);
+                        scale += fabs((double)sv) * sqrt((double)vdx * vdx + (double)vdy * vdy + (double)vdz * vdz);
+                    }
+                }
+                if (sigma_on) {
+                    const REAL ss = mj * F(kernel_w)(r, invh, wc);
+                    asx = FMA(ss, ux, asx);
+                    asy = FMA(ss, uy, asy);
+                    asz = FMA(ss, uz, asz);
+                    scale += fabs((double)(sigma / mi) * (double)ss);
+                }
+            }
+        }
+        REAL bpx = 0, bpy = 0, bpz = 0, bfx = 0, bfy = 0, bfz = 0;
+        if (b != NULL && b->n > 0) {
+            REAL invh, wc, dwc;
+            F(kernel_consts)(hi, &invh, &wc, &dwc);
+            const REAL twoh = hi + hi;
+            const REAL cut = twoh * twoh;
+            it_init(&it, g, b->start, b->end, b->ex, pi, R);
+            while (it_next(&it, &jb, &je, sh)) {
+                for (uint32_t k = jb; k < je; k++) {
+                    const float* pb = b->pos + 4 * (size_t)k;
+                    const REAL dx = xi - NBR(pb, 0);
+                    const REAL dy = yi - NBR(pb, 1);
+                    const REAL dz = zi - NBR(pb, 2);
+                    const REAL r2 = F(dist2)(dx, dy, dz);
+                    if (r2 > cut) {
+                        continue;
+                    }
+                    const REAL r = SQRT(r2);
+                    REAL ux, uy, uz;
+                    if (r > (REAL)0) {
+                        const REAL ir = (REAL)1 / r;
+                        ux = dx * ir;
+                        uy = dy * ir;
+                        uz = dz * ir;
+                    } else {
+                        ux = 0;
+                        uy = 1;
+                        uz = 0;
+                    }
+                    const REAL dw = F(kernel_dw)(r, invh, dwc);
+                    const REAL psi = b->psi[k];
+                    const REAL sp = (psi * pti) * dw;
+                    bpx = FMA(-sp, ux, bpx);
+                    bpy = FMA(-sp, uy, bpy);
+                    bpz = FMA(-sp, uz, bpz);
+                    scale += fabs((double)sp);
+                    const REAL comp = FMA(vzi, dz, FMA(vyi, dy, vxi * dx));
+                    if (comp < (REAL)0) {
+                        const REAL nub = (((REAL)b->fric[k] * hi) * c0) / ((REAL)2 * rhoi);
+                        const REAL pib = (-nub * comp) / (r2 + ei);
+                        const REAL sf = (psi * pib) * dw;
+                        bfx = FMA(-sf, ux, bfx);
+                        bfy = FMA(-sf, uy, bfy);
+                        bfz = FMA(-sf, uz, bfz);
+                        scale += fabs((double)sf);
+                    }
+                }
+            }
+        }
+        REAL ax = P->gravity[0], ay = P->gravity[1], az = P->gravity[2];
+        ax = ax + apx;
+        ay = ay + apy;
+        az = az + apz;
+        if (visc_on) {
+            ax = ax + avx;
+            ay = ay + avy;
+            az = az + avz;
+        }
+        if (sigma_on) {
+            const REAL f = sigma / mi;
+            ax = ax + f * asx;
+            ay = ay + f * asy;
+            az = az + f * asz;
+        }
+        ax = ax + bpx;
+        ay = ay + bpy;
+        az = az + bpz;
+        ax = ax + bfx;
+        ay = ay + bfy;
+        az = az + bfz;
+        acc_out[4 * i + 0] = ax;
+        acc_out[4 * i + 1] = ay;
+        acc_out[4 * i + 2] = az;
+        acc_out[4 * i + 3] = 0;
+        if (scale_out != NULL) {
+            const double g2 = (double)P->gravity[0] * P->gravity[0] + (double)P->gravity[1] * P->gravity[1] +
+                              (double)P->gravity[2] * P->gravity[2];
+            scale_out[i] = scale + sqrt(g2);
+        }
+    }
+}
