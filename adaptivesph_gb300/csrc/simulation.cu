@@ -174,6 +174,10 @@ struct asph_simulation {
     asph_refinement_report last_report{};
     uint32_t last_pairs_listed = 0, last_splits_listed = 0;
 
+    // export staging (device), grown on demand
+    uint8_t* stage = nullptr;
+    size_t stage_bytes = 0;
+
     // pinned host scratch
     uint32_t* h_ctr = nullptr;
     uint64_t* h_small = nullptr;
@@ -721,6 +725,7 @@ void destroy(asph_simulation* s) {
     dfree(s->block_counts);
     dfree(s->rkeys);
     dfree(s->dbg_ids);
+    dfree(s->stage);
     if (s->h_ctr) cudaFreeHost(s->h_ctr);
     if (s->h_small) cudaFreeHost(s->h_small);
     for (auto& e : s->events) {
@@ -1223,11 +1228,17 @@ asph_status asph_simulation_export_host(asph_simulation* sim, float* positions, 
     const uint32_t n = sim->n;
     if (capacity < n) return fail(ASPH_ERR_CAPACITY, "host arrays too small");
     if (n == 0) return ASPH_OK;
-    // stage through the spare half of the sort buffers' neighbours: a dedicated staging allocation
-    uint8_t* stage = nullptr;
+    // staging buffer kept across calls (grown on demand) so that a per-frame export allocates nothing
     const size_t bytes = (size_t)n * (16 + 16 + 4 + 4 + 4);
-    asph_status st;
-    if ((st = dalloc(stage, bytes)) != ASPH_OK) return st;
+    if (bytes > sim->stage_bytes) {
+        dfree(sim->stage);
+        sim->stage = nullptr;
+        sim->stage_bytes = 0;
+        asph_status st;
+        if ((st = dalloc(sim->stage, bytes)) != ASPH_OK) return st;
+        sim->stage_bytes = bytes;
+    }
+    uint8_t* stage = sim->stage;
     float4* dp = reinterpret_cast<float4*>(stage);
     float4* dv = dp + n;
     float* dr = reinterpret_cast<float*>(dv + n);
@@ -1245,7 +1256,6 @@ asph_status asph_simulation_export_host(asph_simulation* sim, float* positions, 
     if (radii) CK(cudaMemcpyAsync(radii, dd, 4 * (size_t)n, cudaMemcpyDeviceToHost, sim->stream));
     if (ids) CK(cudaMemcpyAsync(ids, di, 4 * (size_t)n, cudaMemcpyDeviceToHost, sim->stream));
     CK(cudaStreamSynchronize(sim->stream));
-    dfree(stage);
     return check_errors(sim, false);
 }
 
