@@ -42,6 +42,10 @@ static asph_status cuda_fail(cudaError_t e, const char* what) {
         if (e_ != cudaSuccess) return cuda_fail(e_, #call);        \
     } while (0)
 
+// Drops a stale, non-sticky error left by an earlier runtime call (of this library or of the caller), so that
+// the launch checks below report only errors of the launch itself. Sticky errors persist and are still caught.
+#define API_ENTRY() (void)cudaGetLastError()
+
 #define CK_LAUNCH(what)                                            \
     do {                                                           \
         cudaError_t e_ = cudaGetLastError();                       \
@@ -247,17 +251,23 @@ struct asph_simulation {
         events[h].cls = cls;
         cudaEventRecord(events[h].b, stream);
     }
-    void harvest() {
+    cudaError_t harvest() {
+        cudaError_t first = cudaSuccess;
         for (auto& e : events) {
             float t = 0.f;
-            if (cudaEventElapsedTime(&t, e.a, e.b) == cudaSuccess) {
+            const cudaError_t r = cudaEventElapsedTime(&t, e.a, e.b);
+            if (r == cudaSuccess) {
                 ms[e.cls] += t;
                 timed[e.cls] += 1;
+            } else if (first == cudaSuccess) {
+                first = r;
             }
             event_pool.push_back(e.a);
             event_pool.push_back(e.b);
         }
         events.clear();
+        (void)cudaGetLastError();  // a failed elapsed-time query must not surface in a later launch check
+        return first;
     }
 };
 
@@ -735,6 +745,7 @@ void destroy(asph_simulation* s) {
     for (auto e : s->event_pool) cudaEventDestroy(e);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
     delete s;
+    (void)cudaGetLastError();
 }
 
 }  // namespace
@@ -787,6 +798,7 @@ void asph_refinement_parameters_default(asph_refinement_parameters* p) {
 
 // ---------------------------------------------------------------------------------------------- memory
 asph_status asph_import_buffer_fd(int fd, size_t size, asph_memory** out) {
+    API_ENTRY();
     if (!out || fd < 0 || size == 0) return fail(ASPH_ERR_INVALID_ARGUMENT, "import needs an fd, a size and out");
     *out = nullptr;
     cudaExternalMemoryHandleDesc hd;
@@ -820,6 +832,7 @@ asph_status asph_import_buffer_fd(int fd, size_t size, asph_memory** out) {
 }
 
 asph_status asph_memory_allocate(size_t size, asph_memory** out) {
+    API_ENTRY();
     if (!out || size == 0) return fail(ASPH_ERR_INVALID_ARGUMENT, "allocation needs a size and out");
     *out = nullptr;
     void* p = nullptr;
@@ -837,12 +850,14 @@ asph_status asph_memory_allocate(size_t size, asph_memory** out) {
 }
 
 asph_status asph_memory_device_pointer(const asph_memory* mem, void** out) {
+    API_ENTRY();
     if (!mem || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
     *out = mem->ptr;
     return ASPH_OK;
 }
 
 asph_status asph_memory_size(const asph_memory* mem, size_t* out) {
+    API_ENTRY();
     if (!mem || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
     *out = mem->size;
     return ASPH_OK;
@@ -862,6 +877,7 @@ asph_status asph_simulation_create(const asph_parameters* parameters, const floa
                                    const asph_boundary_particle* boundary, uint32_t boundary_count,
                                    const asph_refinement_parameters* refinement, uint32_t max_fluid_capacity,
                                    uint32_t max_boundary_capacity, asph_simulation** out) {
+    API_ENTRY();
     if (!parameters || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "parameters and out are required");
     *out = nullptr;
     if (count > 0 && !positions) return fail(ASPH_ERR_INVALID_ARGUMENT, "positions are required");
@@ -996,17 +1012,20 @@ asph_status asph_simulation_create(const asph_parameters* parameters, const floa
 void asph_simulation_destroy(asph_simulation* sim) { destroy(sim); }
 
 asph_status asph_simulation_step_async(asph_simulation* sim, float delta_time) {
+    API_ENTRY();
     if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
     return run_step(sim, delta_time, ASPH_STAGE_ALL);
 }
 
 asph_status asph_simulation_update(asph_simulation* sim, float delta_time) {
+    API_ENTRY();
     asph_status st = asph_simulation_step_async(sim, delta_time);
     if (st != ASPH_OK) return st;
     return check_errors(sim, true);
 }
 
 asph_status asph_simulation_run_stages(asph_simulation* sim, float delta_time, uint32_t last_stage) {
+    API_ENTRY();
     if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
     if (last_stage < ASPH_STAGE_INTEGRATE || last_stage > ASPH_STAGE_ALL)
         return fail(ASPH_ERR_INVALID_ARGUMENT, "unknown stage");
@@ -1016,11 +1035,13 @@ asph_status asph_simulation_run_stages(asph_simulation* sim, float delta_time, u
 }
 
 asph_status asph_simulation_synchronize(asph_simulation* sim) {
+    API_ENTRY();
     if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
     return check_errors(sim, true);
 }
 
 asph_status asph_simulation_totals(asph_simulation* sim, asph_totals* out) {
+    API_ENTRY();
     if (!sim || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
     std::memset(out, 0, sizeof(*out));
     out->count = sim->n;
@@ -1047,6 +1068,7 @@ asph_status asph_simulation_totals(asph_simulation* sim, asph_totals* out) {
 }
 
 asph_status asph_simulation_step_cfl(asph_simulation* sim, float cfl, float dt_max, float* dt_used) {
+    API_ENTRY();
     if (!sim || !(cfl > 0.0f)) return fail(ASPH_ERR_INVALID_ARGUMENT, "simulation and cfl > 0 required");
     float dt = dt_max > 0.0f ? dt_max : 3.402823466e38f;
     if (sim->n > 0) {
@@ -1076,6 +1098,7 @@ asph_status asph_simulation_step_cfl(asph_simulation* sim, float cfl, float dt_m
 
 asph_status asph_simulation_update_domain(asph_simulation* sim, const asph_domain* domain,
                                           const asph_boundary_particle* boundary, uint32_t boundary_count) {
+    API_ENTRY();
     if (!sim || !domain) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
     if (boundary_count > 0 && !boundary) return fail(ASPH_ERR_INVALID_ARGUMENT, "boundary particles are required");
     CK(cudaStreamSynchronize(sim->stream));
@@ -1095,18 +1118,21 @@ asph_status asph_simulation_update_domain(asph_simulation* sim, const asph_domai
 }
 
 asph_status asph_simulation_fluid_count(const asph_simulation* sim, uint32_t* out) {
+    API_ENTRY();
     if (!sim || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
     *out = sim->n;
     return ASPH_OK;
 }
 
 asph_status asph_simulation_boundary_count(const asph_simulation* sim, uint32_t* out) {
+    API_ENTRY();
     if (!sim || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
     *out = sim->nb;
     return ASPH_OK;
 }
 
 asph_status asph_simulation_neighbor_counts(asph_simulation* sim, uint32_t* counts, uint32_t capacity) {
+    API_ENTRY();
     if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
     if (counts && capacity < sim->n) return fail(ASPH_ERR_CAPACITY, "counts array too small");
     if (sim->n == 0) return ASPH_OK;
@@ -1131,6 +1157,7 @@ asph_status asph_simulation_neighbor_counts(asph_simulation* sim, uint32_t* coun
 }
 
 asph_status asph_simulation_average_neighbor_count(asph_simulation* sim, float* out) {
+    API_ENTRY();
     if (!sim || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
     *out = 0.0f;
     if (sim->n == 0) return ASPH_OK;
@@ -1152,6 +1179,7 @@ asph_status asph_simulation_average_neighbor_count(asph_simulation* sim, float* 
 }
 
 asph_status asph_simulation_density_info(asph_simulation* sim, float threshold, asph_density_info* out) {
+    API_ENTRY();
     if (!sim || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
     std::memset(out, 0, sizeof(*out));
     out->rest_density = sim->P.rest_density;
@@ -1198,12 +1226,14 @@ asph_status asph_simulation_density_info(asph_simulation* sim, float threshold, 
 }
 
 asph_status asph_simulation_enable_adaptive_refinement(asph_simulation* sim) {
+    API_ENTRY();
     if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
     if (sim->adaptive) sim->frame = sim->R.initial_cooldown;
     return ASPH_OK;
 }
 
 asph_status asph_simulation_export(asph_simulation* sim) {
+    API_ENTRY();
     if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
     if (!sim->have_fbuf) return ASPH_OK;
     const asph_fluid_buffers& f = sim->fbuf;
@@ -1224,6 +1254,7 @@ asph_status asph_simulation_export(asph_simulation* sim) {
 
 asph_status asph_simulation_export_host(asph_simulation* sim, float* positions, float* velocities, float* densities,
                                         float* radii, uint32_t* ids, uint32_t capacity) {
+    API_ENTRY();
     if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
     const uint32_t n = sim->n;
     if (capacity < n) return fail(ASPH_ERR_CAPACITY, "host arrays too small");
@@ -1260,6 +1291,7 @@ asph_status asph_simulation_export_host(asph_simulation* sim, float* positions, 
 }
 
 asph_status asph_simulation_device_errors(asph_simulation* sim, uint32_t* out, int clear) {
+    API_ENTRY();
     if (!sim || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
     CK(cudaStreamSynchronize(sim->stream));
     CK(cudaMemcpy(sim->h_ctr, sim->err, sizeof(uint32_t), cudaMemcpyDeviceToHost));
@@ -1269,6 +1301,7 @@ asph_status asph_simulation_device_errors(asph_simulation* sim, uint32_t* out, i
 }
 
 asph_status asph_simulation_set_stream(asph_simulation* sim, void* cuda_stream) {
+    API_ENTRY();
     if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
     CK(cudaStreamSynchronize(sim->stream));
     sim->stream = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : sim->own_stream;
@@ -1276,6 +1309,7 @@ asph_status asph_simulation_set_stream(asph_simulation* sim, void* cuda_stream) 
 }
 
 asph_status asph_simulation_state_info(asph_simulation* sim, asph_state_info* out) {
+    API_ENTRY();
     if (!sim || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
     out->count = sim->n;
     out->capacity = sim->cap;
@@ -1289,6 +1323,7 @@ asph_status asph_simulation_state_info(asph_simulation* sim, asph_state_info* ou
 asph_status asph_simulation_read_fluid(asph_simulation* sim, float* positions, float* velocities,
                                        float* accelerations, float* densities, float* radii, float* smoothing_radii,
                                        float* masses, uint32_t* ids, uint32_t capacity) {
+    API_ENTRY();
     if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
     const uint32_t n = sim->n;
     if (capacity < n) return fail(ASPH_ERR_CAPACITY, "host arrays too small");
@@ -1325,6 +1360,7 @@ asph_status asph_simulation_write_fluid(asph_simulation* sim, const asph_state_i
                                         const float* velocities, const float* accelerations, const float* densities,
                                         const float* radii, const float* smoothing_radii, const float* masses,
                                         const uint32_t* ids) {
+    API_ENTRY();
     if (!sim || !info) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
     const uint32_t n = info->count;
     if (n > sim->cap) return fail(ASPH_ERR_CAPACITY, "more particles than the fluid capacity");
@@ -1370,6 +1406,7 @@ asph_status asph_simulation_write_fluid(asph_simulation* sim, const asph_state_i
 }
 
 asph_status asph_simulation_grid_info(asph_simulation* sim, asph_grid_info* out) {
+    API_ENTRY();
     if (!sim || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
     for (int a = 0; a < 3; a++) {
         out->reference_cells[a] = sim->grid.gs[a];
@@ -1390,6 +1427,7 @@ asph_status asph_simulation_grid_info(asph_simulation* sim, asph_grid_info* out)
 
 asph_status asph_simulation_read_grid(asph_simulation* sim, uint32_t* keys, uint32_t key_capacity,
                                       uint32_t* cell_start, uint32_t* cell_end, uint32_t cell_capacity) {
+    API_ENTRY();
     if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
     CK(cudaStreamSynchronize(sim->stream));
     if (keys) {
@@ -1407,15 +1445,17 @@ asph_status asph_simulation_read_grid(asph_simulation* sim, uint32_t* keys, uint
 }
 
 asph_status asph_simulation_last_refinement(asph_simulation* sim, asph_refinement_report* out) {
+    API_ENTRY();
     if (!sim || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
     *out = sim->last_report;
     return ASPH_OK;
 }
 
 asph_status asph_simulation_enable_timing(asph_simulation* sim, int enable) {
+    API_ENTRY();
     if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
     CK(cudaStreamSynchronize(sim->stream));
-    sim->harvest();
+    (void)sim->harvest();
     for (int k = 0; k < (int)ASPH_KERNEL_COUNT; k++) {
         sim->ms[k] = 0.0;
         sim->timed[k] = 0;
@@ -1425,9 +1465,11 @@ asph_status asph_simulation_enable_timing(asph_simulation* sim, int enable) {
 }
 
 asph_status asph_simulation_kernel_times(asph_simulation* sim, double* ms, uint32_t* launches, uint32_t n) {
+    API_ENTRY();
     if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
     CK(cudaStreamSynchronize(sim->stream));
-    sim->harvest();
+    const cudaError_t he = sim->harvest();
+    if (he != cudaSuccess) return cuda_fail(he, "cudaEventElapsedTime");
     for (uint32_t k = 0; k < n && k < ASPH_KERNEL_COUNT; k++) {
         if (ms) ms[k] = sim->ms[k];
         if (launches) launches[k] = sim->timed[k];
@@ -1436,6 +1478,7 @@ asph_status asph_simulation_kernel_times(asph_simulation* sim, double* ms, uint3
 }
 
 asph_status asph_simulation_launch_count(const asph_simulation* sim, uint64_t* out) {
+    API_ENTRY();
     if (!sim || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
     *out = sim->launches;
     return ASPH_OK;
@@ -1445,6 +1488,7 @@ asph_status asph_simulation_launch_count(const asph_simulation* sim, uint64_t* o
 
 // Records the ids of merged and split particles of each refinement pass (test hook, not in asph.h).
 extern "C" asph_status asph_debug_record_refinement(asph_simulation* sim, int enable) {
+    API_ENTRY();
     if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
     if (enable && !sim->dbg_ids) {
         asph_status st = dalloc(sim->dbg_ids, 3 * (size_t)sim->cap);
@@ -1456,6 +1500,7 @@ extern "C" asph_status asph_debug_record_refinement(asph_simulation* sim, int en
 
 extern "C" asph_status asph_debug_refinement_ids(asph_simulation* sim, uint32_t* keep, uint32_t* removed,
                                                  uint32_t* split, uint32_t capacity) {
+    API_ENTRY();
     if (!sim || !sim->dbg_ids) return fail(ASPH_ERR_INVALID_ARGUMENT, "recording not enabled");
     CK(cudaStreamSynchronize(sim->stream));
     const uint32_t np = sim->last_pairs_listed, ns = sim->last_splits_listed;
