@@ -20,6 +20,17 @@ struct StepArgs {
     uint32_t* err;
 };
 
+// Per-particle neighbour lists of the current step: entry k of particle i at idx[k * stride + i] (one column per
+// particle, so a warp reading entry k of 32 consecutive particles reads 128 contiguous bytes). The density pass
+// fills them in the canonical candidate order; cnt[i] > maxn marks an overflowed list, for which the later passes
+// scan the candidate cells again.
+struct NbrDev {
+    uint32_t* idx;
+    uint32_t* cnt;
+    uint32_t stride;
+    uint32_t maxn;
+};
+
 struct ReorderArgs {
     const uint32_t* keys_sorted;
     const uint32_t* vals_sorted;
@@ -48,8 +59,9 @@ __global__ void k_boundary_reorder(GridDev g, const float4* pos_in, const float*
                                    const uint32_t* keys_sorted, const uint32_t* vals_sorted, uint32_t n,
                                    float4* pos_out, float* fric_out, uint32_t* start, uint32_t* end,
                                    uint8_t* refflag);
-__global__ void k_density(StepArgs a, CellsDev c, BoundaryDev b);
-cudaError_t launch_forces(bool morris, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c, BoundaryDev b);
+__global__ void k_density(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl);
+cudaError_t launch_forces(bool morris, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c, BoundaryDev b,
+                          NbrDev nl);
 __global__ void k_neighbor_counts(StepArgs a, CellsDev c, uint32_t* counts, unsigned long long* total);
 __global__ void k_export(StepArgs a, float pending_half, int has_pending, float4* pos_out, float4* vel_out,
                          float* rho_out, float* rad_out, uint32_t* id_out);

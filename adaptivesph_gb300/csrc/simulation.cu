@@ -135,6 +135,9 @@ struct asph_simulation {
     BufferSet set[2];
     int cur = 0;
     float4* kc = nullptr;
+    uint32_t* nbr_idx = nullptr;  // [maxn * cap] neighbour lists, one column per particle
+    uint32_t* nbr_cnt = nullptr;  // [cap]
+    uint32_t maxn = 128;
     uint32_t* keys = nullptr;
     uint32_t* vals = nullptr;
     void* sort_mem = nullptr;
@@ -224,6 +227,8 @@ struct asph_simulation {
     }
 
     CellsDev cells() const { return CellsDev{cell_start, cell_end, cell_hmax, ex, hmax_all}; }
+
+    NbrDev nbrs() const { return NbrDev{nbr_idx, nbr_cnt, cap, maxn}; }
 
     BoundaryDev boundary() const {
         return BoundaryDev{bpos, bfric, bstart, bend, brefflag, bex[0], bex[1], nb};
@@ -495,7 +500,7 @@ asph_status build_grid(asph_simulation* s, bool integrate, float dt, bool carry_
 asph_status run_density(asph_simulation* s) {
     StepArgs a = s->args(s->cur);
     int h = s->tic();
-    k_density<<<blocks_for(s->n), 256, 0, s->stream>>>(a, s->cells(), s->boundary());
+    k_density<<<blocks_for(s->n), 256, 0, s->stream>>>(a, s->cells(), s->boundary(), s->nbrs());
     CK_LAUNCH("k_density");
     s->toc(h, ASPH_KERNEL_DENSITY);
     s->launches++;
@@ -505,7 +510,7 @@ asph_status run_density(asph_simulation* s) {
 asph_status run_forces(asph_simulation* s) {
     StepArgs a = s->args(s->cur);
     int h = s->tic();
-    CK(launch_forces(s->phys.morris != 0, blocks_for(s->n), s->stream, a, s->cells(), s->boundary()));
+    CK(launch_forces(s->phys.morris != 0, blocks_for(s->n), s->stream, a, s->cells(), s->boundary(), s->nbrs()));
     s->toc(h, ASPH_KERNEL_FORCES);
     s->launches++;
     return ASPH_OK;
@@ -711,6 +716,8 @@ void destroy(asph_simulation* s) {
         dfree(s->set[k].id);
     }
     dfree(s->kc);
+    dfree(s->nbr_idx);
+    dfree(s->nbr_cnt);
     dfree(s->keys);
     dfree(s->vals);
     dfree(s->sort_mem);
@@ -899,6 +906,8 @@ asph_status asph_simulation_create(const asph_parameters* parameters, const floa
     const uint32_t cap = adaptive ? refinement->max_particle_count : std::max(max_fluid_capacity, count);
     if (count > cap) return fail(ASPH_ERR_CAPACITY, "more particles than the fluid capacity");
     if (cap > (1u << 30)) return fail(ASPH_ERR_UNSUPPORTED, "fluid capacity above 2^30");
+    if (P.boundary_mode == ASPH_BOUNDARY_PERIODIC && cap >= (1u << 27))
+        return fail(ASPH_ERR_UNSUPPORTED, "a periodic box holds at most 2^27 - 1 particles");
     asph_simulation* s = new (std::nothrow) asph_simulation;
     if (!s) return fail(ASPH_ERR_OUT_OF_MEMORY, "host allocation failed");
     s->P = P;
@@ -943,6 +952,8 @@ asph_status asph_simulation_create(const asph_parameters* parameters, const floa
         TRY(dalloc(s->set[k].id, C));
     }
     TRY(dalloc(s->kc, C));
+    TRY(dalloc(s->nbr_idx, (size_t)s->maxn * C));
+    TRY(dalloc(s->nbr_cnt, C));
     const uint32_t sort_items = std::max(C, std::max(boundary_count, max_boundary_capacity));
     TRY(dalloc(s->keys, sort_items));
     TRY(dalloc(s->vals, sort_items));

@@ -234,33 +234,102 @@ __device__ __forceinline__ bool boundary_near(const GridDev& g, const BoundaryDe
     return false;
 }
 
+// Periodic image of a listed neighbour: the index keeps 27 bits, the cell's image offset (-1, 0, +1 per axis)
+// is packed into the top 5 bits.
+constexpr uint32_t kIdxBits = 27;
+constexpr uint32_t kIdxMask = (1u << kIdxBits) - 1u;
+
+__device__ __forceinline__ uint32_t shift_code(const GridDev& g, float shx, float shy, float shz) {
+    const int cx = shx < 0.0f ? 0 : (shx > 0.0f ? 2 : 1);
+    const int cy = shy < 0.0f ? 0 : (shy > 0.0f ? 2 : 1);
+    const int cz = shz < 0.0f ? 0 : (shz > 0.0f ? 2 : 1);
+    return (uint32_t)(cx + 3 * cy + 9 * cz);
+}
+
+__device__ __forceinline__ void decode_entry(const GridDev& g, uint32_t e, uint32_t& j, float& shx, float& shy,
+                                             float& shz) {
+    if (!g.periodic) {
+        j = e;
+        shx = shy = shz = 0.0f;
+        return;
+    }
+    j = e & kIdxMask;
+    const uint32_t code = e >> kIdxBits;
+    const int cx = (int)(code % 3u), cy = (int)((code / 3u) % 3u), cz = (int)(code / 9u);
+    shx = cx == 0 ? -g.scale[0] : (cx == 2 ? g.scale[0] : 0.0f);
+    shy = cy == 0 ? -g.scale[1] : (cy == 2 ? g.scale[1] : 0.0f);
+    shz = cz == 0 ? -g.scale[2] : (cz == 2 ? g.scale[2] : 0.0f);
+}
+
+// Fluid density term of neighbour j (computeDensities, cuda/src/algorithm/Algorithm.cu:17-54); returns false when j
+// fails the support test r^2 <= (2 h_j)^2.
+__device__ __forceinline__ bool density_term(const StepArgs& a, float4 pi, uint32_t j, float shx, float shy,
+                                             float shz, float& rho) {
+    const float4 pj = __ldg(a.ph + j);
+    const bool periodic = a.grid.periodic;
+    const float xj = periodic ? pj.x + shx : pj.x;
+    const float yj = periodic ? pj.y + shy : pj.y;
+    const float zj = periodic ? pj.z + shz : pj.z;
+    const float dx = xj - pi.x, dy = yj - pi.y, dz = zj - pi.z;
+    const float r2 = dist2(dx, dy, dz);
+    const float twoh = pj.w + pj.w;
+    if (r2 > twoh * twoh) return false;
+    const float4 kj = __ldg(a.kc + j);
+    const float w = kernel_w(sqrtf(r2), kj.x, kj.y);
+    rho = fmaf(kj.w, w, rho);
+    return true;
+}
+
+// The candidate cells of the density/force passes: reference cells of [x - 2h_i, x + 2h_i].
+template <class Body>
+__device__ __forceinline__ void fluid_candidates(const StepArgs& a, const CellsDev& c, float4 pi, Body&& body) {
+    const float R = pi.w + pi.w;
+    for_each_cell<true>(a.grid, c.start, c.end, c.hmax, c.ex[0], c.ex[1], pi.x, pi.y, pi.z, R, 2.0f * *c.hmax_all,
+                        0.0f, body);
+}
+
 // computeDensities (cuda/src/algorithm/Algorithm.cu:17-54) + computeBoundaryDensityContribution
-// (cuda/src/algorithm/BoundaryAlgorithm.cu:15-51), then p/rho^2 for the force pass.
-__global__ void __launch_bounds__(256) k_density(StepArgs a, CellsDev c, BoundaryDev b) {
+// (cuda/src/algorithm/BoundaryAlgorithm.cu:15-51), then p/rho^2 for the force pass. The candidate scan records the
+// accepted neighbours (self included) in the particle's list; the density is then summed over the list, which
+// keeps the scan loop free of the kernel evaluation (the divergent part) and the sum in candidate order.
+__global__ void __launch_bounds__(256) k_density(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     const float4 pi = a.ph[i];
-    const float R = pi.w + pi.w;
-    const uint32_t ex0 = c.ex[0], ex1 = c.ex[1];
-    const float hall = *c.hmax_all;
     const bool periodic = a.grid.periodic;
+    uint32_t cnt = 0;
+    uint32_t* col = nl.idx + i;
+    const uint32_t stride = nl.stride, maxn = nl.maxn;
+    fluid_candidates(a, c, pi, [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
+        const uint32_t code = periodic ? (shift_code(a.grid, shx, shy, shz) << kIdxBits) : 0u;
+        for (uint32_t j = jb; j < je; ++j) {
+            const float4 pj = __ldg(a.ph + j);
+            const float xj = periodic ? pj.x + shx : pj.x;
+            const float yj = periodic ? pj.y + shy : pj.y;
+            const float zj = periodic ? pj.z + shz : pj.z;
+            const float dx = xj - pi.x, dy = yj - pi.y, dz = zj - pi.z;
+            const float r2 = dist2(dx, dy, dz);
+            const float twoh = pj.w + pj.w;
+            if (r2 > twoh * twoh) continue;
+            if (cnt < maxn) col[(size_t)cnt * stride] = j | code;
+            cnt++;
+        }
+    });
+    nl.cnt[i] = cnt;
     float rho = 0.0f;
-    for_each_cell<true>(a.grid, c.start, c.end, c.hmax, ex0, ex1, pi.x, pi.y, pi.z, R, 2.0f * hall, 0.0f,
-                        [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
-                            for (uint32_t j = jb; j < je; ++j) {
-                                const float4 pj = __ldg(a.ph + j);
-                                const float xj = periodic ? pj.x + shx : pj.x;
-                                const float yj = periodic ? pj.y + shy : pj.y;
-                                const float zj = periodic ? pj.z + shz : pj.z;
-                                const float dx = xj - pi.x, dy = yj - pi.y, dz = zj - pi.z;
-                                const float r2 = dist2(dx, dy, dz);
-                                const float twoh = pj.w + pj.w;
-                                if (r2 > twoh * twoh) continue;
-                                const float4 kj = __ldg(a.kc + j);
-                                const float w = kernel_w(sqrtf(r2), kj.x, kj.y);
-                                rho = fmaf(kj.w, w, rho);
-                            }
-                        });
+    if (cnt <= maxn) {
+        for (uint32_t k = 0; k < cnt; ++k) {
+            uint32_t j;
+            float shx, shy, shz;
+            decode_entry(a.grid, __ldg(col + (size_t)k * stride), j, shx, shy, shz);
+            density_term(a, pi, j, shx, shy, shz, rho);
+        }
+    } else {
+        fluid_candidates(a, c, pi, [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
+            for (uint32_t j = jb; j < je; ++j) density_term(a, pi, j, shx, shy, shz, rho);
+        });
+    }
+    const float R = pi.w + pi.w;
     float rb = 0.0f;
     if (boundary_near(a.grid, b, pi.x, pi.y, pi.z, R)) {
         const float4 ki = a.kc[i];
@@ -285,13 +354,84 @@ __global__ void __launch_bounds__(256) k_density(StepArgs a, CellsDev c, Boundar
     a.rp[i] = make_float2(rh, pressure_term(rh, a.phys.rho0, a.phys.B));
 }
 
+// Per-particle constants and accumulators of the force pass.
+struct ForceAcc {
+    float apx, apy, apz, avx, avy, avz, asx, asy, asz;
+};
+
+// Pressure, viscosity and cohesion terms of fluid neighbour j (cuda/src/algorithm/Algorithm.cu:56-221).
+template <bool kMorris>
+__device__ __forceinline__ void force_term(const StepArgs& a, float4 pi, float4 vi, float rhoi, float pti, float Ki,
+                                           float ei, bool visc_on, bool sigma_on, uint32_t j, float shx, float shy,
+                                           float shz, ForceAcc& f) {
+    const bool periodic = a.grid.periodic;
+    const float4 pj = __ldg(a.ph + j);
+    const float xj = periodic ? pj.x + shx : pj.x;
+    const float yj = periodic ? pj.y + shy : pj.y;
+    const float zj = periodic ? pj.z + shz : pj.z;
+    const float dx = pi.x - xj, dy = pi.y - yj, dz = pi.z - zj;
+    const float r2 = dist2(dx, dy, dz);
+    const float twoh = pj.w + pj.w;
+    if (r2 > twoh * twoh) return;
+    const float4 kj = __ldg(a.kc + j);
+    const float2 rpj = __ldg(a.rp + j);
+    const float r = sqrtf(r2);
+    float ux, uy, uz;
+    if (r > 0.0f) {
+        const float ir = 1.0f / r;
+        ux = dx * ir;
+        uy = dy * ir;
+        uz = dz * ir;
+    } else {
+        ux = 0.0f;
+        uy = 1.0f;
+        uz = 0.0f;
+    }
+    const float dw = kernel_dw(r, kj.x, kj.z);
+    const float mj = kj.w;
+    {
+        const float sp = (mj * dw) * (pti + rpj.y);
+        f.apx = fmaf(-sp, ux, f.apx);
+        f.apy = fmaf(-sp, uy, f.apy);
+        f.apz = fmaf(-sp, uz, f.apz);
+    }
+    if (visc_on) {
+        const float4 vj = __ldg(a.vm + j);
+        const float vdx = vi.x - vj.x, vdy = vi.y - vj.y, vdz = vi.z - vj.z;
+        const float rhoj = rpj.x;
+        if (!kMorris) {
+            const float comp = fmaf(vdz, dz, fmaf(vdy, dy, vdx * dx));
+            if (comp < 0.0f) {
+                const float nuij = Ki / (rhoi + rhoj);
+                const float piv = (-nuij * comp) / (r2 + ei);
+                const float sv = (mj * piv) * dw;
+                f.avx = fmaf(-sv, ux, f.avx);
+                f.avy = fmaf(-sv, uy, f.avy);
+                f.avz = fmaf(-sv, uz, f.avz);
+            }
+        } else {
+            const float coef = ((mj * a.phys.nu) * (rhoi + rhoj)) / (rhoi * rhoj);
+            const float sv = coef * ((r * dw) / (r2 + ei));
+            f.avx = fmaf(sv, vdx, f.avx);
+            f.avy = fmaf(sv, vdy, f.avy);
+            f.avz = fmaf(sv, vdz, f.avz);
+        }
+    }
+    if (sigma_on) {
+        const float ss = mj * kernel_w(r, kj.x, kj.y);
+        f.asx = fmaf(ss, ux, f.asx);
+        f.asy = fmaf(ss, uy, f.asy);
+        f.asz = fmaf(ss, uz, f.asz);
+    }
+}
+
 // computeExternalAccelerations, computePressureAccelerations, computeViscosityAccelerations,
 // computeSurfaceTensionAccelerations (cuda/src/algorithm/Algorithm.cu:56-232) and
 // computeBoundaryPressureAcceleration / computeBoundaryFrictionAcceleration
-// (cuda/src/algorithm/BoundaryAlgorithm.cu:53-162) in one pass; each term keeps its own accumulator and
-// they are added to gravity in the reference's kernel order.
+// (cuda/src/algorithm/BoundaryAlgorithm.cu:53-162) in one pass over the neighbour list; each term keeps its own
+// accumulator and they are added to gravity in the reference's kernel order.
 template <bool kMorris>
-__global__ void __launch_bounds__(256, 2) k_forces(StepArgs a, CellsDev c, BoundaryDev b) {
+__global__ void __launch_bounds__(256, 2) k_forces(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     const float4 pi = a.ph[i];
@@ -303,75 +443,25 @@ __global__ void __launch_bounds__(256, 2) k_forces(StepArgs a, CellsDev c, Bound
     const float ei = (0.01f * hi) * hi;
     const float R = hi + hi;
     const bool visc_on = a.phys.visc_on, sigma_on = a.phys.sigma_on, periodic = a.grid.periodic;
-    const float nu_k = a.phys.nu;
-    const uint32_t ex0 = c.ex[0], ex1 = c.ex[1];
-    const float hall = *c.hmax_all;
-    float apx = 0.f, apy = 0.f, apz = 0.f, avx = 0.f, avy = 0.f, avz = 0.f, asx = 0.f, asy = 0.f, asz = 0.f;
-    for_each_cell<true>(
-        a.grid, c.start, c.end, c.hmax, ex0, ex1, pi.x, pi.y, pi.z, R, 2.0f * hall, 0.0f,
-        [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
+    ForceAcc f = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    const uint32_t cnt = nl.cnt[i];
+    if (cnt <= nl.maxn) {
+        const uint32_t* col = nl.idx + i;
+        for (uint32_t k = 0; k < cnt; ++k) {
+            uint32_t j;
+            float shx, shy, shz;
+            decode_entry(a.grid, __ldg(col + (size_t)k * nl.stride), j, shx, shy, shz);
+            if (j == i) continue;
+            force_term<kMorris>(a, pi, vi, rhoi, pti, Ki, ei, visc_on, sigma_on, j, shx, shy, shz, f);
+        }
+    } else {
+        fluid_candidates(a, c, pi, [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
             for (uint32_t j = jb; j < je; ++j) {
                 if (j == i) continue;
-                const float4 pj = __ldg(a.ph + j);
-                const float xj = periodic ? pj.x + shx : pj.x;
-                const float yj = periodic ? pj.y + shy : pj.y;
-                const float zj = periodic ? pj.z + shz : pj.z;
-                const float dx = pi.x - xj, dy = pi.y - yj, dz = pi.z - zj;
-                const float r2 = dist2(dx, dy, dz);
-                const float twoh = pj.w + pj.w;
-                if (r2 > twoh * twoh) continue;
-                const float4 kj = __ldg(a.kc + j);
-                const float2 rpj = __ldg(a.rp + j);
-                const float r = sqrtf(r2);
-                float ux, uy, uz;
-                if (r > 0.0f) {
-                    const float ir = 1.0f / r;
-                    ux = dx * ir;
-                    uy = dy * ir;
-                    uz = dz * ir;
-                } else {
-                    ux = 0.0f;
-                    uy = 1.0f;
-                    uz = 0.0f;
-                }
-                const float dw = kernel_dw(r, kj.x, kj.z);
-                const float mj = kj.w;
-                {
-                    const float sp = (mj * dw) * (pti + rpj.y);
-                    apx = fmaf(-sp, ux, apx);
-                    apy = fmaf(-sp, uy, apy);
-                    apz = fmaf(-sp, uz, apz);
-                }
-                if (visc_on) {
-                    const float4 vj = __ldg(a.vm + j);
-                    const float vdx = vi.x - vj.x, vdy = vi.y - vj.y, vdz = vi.z - vj.z;
-                    const float rhoj = rpj.x;
-                    if (!kMorris) {
-                        const float comp = fmaf(vdz, dz, fmaf(vdy, dy, vdx * dx));
-                        if (comp < 0.0f) {
-                            const float nuij = Ki / (rhoi + rhoj);
-                            const float piv = (-nuij * comp) / (r2 + ei);
-                            const float sv = (mj * piv) * dw;
-                            avx = fmaf(-sv, ux, avx);
-                            avy = fmaf(-sv, uy, avy);
-                            avz = fmaf(-sv, uz, avz);
-                        }
-                    } else {
-                        const float coef = ((mj * nu_k) * (rhoi + rhoj)) / (rhoi * rhoj);
-                        const float sv = coef * ((r * dw) / (r2 + ei));
-                        avx = fmaf(sv, vdx, avx);
-                        avy = fmaf(sv, vdy, avy);
-                        avz = fmaf(sv, vdz, avz);
-                    }
-                }
-                if (sigma_on) {
-                    const float ss = mj * kernel_w(r, kj.x, kj.y);
-                    asx = fmaf(ss, ux, asx);
-                    asy = fmaf(ss, uy, asy);
-                    asz = fmaf(ss, uz, asz);
-                }
+                force_term<kMorris>(a, pi, vi, rhoi, pti, Ki, ei, visc_on, sigma_on, j, shx, shy, shz, f);
             }
         });
+    }
     float bpx = 0.f, bpy = 0.f, bpz = 0.f, bfx = 0.f, bfy = 0.f, bfz = 0.f;
     if (boundary_near(a.grid, b, pi.x, pi.y, pi.z, R)) {
         const float4 ki = a.kc[i];
@@ -417,19 +507,19 @@ __global__ void __launch_bounds__(256, 2) k_forces(StepArgs a, CellsDev c, Bound
                              });
     }
     float ax = a.phys.gravity[0], ay = a.phys.gravity[1], az = a.phys.gravity[2];
-    ax = ax + apx;
-    ay = ay + apy;
-    az = az + apz;
+    ax = ax + f.apx;
+    ay = ay + f.apy;
+    az = az + f.apz;
     if (visc_on) {
-        ax = ax + avx;
-        ay = ay + avy;
-        az = az + avz;
+        ax = ax + f.avx;
+        ay = ay + f.avy;
+        az = az + f.avz;
     }
     if (sigma_on) {
-        const float f = a.phys.sigma / mi;
-        ax = ax + f * asx;
-        ay = ay + f * asy;
-        az = az + f * asz;
+        const float fs = a.phys.sigma / mi;
+        ax = ax + fs * f.asx;
+        ay = ay + fs * f.asy;
+        az = az + fs * f.asz;
     }
     ax = ax + bpx;
     ay = ay + bpy;
@@ -441,11 +531,12 @@ __global__ void __launch_bounds__(256, 2) k_forces(StepArgs a, CellsDev c, Bound
     a.acc[i] = make_float4(ax, ay, az, 0.0f);
 }
 
-cudaError_t launch_forces(bool morris, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c, BoundaryDev b) {
+cudaError_t launch_forces(bool morris, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c, BoundaryDev b,
+                          NbrDev nl) {
     if (morris)
-        k_forces<true><<<blocks, 256, 0, stream>>>(a, c, b);
+        k_forces<true><<<blocks, 256, 0, stream>>>(a, c, b, nl);
     else
-        k_forces<false><<<blocks, 256, 0, stream>>>(a, c, b);
+        k_forces<false><<<blocks, 256, 0, stream>>>(a, c, b, nl);
     return cudaGetLastError();
 }
 
