@@ -39,8 +39,8 @@ struct CellsDev {
     const uint32_t* start;
     const uint32_t* end;
     const float* hmax;       // max smoothing length of the members of each sub-cell
+    const float* hmax_ref;   // max smoothing length of the members of each reference cell (0: empty)
     const uint32_t* ex;      // [2] reference cells excluded by the reference's cell-boundary quirk
-    const float* hmax_all;   // [1] max smoothing length over all particles
 };
 
 struct BoundaryDev {
@@ -155,9 +155,9 @@ __device__ __forceinline__ float clampf_(float x, float lo, float hi) {
     return x > hi ? hi : x;
 }
 
-// Reference-cell range of the query box [x - R, x + R] on one axis (NeighborGrid.cuh:96-101), as the
-// sub-cell range [2 lo, 2 hi + 1]. Returns false for an empty range.
-__device__ __forceinline__ bool box_axis(const GridDev& g, int a, float p, float R, int32_t& slo, int32_t& shi) {
+// Reference-cell range [lo, hi] of the query box [x - R, x + R] on one axis (NeighborGrid.cuh:96-101).
+// Returns false for an empty range.
+__device__ __forceinline__ bool box_axis(const GridDev& g, int a, float p, float R, int32_t& lo, int32_t& hi) {
     const float rel = p - g.dmin[a];
     const float lof = clampf_((rel - R) / g.cs[a], -1.0e7f, 1.0e7f);
     const float hif = clampf_((rel + R) / g.cs[a], -1.0e7f, 1.0e7f);
@@ -172,83 +172,103 @@ __device__ __forceinline__ bool box_axis(const GridDev& g, int a, float p, float
         h = (int32_t)floorf(hif);
         if (h - l + 1 > g.gs[a]) h = l + g.gs[a] - 1;
     }
-    slo = 2 * l;
-    shi = 2 * h + 1;
+    lo = l;
+    hi = h;
     return l <= h;
 }
 
-// Narrows a sub-cell range to the sub-cells whose slab can hold a point within Rc of p (conservative; only
-// ever skips sub-cells none of whose members can pass the distance test, so sums are unchanged).
-__device__ __forceinline__ void trim_axis(const GridDev& g, int a, float p, float Rc, int32_t& slo, int32_t& shi) {
-    const float rel = p - g.dmin[a];
-    const float m = g.cull_margin;
-    const int32_t lo2 = (int32_t)ceilf((rel - Rc - m) / g.w[a] - 1.0f);
-    const int32_t hi2 = (int32_t)floorf((rel + Rc + m) / g.w[a]);
-    slo = lo2 > slo ? lo2 : slo;
-    shi = hi2 < shi ? hi2 : shi;
+// Wraps a (possibly out-of-range) cell index of a periodic grid into [0, n) and returns the image offset.
+__device__ __forceinline__ int32_t wrap_cell(int32_t c, int32_t n, float L, bool periodic, float& sh) {
+    sh = 0.0f;
+    if (periodic) {
+        if (c < 0) {
+            c += n;
+            sh = -L;
+        } else if (c >= n) {
+            c -= n;
+            sh = L;
+        }
+    }
+    return c;
 }
 
-// Visits the candidate cells of a query in the canonical order (sub-cells z, y, x over the reference box),
-// skipping the excluded reference cells and empty cells. With cull, sub-cells that cannot hold a member
-// within 2*hmax(cell) (or within Rfix when Rfix > 0) of p are skipped as well.
-// body(begin, end, sx, sy, sz) gets the member range [begin, end) and the periodic image shifts.
+// Distance from p to the interval [lo, lo + w] widened by m on both sides.
+__device__ __forceinline__ float gap1(float p, float lo, float w, float m) {
+    return fmaxf(fmaxf((lo - m) - p, p - (lo + w + m)), 0.0f);
+}
+
+// Visits the candidate cells of a query in the canonical order: the reference cells of the box [x-R, x+R]
+// (z, y, x order), skipping the cells excluded by the reference's cell-boundary quirk, and within each the
+// 2x2x2 sub-cells (z, y, x order) that hold particles. With kCull, a reference cell or sub-cell that cannot
+// hold a member within reach of p is skipped: reach = Rfix when Rfix > 0, else 2 * (max h of the cell). Culling
+// never skips a member that passes a support test, so sums over the visited members are unchanged.
+// body(begin, end, shx, shy, shz) gets the member range and the periodic image offsets.
 template <bool kCull, class Body>
 __device__ __forceinline__ void for_each_cell(const GridDev& g, const uint32_t* __restrict__ start,
                                               const uint32_t* __restrict__ end, const float* __restrict__ hmax,
-                                              uint32_t ex0, uint32_t ex1, float px, float py, float pz, float R,
-                                              float Rtrim, float Rfix, Body&& body) {
+                                              const float* __restrict__ hmax_ref, uint32_t ex0, uint32_t ex1,
+                                              float px, float py, float pz, float R, float Rfix, Body&& body) {
     int32_t lo[3], hi[3];
     const float p[3] = {px, py, pz};
     bool ok = true;
 #pragma unroll
-    for (int a = 0; a < 3; a++) {
-        ok &= box_axis(g, a, p[a], R, lo[a], hi[a]);
-        if (kCull) trim_axis(g, a, p[a], Rtrim, lo[a], hi[a]);
-    }
+    for (int a = 0; a < 3; a++) ok &= box_axis(g, a, p[a], R, lo[a], hi[a]);
     if (!ok) return;
-    for (int32_t sz = lo[2]; sz <= hi[2]; ++sz) {
-        int32_t cz = sz;
-        float shz = 0.0f;
-        if (g.periodic) {
-            if (cz < 0) { cz += g.sgs[2]; shz = -g.scale[2]; }
-            else if (cz >= g.sgs[2]) { cz -= g.sgs[2]; shz = g.scale[2]; }
-        }
-        for (int32_t sy = lo[1]; sy <= hi[1]; ++sy) {
-            int32_t cy = sy;
-            float shy = 0.0f;
-            if (g.periodic) {
-                if (cy < 0) { cy += g.sgs[1]; shy = -g.scale[1]; }
-                else if (cy >= g.sgs[1]) { cy -= g.sgs[1]; shy = g.scale[1]; }
-            }
-            for (int32_t sx = lo[0]; sx <= hi[0]; ++sx) {
-                int32_t cx = sx;
-                float shx = 0.0f;
-                if (g.periodic) {
-                    if (cx < 0) { cx += g.sgs[0]; shx = -g.scale[0]; }
-                    else if (cx >= g.sgs[0]) { cx -= g.sgs[0]; shx = g.scale[0]; }
-                    // a position more than one period outside the box (never after the first drift) has no cells
-                    if (cx < 0 || cx >= g.sgs[0] || cy < 0 || cy >= g.sgs[1] || cz < 0 || cz >= g.sgs[2]) continue;
-                } else {
-                    const uint32_t rk = (uint32_t)((cx >> 1) + g.gs[0] * ((cy >> 1) + g.gs[1] * (cz >> 1)));
-                    if (rk == ex0 || rk == ex1) continue;
-                }
-                const uint32_t lin = (uint32_t)cx + (uint32_t)g.sgs[0] * ((uint32_t)cy + (uint32_t)g.sgs[1] * (uint32_t)cz);
-                const uint32_t b = __ldg(start + lin);
-                if (b == kEmpty) continue;
+    const bool periodic = g.periodic;
+    const float m = g.cull_margin;
+    for (int32_t rz = lo[2]; rz <= hi[2]; ++rz) {
+        float shz;
+        const int32_t cz = wrap_cell(rz, g.gs[2], g.scale[2], periodic, shz);
+        if (cz < 0 || cz >= g.gs[2]) continue;
+        for (int32_t ry = lo[1]; ry <= hi[1]; ++ry) {
+            float shy;
+            const int32_t cy = wrap_cell(ry, g.gs[1], g.scale[1], periodic, shy);
+            if (cy < 0 || cy >= g.gs[1]) continue;
+            for (int32_t rx = lo[0]; rx <= hi[0]; ++rx) {
+                float shx;
+                const int32_t cx = wrap_cell(rx, g.gs[0], g.scale[0], periodic, shx);
+                if (cx < 0 || cx >= g.gs[0]) continue;
+                const uint32_t rk = (uint32_t)cx + (uint32_t)g.gs[0] * ((uint32_t)cy + (uint32_t)g.gs[1] * (uint32_t)cz);
+                if (!periodic && (rk == ex0 || rk == ex1)) continue;
+                // sub-cell ranges of this reference cell, narrowed to the slabs within reach
+                int32_t s0[3] = {2 * cx, 2 * cy, 2 * cz}, s1[3] = {2 * cx + 1, 2 * cy + 1, 2 * cz + 1};
                 if (kCull) {
-                    const float reach = Rfix > 0.0f ? Rfix : 2.0f * __ldg(hmax + lin);
-                    // distance from p to the (widened) box of the sub-cell, in the unshifted frame of the cell
-                    const float bx0 = g.dmin[0] + (float)cx * g.w[0] - g.cull_margin + shx;
-                    const float by0 = g.dmin[1] + (float)cy * g.w[1] - g.cull_margin + shy;
-                    const float bz0 = g.dmin[2] + (float)cz * g.w[2] - g.cull_margin + shz;
-                    const float bw = 2.0f * g.cull_margin;
-                    const float ddx = fmaxf(fmaxf(bx0 - px, px - (bx0 + g.w[0] + bw)), 0.0f);
-                    const float ddy = fmaxf(fmaxf(by0 - py, py - (by0 + g.w[1] + bw)), 0.0f);
-                    const float ddz = fmaxf(fmaxf(bz0 - pz, pz - (bz0 + g.w[2] + bw)), 0.0f);
-                    const float d2 = ddx * ddx + ddy * ddy + ddz * ddz;
-                    if (d2 > reach * reach * 1.0001f) continue;
+                    const float hr = __ldg(hmax_ref + rk);
+                    if (hr <= 0.0f) continue;  // no particles in this reference cell
+                    const float reach = (Rfix > 0.0f ? Rfix : 2.0f * hr) * 1.00005f;
+                    const float sh[3] = {shx, shy, shz};
+                    const int32_t c3[3] = {cx, cy, cz};
+                    float d2 = 0.0f;
+                    bool any = true;
+#pragma unroll
+                    for (int a = 0; a < 3; a++) {
+                        const float base = g.dmin[a] + (float)c3[a] * g.cs[a] + sh[a];
+                        const float d = gap1(p[a], base, g.cs[a], m);
+                        d2 += d * d;
+                        const bool k0 = gap1(p[a], base, g.w[a], m) <= reach;
+                        const bool k1 = gap1(p[a], base + g.w[a], g.w[a], m) <= reach;
+                        s0[a] = k0 ? 2 * c3[a] : 2 * c3[a] + 1;
+                        s1[a] = k1 ? 2 * c3[a] + 1 : 2 * c3[a];
+                        any &= (k0 || k1);
+                    }
+                    if (!any || d2 > reach * reach) continue;
                 }
-                body(b, __ldg(end + lin), shx, shy, shz);
+                for (int32_t sz = s0[2]; sz <= s1[2]; ++sz)
+                    for (int32_t sy = s0[1]; sy <= s1[1]; ++sy)
+                        for (int32_t sx = s0[0]; sx <= s1[0]; ++sx) {
+                            const uint32_t lin =
+                                (uint32_t)sx + (uint32_t)g.sgs[0] * ((uint32_t)sy + (uint32_t)g.sgs[1] * (uint32_t)sz);
+                            const uint32_t b = __ldg(start + lin);
+                            if (b == kEmpty) continue;
+                            if (kCull) {
+                                const float reach = (Rfix > 0.0f ? Rfix : 2.0f * __ldg(hmax + lin)) * 1.00005f;
+                                const float dx = gap1(px, g.dmin[0] + (float)sx * g.w[0] + shx, g.w[0], m);
+                                const float dy = gap1(py, g.dmin[1] + (float)sy * g.w[1] + shy, g.w[1], m);
+                                const float dz = gap1(pz, g.dmin[2] + (float)sz * g.w[2] + shz, g.w[2], m);
+                                if (dx * dx + dy * dy + dz * dz > reach * reach) continue;
+                            }
+                            body(b, __ldg(end + lin), shx, shy, shz);
+                        }
             }
         }
     }

@@ -43,7 +43,7 @@ struct ReorderArgs {
     uint32_t* start;
     uint32_t* end;
     float* hmax;
-    float* hmax_all;
+    float* hmax_ref;
 };
 
 __global__ void k_integrate_keys(StepArgs a, float dt, float pending_half, int has_pending, uint32_t* keys,

@@ -67,7 +67,7 @@ __device__ float vorticity_mag(const StepArgs& a, const CellsDev& c, uint32_t i)
     kernel_consts(hi, invh, wc, dwc);
     float d[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     int valid = 0;
-    for_each_cell<kCull>(a.grid, c.start, c.end, c.hmax, c.ex[0], c.ex[1], pi.x, pi.y, pi.z, hi, hi, hi,
+    for_each_cell<kCull>(a.grid, c.start, c.end, c.hmax, c.hmax_ref, c.ex[0], c.ex[1], pi.x, pi.y, pi.z, hi, hi,
                          [&](uint32_t jb, uint32_t je, float, float, float) {
                              for (uint32_t j = jb; j < je; ++j) {
                                  if (j == i) continue;
@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(256) k_merge_candidates(StepArgs a, CellsDev c
     const float he = pe.w;
     float best = 3.402823466e38f;
     uint32_t bj = kNone, bid = 0xffffffffu;
-    for_each_cell<true>(a.grid, c.start, c.end, c.hmax, c.ex[0], c.ex[1], pe.x, pe.y, pe.z, he, he, he,
+    for_each_cell<true>(a.grid, c.start, c.end, c.hmax, c.hmax_ref, c.ex[0], c.ex[1], pe.x, pe.y, pe.z, he, he,
                         [&](uint32_t jb, uint32_t je, float, float, float) {
                             for (uint32_t j = jb; j < je; ++j) {
                                 if (j == e) continue;

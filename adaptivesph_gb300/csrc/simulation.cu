@@ -146,7 +146,8 @@ struct asph_simulation {
     uint32_t* cell_end = nullptr;
     float* cell_hmax = nullptr;
     uint32_t cells_alloc = 0;
-    float* hmax_all = nullptr;
+    float* hmax_ref = nullptr;  // [gs.x * gs.y * gs.z] max h per reference cell
+    uint32_t refcells_alloc = 0;
     uint32_t* ex = nullptr;
     unsigned long long* q3 = nullptr;
     uint32_t* err = nullptr;
@@ -226,7 +227,7 @@ struct asph_simulation {
         return a;
     }
 
-    CellsDev cells() const { return CellsDev{cell_start, cell_end, cell_hmax, ex, hmax_all}; }
+    CellsDev cells() const { return CellsDev{cell_start, cell_end, cell_hmax, hmax_ref, ex}; }
 
     NbrDev nbrs() const { return NbrDev{nbr_idx, nbr_cnt, cap, maxn}; }
 
@@ -342,6 +343,14 @@ void make_phys(const asph_parameters& P, PhysDev& ph) {
 }
 
 asph_status alloc_cells(asph_simulation* s) {
+    const uint32_t refcells = (uint32_t)(s->grid.gs[0] * s->grid.gs[1] * s->grid.gs[2]);
+    if (refcells > s->refcells_alloc) {
+        dfree(s->hmax_ref);
+        s->refcells_alloc = 0;
+        asph_status st0 = dalloc(s->hmax_ref, refcells);
+        if (st0 != ASPH_OK) return st0;
+        s->refcells_alloc = refcells;
+    }
     if (s->grid.ncells <= s->cells_alloc) return ASPH_OK;
     dfree(s->cell_start);
     dfree(s->cell_end);
@@ -469,7 +478,7 @@ asph_status build_grid(asph_simulation* s, bool integrate, float dt, bool carry_
     CK(cudaMemsetAsync(s->cell_start, 0xff, sizeof(uint32_t) * s->grid.ncells, s->stream));
     CK(cudaMemsetAsync(s->cell_end, 0, sizeof(uint32_t) * s->grid.ncells, s->stream));
     CK(cudaMemsetAsync(s->cell_hmax, 0, sizeof(float) * s->grid.ncells, s->stream));
-    CK(cudaMemsetAsync(s->hmax_all, 0, sizeof(float), s->stream));
+    CK(cudaMemsetAsync(s->hmax_ref, 0, sizeof(float) * s->refcells_alloc, s->stream));
     k_excluded<<<1, 1, 0, s->stream>>>(s->q3, nullptr, n, s->ex, s->grid.periodic);
     CK_LAUNCH("k_excluded");
     ReorderArgs r;
@@ -484,7 +493,7 @@ asph_status build_grid(asph_simulation* s, bool integrate, float dt, bool carry_
     r.start = s->cell_start;
     r.end = s->cell_end;
     r.hmax = s->cell_hmax;
-    r.hmax_all = s->hmax_all;
+    r.hmax_ref = s->hmax_ref;
     const int nxt = 1 - s->cur;
     StepArgs b = s->args(nxt);
     h = s->tic();
@@ -724,7 +733,7 @@ void destroy(asph_simulation* s) {
     dfree(s->cell_start);
     dfree(s->cell_end);
     dfree(s->cell_hmax);
-    dfree(s->hmax_all);
+    dfree(s->hmax_ref);
     dfree(s->ex);
     dfree(s->q3);
     dfree(s->err);
@@ -963,7 +972,6 @@ asph_status asph_simulation_create(const asph_parameters* parameters, const floa
         s->sort_mem = mem;
         sort_scratch_bind(s->ss, mem, sort_items);
     }
-    TRY(dalloc(s->hmax_all, 1));
     TRY(dalloc(s->ex, 4));
     TRY(dalloc(s->q3, 2));
     TRY(dalloc(s->err, 1));
@@ -989,7 +997,6 @@ asph_status asph_simulation_create(const asph_parameters* parameters, const floa
         return cuda_fail(e, "cudaMallocHost");
     }
     CK(cudaMemsetAsync(s->err, 0, sizeof(uint32_t), s->stream));
-    CK(cudaMemsetAsync(s->hmax_all, 0, sizeof(float), s->stream));
     s->bcap = 0;
     TRY(setup_boundary(s, boundary, boundary_count));
     if (count > 0) {

@@ -173,7 +173,9 @@ __global__ void __launch_bounds__(256) k_reorder_cells(StepArgs a, ReorderArgs r
     }
     if ((threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) {
         atomicMax(reinterpret_cast<int*>(r.hmax) + lin, __float_as_int(hm));
-        atomicMax(reinterpret_cast<int*>(r.hmax_all), __float_as_int(hm));
+        const uint32_t sx = compact1by2(key), sy = compact1by2(key >> 1), sz = compact1by2(key >> 2);
+        const uint32_t rk = (sx >> 1) + (uint32_t)a.grid.gs[0] * ((sy >> 1) + (uint32_t)a.grid.gs[1] * (sz >> 1));
+        atomicMax(reinterpret_cast<int*>(r.hmax_ref) + rk, __float_as_int(hm));
     }
 }
 
@@ -284,15 +286,13 @@ __device__ __forceinline__ bool density_term(const StepArgs& a, float4 pi, uint3
 template <class Body>
 __device__ __forceinline__ void fluid_candidates(const StepArgs& a, const CellsDev& c, float4 pi, Body&& body) {
     const float R = pi.w + pi.w;
-    for_each_cell<true>(a.grid, c.start, c.end, c.hmax, c.ex[0], c.ex[1], pi.x, pi.y, pi.z, R, 2.0f * *c.hmax_all,
-                        0.0f, body);
+    for_each_cell<true>(a.grid, c.start, c.end, c.hmax, c.hmax_ref, c.ex[0], c.ex[1], pi.x, pi.y, pi.z, R, 0.0f, body);
 }
 
 // computeDensities (cuda/src/algorithm/Algorithm.cu:17-54) + computeBoundaryDensityContribution
-// (cuda/src/algorithm/BoundaryAlgorithm.cu:15-51), then p/rho^2 for the force pass. The candidate scan records the
-// accepted neighbours (self included) in the particle's list; the density is then summed over the list, which
-// keeps the scan loop free of the kernel evaluation (the divergent part) and the sum in candidate order.
-__global__ void __launch_bounds__(256) k_density(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
+// (cuda/src/algorithm/BoundaryAlgorithm.cu:15-51), then p/rho^2 for the force pass. The scan also records the
+// accepted neighbours (self included) in the particle's list, in candidate order, for the force pass.
+__global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     const float4 pi = a.ph[i];
@@ -300,41 +300,22 @@ __global__ void __launch_bounds__(256) k_density(StepArgs a, CellsDev c, Boundar
     uint32_t cnt = 0;
     uint32_t* col = nl.idx + i;
     const uint32_t stride = nl.stride, maxn = nl.maxn;
+    float rho = 0.0f;
     fluid_candidates(a, c, pi, [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
         const uint32_t code = periodic ? (shift_code(a.grid, shx, shy, shz) << kIdxBits) : 0u;
         for (uint32_t j = jb; j < je; ++j) {
-            const float4 pj = __ldg(a.ph + j);
-            const float xj = periodic ? pj.x + shx : pj.x;
-            const float yj = periodic ? pj.y + shy : pj.y;
-            const float zj = periodic ? pj.z + shz : pj.z;
-            const float dx = xj - pi.x, dy = yj - pi.y, dz = zj - pi.z;
-            const float r2 = dist2(dx, dy, dz);
-            const float twoh = pj.w + pj.w;
-            if (r2 > twoh * twoh) continue;
+            if (!density_term(a, pi, j, shx, shy, shz, rho)) continue;
             if (cnt < maxn) col[(size_t)cnt * stride] = j | code;
             cnt++;
         }
     });
     nl.cnt[i] = cnt;
-    float rho = 0.0f;
-    if (cnt <= maxn) {
-        for (uint32_t k = 0; k < cnt; ++k) {
-            uint32_t j;
-            float shx, shy, shz;
-            decode_entry(a.grid, __ldg(col + (size_t)k * stride), j, shx, shy, shz);
-            density_term(a, pi, j, shx, shy, shz, rho);
-        }
-    } else {
-        fluid_candidates(a, c, pi, [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
-            for (uint32_t j = jb; j < je; ++j) density_term(a, pi, j, shx, shy, shz, rho);
-        });
-    }
     const float R = pi.w + pi.w;
     float rb = 0.0f;
     if (boundary_near(a.grid, b, pi.x, pi.y, pi.z, R)) {
         const float4 ki = a.kc[i];
         const float cut = R * R;
-        for_each_cell<false>(a.grid, b.start, b.end, nullptr, b.ex0, b.ex1, pi.x, pi.y, pi.z, R, 0.0f, 0.0f,
+        for_each_cell<false>(a.grid, b.start, b.end, nullptr, nullptr, b.ex0, b.ex1, pi.x, pi.y, pi.z, R, 0.0f,
                              [&](uint32_t kb, uint32_t ke, float shx, float shy, float shz) {
                                  for (uint32_t k = kb; k < ke; ++k) {
                                      const float4 pb = __ldg(b.pos + k);
@@ -431,7 +412,7 @@ __device__ __forceinline__ void force_term(const StepArgs& a, float4 pi, float4 
 // (cuda/src/algorithm/BoundaryAlgorithm.cu:53-162) in one pass over the neighbour list; each term keeps its own
 // accumulator and they are added to gravity in the reference's kernel order.
 template <bool kMorris>
-__global__ void __launch_bounds__(256, 2) k_forces(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
+__global__ void __launch_bounds__(256, 3) k_forces(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     const float4 pi = a.ph[i];
@@ -466,7 +447,7 @@ __global__ void __launch_bounds__(256, 2) k_forces(StepArgs a, CellsDev c, Bound
     if (boundary_near(a.grid, b, pi.x, pi.y, pi.z, R)) {
         const float4 ki = a.kc[i];
         const float cut = R * R;
-        for_each_cell<false>(a.grid, b.start, b.end, nullptr, b.ex0, b.ex1, pi.x, pi.y, pi.z, R, 0.0f, 0.0f,
+        for_each_cell<false>(a.grid, b.start, b.end, nullptr, nullptr, b.ex0, b.ex1, pi.x, pi.y, pi.z, R, 0.0f,
                              [&](uint32_t kb, uint32_t ke, float shx, float shy, float shz) {
                                  for (uint32_t k = kb; k < ke; ++k) {
                                      const float4 pb = __ldg(b.pos + k);
@@ -549,8 +530,8 @@ __global__ void __launch_bounds__(256) k_neighbor_counts(StepArgs a, CellsDev c,
         const float4 pi = a.ph[i];
         const float R = pi.w + pi.w;
         const bool periodic = a.grid.periodic;
-        for_each_cell<true>(a.grid, c.start, c.end, c.hmax, c.ex[0], c.ex[1], pi.x, pi.y, pi.z, R, 2.0f * *c.hmax_all,
-                            0.0f, [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
+        for_each_cell<true>(a.grid, c.start, c.end, c.hmax, c.hmax_ref, c.ex[0], c.ex[1], pi.x, pi.y, pi.z, R, 0.0f,
+                            [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
                                 for (uint32_t j = jb; j < je; ++j) {
                                     if (j == i) continue;
                                     const float4 pj = __ldg(a.ph + j);

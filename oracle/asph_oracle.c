@@ -136,13 +136,17 @@ void orc_cell_of(const orc_grid* g, const float* p, uint32_t* key, uint32_t* ref
 /* ------------------------------------------------------------------ neighbour-cell iterator */
 /* forEachFluidNeighbor / forEachBoundaryNeighbor (cuda/src/simulation/neighbors/NeighborGrid.cuh:90-164): the
  * candidate cells are the reference cells overlapping [x - R, x + R] (truncated toward zero, clamped to the
- * grid), minus the cells the reference's boundary pass leaves unset. They are visited here as their sub-cells
- * in z, y, x order; members of a sub-cell in cell-sorted order. */
+ * grid), minus the cells the reference's boundary pass leaves unset. The canonical visiting order: reference
+ * cells in z, y, x order; within each, its 2x2x2 sub-cells in z, y, x order; members of a sub-cell in
+ * cell-sorted order. */
 typedef struct orc_iter {
     const orc_grid* g;
     const uint32_t *start, *end;
     uint32_t ex0, ex1;
-    int32_t lo[3], hi[3], s[3];
+    int32_t lo[3], hi[3], r[3]; /* reference-cell box and the current reference cell (unwrapped) */
+    int32_t c[3];               /* current reference cell, wrapped */
+    float sh[3];                /* its periodic image offset */
+    int q;                      /* next sub-cell of the current reference cell, 0..8 */
     int empty;
 } orc_iter;
 
@@ -185,12 +189,61 @@ static void it_init(orc_iter* it, const orc_grid* g, const uint32_t* start, cons
         if (l > h) {
             it->empty = 1;
         }
-        it->lo[a] = 2 * l;
-        it->hi[a] = 2 * h + 1;
+        it->lo[a] = l;
+        it->hi[a] = h;
     }
-    it->s[0] = it->lo[0] - 1;
-    it->s[1] = it->lo[1];
-    it->s[2] = it->lo[2];
+    it->r[0] = it->lo[0] - 1;
+    it->r[1] = it->lo[1];
+    it->r[2] = it->lo[2];
+    it->q = 8;
+}
+
+/* moves to the next reference cell of the box that is neither excluded nor outside a periodic grid */
+static int it_next_ref(orc_iter* it)
+{
+    const orc_grid* g = it->g;
+    for (;;) {
+        if (++it->r[0] > it->hi[0]) {
+            it->r[0] = it->lo[0];
+            if (++it->r[1] > it->hi[1]) {
+                it->r[1] = it->lo[1];
+                if (++it->r[2] > it->hi[2]) {
+                    it->empty = 1;
+                    return 0;
+                }
+            }
+        }
+        int ok = 1;
+        for (int a = 0; a < 3; a++) {
+            int32_t c = it->r[a];
+            float sh = 0.0f;
+            if (g->periodic) {
+                if (c < 0) {
+                    c += g->gs[a];
+                    sh = -g->scale[a];
+                } else if (c >= g->gs[a]) {
+                    c -= g->gs[a];
+                    sh = g->scale[a];
+                }
+                if (c < 0 || c >= g->gs[a]) {
+                    ok = 0;
+                }
+            }
+            it->c[a] = c;
+            it->sh[a] = sh;
+        }
+        if (!ok) {
+            continue;
+        }
+        if (!g->periodic) {
+            const uint32_t rk = (uint32_t)(it->c[0] + g->gs[0] * (it->c[1] + g->gs[1] * it->c[2]));
+            if (rk == it->ex0 || rk == it->ex1) {
+                continue;
+            }
+        }
+        it->q = 0;
+        return 1;
+    }
 }
 
 static int it_next(orc_iter* it, uint32_t* b, uint32_t* e, float sh[3])
@@ -200,44 +253,18 @@ static int it_next(orc_iter* it, uint32_t* b, uint32_t* e, float sh[3])
         return 0;
     }
     for (;;) {
-        if (++it->s[0] > it->hi[0]) {
-            it->s[0] = it->lo[0];
-            if (++it->s[1] > it->hi[1]) {
-                it->s[1] = it->lo[1];
-                if (++it->s[2] > it->hi[2]) {
-                    it->empty = 1;
-                    return 0;
-                }
-            }
+        if (it->q >= 8 && !it_next_ref(it)) {
+            return 0;
         }
-        int32_t c[3];
-        for (int a = 0; a < 3; a++) {
-            c[a] = it->s[a];
-            sh[a] = 0.0f;
-            if (g->periodic) {
-                if (c[a] < 0) {
-                    c[a] += g->sgs[a];
-                    sh[a] = -g->scale[a];
-                } else if (c[a] >= g->sgs[a]) {
-                    c[a] -= g->sgs[a];
-                    sh[a] = g->scale[a];
-                }
-            }
-        }
-        if (!g->periodic) {
-            const uint32_t rk =
-                (uint32_t)((c[0] >> 1) + g->gs[0] * ((c[1] >> 1) + g->gs[1] * (c[2] >> 1)));
-            if (rk == it->ex0 || rk == it->ex1) {
-                continue;
-            }
-        } else if (c[0] < 0 || c[0] >= g->sgs[0] || c[1] < 0 || c[1] >= g->sgs[1] || c[2] < 0 ||
-                   c[2] >= g->sgs[2]) {
-            continue;
-        }
-        const uint32_t lin = (uint32_t)(c[0] + g->sgs[0] * (c[1] + g->sgs[1] * c[2]));
+        const int q = it->q++;
+        const int32_t sx = 2 * it->c[0] + (q & 1), sy = 2 * it->c[1] + ((q >> 1) & 1), sz = 2 * it->c[2] + (q >> 2);
+        const uint32_t lin = (uint32_t)(sx + g->sgs[0] * (sy + g->sgs[1] * sz));
         if (it->start[lin] == ORC_EMPTY) {
             continue;
         }
+        sh[0] = it->sh[0];
+        sh[1] = it->sh[1];
+        sh[2] = it->sh[2];
         *b = it->start[lin];
         *e = it->end[lin];
         return 1;
