@@ -19,7 +19,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libasph_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-CU_SOURCES = ["step_kernels.cu", "refine_kernels.cu", "radix_sort.cu", "simulation.cu"]
+CU_SOURCES = ["step_kernels.cu", "neighbor_kernels.cu", "refine_kernels.cu", "radix_sort.cu", "simulation.cu"]
 CPP_SOURCES = ["boundary_domain.cpp"]
 HEADERS = ["asph_device.cuh", "asph_kernels.cuh", "asph_refine.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

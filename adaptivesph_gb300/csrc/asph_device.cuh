@@ -203,11 +203,14 @@ __device__ __forceinline__ float gap1(float p, float lo, float w, float m) {
 // hold a member within reach of p is skipped: reach = Rfix when Rfix > 0, else 2 * (max h of the cell). Culling
 // never skips a member that passes a support test, so sums over the visited members are unchanged.
 // body(begin, end, shx, shy, shz) gets the member range and the periodic image offsets.
-template <bool kCull, class Body>
+// With kLanes = 32 the reference cells of the box are dealt round-robin to the lanes of a warp by their ordinal
+// in the box (z, y, x order): lane l visits ordinals o with o % 32 == l (the order of the heavy-particle passes).
+template <bool kCull, int kLanes = 1, class Body>
 __device__ __forceinline__ void for_each_cell(const GridDev& g, const uint32_t* __restrict__ start,
                                               const uint32_t* __restrict__ end, const float* __restrict__ hmax,
                                               const float* __restrict__ hmax_ref, uint32_t ex0, uint32_t ex1,
-                                              float px, float py, float pz, float R, float Rfix, Body&& body) {
+                                              float px, float py, float pz, float R, float Rfix, Body&& body,
+                                              int lane = 0) {
     int32_t lo[3], hi[3];
     const float p[3] = {px, py, pz};
     bool ok = true;
@@ -216,16 +219,17 @@ __device__ __forceinline__ void for_each_cell(const GridDev& g, const uint32_t* 
     if (!ok) return;
     const bool periodic = g.periodic;
     const float m = g.cull_margin;
+    int32_t ord = -1;
     for (int32_t rz = lo[2]; rz <= hi[2]; ++rz) {
-        float shz;
-        const int32_t cz = wrap_cell(rz, g.gs[2], g.scale[2], periodic, shz);
-        if (cz < 0 || cz >= g.gs[2]) continue;
         for (int32_t ry = lo[1]; ry <= hi[1]; ++ry) {
-            float shy;
-            const int32_t cy = wrap_cell(ry, g.gs[1], g.scale[1], periodic, shy);
-            if (cy < 0 || cy >= g.gs[1]) continue;
             for (int32_t rx = lo[0]; rx <= hi[0]; ++rx) {
-                float shx;
+                ++ord;
+                if (kLanes > 1 && (ord & (kLanes - 1)) != lane) continue;
+                float shz, shy, shx;
+                const int32_t cz = wrap_cell(rz, g.gs[2], g.scale[2], periodic, shz);
+                if (cz < 0 || cz >= g.gs[2]) continue;
+                const int32_t cy = wrap_cell(ry, g.gs[1], g.scale[1], periodic, shy);
+                if (cy < 0 || cy >= g.gs[1]) continue;
                 const int32_t cx = wrap_cell(rx, g.gs[0], g.scale[0], periodic, shx);
                 if (cx < 0 || cx >= g.gs[0]) continue;
                 const uint32_t rk = (uint32_t)cx + (uint32_t)g.gs[0] * ((uint32_t)cy + (uint32_t)g.gs[1] * (uint32_t)cz);

@@ -20,14 +20,15 @@ struct StepArgs {
     uint32_t* err;
 };
 
-// Per-particle neighbour lists of the current step: entry k of particle i at idx[k * stride + i] (one column per
-// particle, so a warp reading entry k of 32 consecutive particles reads 128 contiguous bytes). The density pass
-// fills them in the canonical candidate order; cnt[i] > maxn marks an overflowed list, for which the later passes
-// scan the candidate cells again.
+// Per-particle neighbour lists of the current step: row i holds the accepted neighbours of particle i in the
+// canonical candidate order, idx[i * maxn + k]. cnt[i] > maxn marks an overflowed row (the force pass scans the
+// cells again); cnt[i] == kHeavyMark marks a heavy particle, queued in heavy[0, *heavy_n) for the warp kernels.
+constexpr uint32_t kHeavyMark = 0xffffffffu;
 struct NbrDev {
     uint32_t* idx;
     uint32_t* cnt;
-    uint32_t stride;
+    uint32_t* heavy;
+    uint32_t* heavy_n;
     uint32_t maxn;
 };
 
@@ -59,9 +60,11 @@ __global__ void k_boundary_reorder(GridDev g, const float4* pos_in, const float*
                                    const uint32_t* keys_sorted, const uint32_t* vals_sorted, uint32_t n,
                                    float4* pos_out, float* fric_out, uint32_t* start, uint32_t* end,
                                    uint8_t* refflag);
-__global__ void k_density(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl);
-cudaError_t launch_forces(bool morris, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c, BoundaryDev b,
-                          NbrDev nl);
+// density pass (ordinary particles, then the heavy ones) and force pass (neighbour_kernels.cu)
+cudaError_t launch_density(uint32_t blocks, uint32_t heavy_blocks, cudaStream_t stream, StepArgs a, CellsDev c,
+                           BoundaryDev b, NbrDev nl);
+cudaError_t launch_forces(bool morris, uint32_t blocks, uint32_t heavy_blocks, cudaStream_t stream, StepArgs a,
+                          CellsDev c, BoundaryDev b, NbrDev nl);
 __global__ void k_neighbor_counts(StepArgs a, CellsDev c, uint32_t* counts, unsigned long long* total);
 __global__ void k_export(StepArgs a, float pending_half, int has_pending, float4* pos_out, float4* vel_out,
                          float* rho_out, float* rad_out, uint32_t* id_out);

@@ -1,0 +1,504 @@
+// neighbor_kernels.cu — the neighbour passes of a step: density (+ neighbour lists) and forces.
+//
+// computeDensities / computeBoundaryDensityContribution (cuda/src/algorithm/Algorithm.cu:17-54,
+// cuda/src/algorithm/BoundaryAlgorithm.cu:15-51) and the acceleration kernels (Algorithm.cu:56-232,
+// BoundaryAlgorithm.cu:53-162) of SphSimulation::update (cuda/src/simulation/SphSimulation.cu:101-120).
+//
+// Ordinary particles: one thread per particle. The density pass scans the candidate cells in the canonical order,
+// sums the density as it goes and records the accepted neighbours (self included) in the particle's row of the
+// neighbour list; rows are staged in shared memory and flushed 16 entries (64 bytes) at a time, so list writes are
+// whole-segment stores. The force pass walks the row (16-byte loads) instead of the cells.
+// Heavy particles (query box of more than 27 reference cells, i.e. smoothing lengths grown by merging): one warp
+// per particle, the box's reference cells dealt round-robin to the lanes, partial sums combined by a fixed
+// butterfly; they are queued by the density pass and handled by separate warp kernels, so a few large boxes do not
+// stall whole blocks.
+#include "asph_device.cuh"
+#include "asph_kernels.cuh"
+
+namespace asph {
+
+namespace {
+
+constexpr uint32_t kIdxBits = 27;
+constexpr uint32_t kIdxMask = (1u << kIdxBits) - 1u;
+constexpr int kStage = 16;         // list entries staged per thread before a flush
+constexpr int kStageStride = 17;   // padded row (no bank conflicts between threads)
+constexpr int kHeavyCells = 27;    // more reference cells than this in the query box: heavy particle
+
+// Periodic image of a listed neighbour: the index keeps 27 bits, the cell's image offset (-1, 0, +1 per axis)
+// is packed into the top 5 bits.
+__device__ __forceinline__ uint32_t shift_code(float shx, float shy, float shz) {
+    const int cx = shx < 0.0f ? 0 : (shx > 0.0f ? 2 : 1);
+    const int cy = shy < 0.0f ? 0 : (shy > 0.0f ? 2 : 1);
+    const int cz = shz < 0.0f ? 0 : (shz > 0.0f ? 2 : 1);
+    return (uint32_t)(cx + 3 * cy + 9 * cz);
+}
+
+__device__ __forceinline__ void decode_entry(const GridDev& g, uint32_t e, uint32_t& j, float& shx, float& shy,
+                                             float& shz) {
+    if (!g.periodic) {
+        j = e;
+        shx = shy = shz = 0.0f;
+        return;
+    }
+    j = e & kIdxMask;
+    const uint32_t code = e >> kIdxBits;
+    const int cx = (int)(code % 3u), cy = (int)((code / 3u) % 3u), cz = (int)(code / 9u);
+    shx = cx == 0 ? -g.scale[0] : (cx == 2 ? g.scale[0] : 0.0f);
+    shy = cy == 0 ? -g.scale[1] : (cy == 2 ? g.scale[1] : 0.0f);
+    shz = cz == 0 ? -g.scale[2] : (cz == 2 ? g.scale[2] : 0.0f);
+}
+
+// Number of reference cells in the query box [x - R, x + R].
+__device__ __forceinline__ int box_cells(const GridDev& g, float4 p, float R) {
+    int32_t lo, hi;
+    int n = 1;
+    const float pp[3] = {p.x, p.y, p.z};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        if (!box_axis(g, a, pp[a], R, lo, hi)) return 0;
+        n *= (hi - lo + 1);
+    }
+    return n;
+}
+
+__device__ __forceinline__ float warp_sum_butterfly(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = v + __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// True when any reference cell of the query box of p holds boundary particles.
+__device__ __forceinline__ bool boundary_near(const GridDev& g, const BoundaryDev& b, float px, float py, float pz,
+                                              float R) {
+    if (b.n == 0) return false;
+    int32_t lo[3], hi[3];
+    const float p[3] = {px, py, pz};
+    bool ok = true;
+#pragma unroll
+    for (int a = 0; a < 3; a++) ok &= box_axis(g, a, p[a], R, lo[a], hi[a]);
+    if (!ok) return false;
+    for (int32_t z = lo[2]; z <= hi[2]; z++)
+        for (int32_t y = lo[1]; y <= hi[1]; y++)
+            for (int32_t x = lo[0]; x <= hi[0]; x++) {
+                int32_t cx = x, cy = y, cz = z;
+                if (g.periodic) {
+                    cx = (cx % g.gs[0] + g.gs[0]) % g.gs[0];
+                    cy = (cy % g.gs[1] + g.gs[1]) % g.gs[1];
+                    cz = (cz % g.gs[2] + g.gs[2]) % g.gs[2];
+                }
+                if (__ldg(b.refflag + cx + g.gs[0] * (cy + g.gs[1] * cz))) return true;
+            }
+    return false;
+}
+
+// Fluid density term of neighbour j (Algorithm.cu:29-51); false when j fails r^2 <= (2 h_j)^2.
+__device__ __forceinline__ bool density_term(const StepArgs& a, float4 pi, uint32_t j, float shx, float shy,
+                                             float shz, float& rho) {
+    const float4 pj = __ldg(a.ph + j);
+    const bool periodic = a.grid.periodic;
+    const float xj = periodic ? pj.x + shx : pj.x;
+    const float yj = periodic ? pj.y + shy : pj.y;
+    const float zj = periodic ? pj.z + shz : pj.z;
+    const float dx = xj - pi.x, dy = yj - pi.y, dz = zj - pi.z;
+    const float r2 = dist2(dx, dy, dz);
+    const float twoh = pj.w + pj.w;
+    if (r2 > twoh * twoh) return false;
+    const float4 kj = __ldg(a.kc + j);
+    const float w = kernel_w(sqrtf(r2), kj.x, kj.y);
+    rho = fmaf(kj.w, w, rho);
+    return true;
+}
+
+// Boundary density of particle i over the cells of lane `lane` (BoundaryAlgorithm.cu:15-51).
+template <int kLanes>
+__device__ __forceinline__ float boundary_density(const StepArgs& a, const BoundaryDev& b, uint32_t i, float4 pi,
+                                                  int lane) {
+    const float R = pi.w + pi.w;
+    const float4 ki = a.kc[i];
+    const float cut = R * R;
+    const bool periodic = a.grid.periodic;
+    float rb = 0.0f;
+    for_each_cell<false, kLanes>(
+        a.grid, b.start, b.end, nullptr, nullptr, b.ex0, b.ex1, pi.x, pi.y, pi.z, R, 0.0f,
+        [&](uint32_t kb, uint32_t ke, float shx, float shy, float shz) {
+            for (uint32_t k = kb; k < ke; ++k) {
+                const float4 pb = __ldg(b.pos + k);
+                const float xb = periodic ? pb.x + shx : pb.x;
+                const float yb = periodic ? pb.y + shy : pb.y;
+                const float zb = periodic ? pb.z + shz : pb.z;
+                const float dx = xb - pi.x, dy = yb - pi.y, dz = zb - pi.z;
+                const float r2 = dist2(dx, dy, dz);
+                if (r2 > cut) continue;
+                const float w = kernel_w(sqrtf(r2), ki.x, ki.y);
+                rb = fmaf(pb.w, w, rb);
+            }
+        },
+        lane);
+    return rb;
+}
+
+// Accumulators of the force pass: pressure, viscosity, cohesion; boundary pressure, boundary friction.
+struct ForceAcc {
+    float ap[3], av[3], as[3], bp[3], bf[3];
+};
+
+struct ForceCtx {
+    float4 pi, vi;
+    float rhoi, pti, Ki, ei, hi;
+    bool visc_on, sigma_on;
+};
+
+__device__ __forceinline__ ForceCtx force_ctx(const StepArgs& a, uint32_t i) {
+    ForceCtx c;
+    c.pi = a.ph[i];
+    c.vi = a.vm[i];
+    const float2 rpi = a.rp[i];
+    c.hi = c.pi.w;
+    c.rhoi = rpi.x;
+    c.pti = rpi.y;
+    c.Ki = ((2.0f * a.phys.alpha) * c.hi) * a.phys.c0;
+    c.ei = (0.01f * c.hi) * c.hi;
+    c.visc_on = a.phys.visc_on;
+    c.sigma_on = a.phys.sigma_on;
+    return c;
+}
+
+// Pressure, viscosity and cohesion terms of fluid neighbour j (Algorithm.cu:56-221).
+template <bool kMorris>
+__device__ __forceinline__ void force_term(const StepArgs& a, const ForceCtx& c, uint32_t j, float shx, float shy,
+                                           float shz, ForceAcc& f) {
+    const bool periodic = a.grid.periodic;
+    const float4 pj = __ldg(a.ph + j);
+    const float xj = periodic ? pj.x + shx : pj.x;
+    const float yj = periodic ? pj.y + shy : pj.y;
+    const float zj = periodic ? pj.z + shz : pj.z;
+    const float dx = c.pi.x - xj, dy = c.pi.y - yj, dz = c.pi.z - zj;
+    const float r2 = dist2(dx, dy, dz);
+    const float twoh = pj.w + pj.w;
+    if (r2 > twoh * twoh) return;
+    const float4 kj = __ldg(a.kc + j);
+    const float2 rpj = __ldg(a.rp + j);
+    const float r = sqrtf(r2);
+    float u[3];
+    if (r > 0.0f) {
+        const float ir = 1.0f / r;
+        u[0] = dx * ir;
+        u[1] = dy * ir;
+        u[2] = dz * ir;
+    } else {
+        u[0] = 0.0f;
+        u[1] = 1.0f;
+        u[2] = 0.0f;
+    }
+    const float dw = kernel_dw(r, kj.x, kj.z);
+    const float mj = kj.w;
+    {
+        const float sp = (mj * dw) * (c.pti + rpj.y);
+#pragma unroll
+        for (int q = 0; q < 3; q++) f.ap[q] = fmaf(-sp, u[q], f.ap[q]);
+    }
+    if (c.visc_on) {
+        const float4 vj = __ldg(a.vm + j);
+        const float vd[3] = {c.vi.x - vj.x, c.vi.y - vj.y, c.vi.z - vj.z};
+        const float rhoj = rpj.x;
+        if (!kMorris) {
+            const float comp = fmaf(vd[2], dz, fmaf(vd[1], dy, vd[0] * dx));
+            if (comp < 0.0f) {
+                const float nuij = c.Ki / (c.rhoi + rhoj);
+                const float piv = (-nuij * comp) / (r2 + c.ei);
+                const float sv = (mj * piv) * dw;
+#pragma unroll
+                for (int q = 0; q < 3; q++) f.av[q] = fmaf(-sv, u[q], f.av[q]);
+            }
+        } else {
+            const float coef = ((mj * a.phys.nu) * (c.rhoi + rhoj)) / (c.rhoi * rhoj);
+            const float sv = coef * ((r * dw) / (r2 + c.ei));
+#pragma unroll
+            for (int q = 0; q < 3; q++) f.av[q] = fmaf(sv, vd[q], f.av[q]);
+        }
+    }
+    if (c.sigma_on) {
+        const float ss = mj * kernel_w(r, kj.x, kj.y);
+#pragma unroll
+        for (int q = 0; q < 3; q++) f.as[q] = fmaf(ss, u[q], f.as[q]);
+    }
+}
+
+// Boundary pressure and friction (BoundaryAlgorithm.cu:53-162) over the cells of lane `lane`.
+template <int kLanes>
+__device__ __forceinline__ void boundary_forces(const StepArgs& a, const BoundaryDev& b, uint32_t i,
+                                                const ForceCtx& c, ForceAcc& f, int lane) {
+    const float R = c.hi + c.hi;
+    const float4 ki = a.kc[i];
+    const float cut = R * R;
+    const bool periodic = a.grid.periodic;
+    const float c0 = a.phys.c0;
+    for_each_cell<false, kLanes>(
+        a.grid, b.start, b.end, nullptr, nullptr, b.ex0, b.ex1, c.pi.x, c.pi.y, c.pi.z, R, 0.0f,
+        [&](uint32_t kb, uint32_t ke, float shx, float shy, float shz) {
+            for (uint32_t k = kb; k < ke; ++k) {
+                const float4 pb = __ldg(b.pos + k);
+                const float xb = periodic ? pb.x + shx : pb.x;
+                const float yb = periodic ? pb.y + shy : pb.y;
+                const float zb = periodic ? pb.z + shz : pb.z;
+                const float dx = c.pi.x - xb, dy = c.pi.y - yb, dz = c.pi.z - zb;
+                const float r2 = dist2(dx, dy, dz);
+                if (r2 > cut) continue;
+                const float r = sqrtf(r2);
+                float u[3];
+                if (r > 0.0f) {
+                    const float ir = 1.0f / r;
+                    u[0] = dx * ir;
+                    u[1] = dy * ir;
+                    u[2] = dz * ir;
+                } else {
+                    u[0] = 0.0f;
+                    u[1] = 1.0f;
+                    u[2] = 0.0f;
+                }
+                const float dw = kernel_dw(r, ki.x, ki.z);
+                const float psi = pb.w;
+                const float sp = (psi * c.pti) * dw;
+#pragma unroll
+                for (int q = 0; q < 3; q++) f.bp[q] = fmaf(-sp, u[q], f.bp[q]);
+                const float comp = fmaf(c.vi.z, dz, fmaf(c.vi.y, dy, c.vi.x * dx));
+                if (comp < 0.0f) {
+                    const float nub = ((__ldg(b.fric + k) * c.hi) * c0) / (2.0f * c.rhoi);
+                    const float pib = (-nub * comp) / (r2 + c.ei);
+                    const float sf = (psi * pib) * dw;
+#pragma unroll
+                    for (int q = 0; q < 3; q++) f.bf[q] = fmaf(-sf, u[q], f.bf[q]);
+                }
+            }
+        },
+        lane);
+}
+
+// a = g + pressure + viscosity + cohesion + boundary pressure + boundary friction, in the reference's kernel order.
+__device__ __forceinline__ void finish_force(const StepArgs& a, uint32_t i, const ForceCtx& c, const ForceAcc& f) {
+    float acc[3];
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        float v = a.phys.gravity[q];
+        v = v + f.ap[q];
+        if (c.visc_on) v = v + f.av[q];
+        if (c.sigma_on) v = v + (a.phys.sigma / c.vi.w) * f.as[q];
+        v = v + f.bp[q];
+        v = v + f.bf[q];
+        acc[q] = v;
+    }
+    if (!(isfinite(acc[0]) && isfinite(acc[1]) && isfinite(acc[2]))) atomicOr(a.err, 0x2u);
+    a.acc[i] = make_float4(acc[0], acc[1], acc[2], 0.0f);
+}
+
+template <bool kCull, class Body>
+__device__ __forceinline__ void fluid_candidates(const StepArgs& a, const CellsDev& c, float4 pi, Body&& body) {
+    const float R = pi.w + pi.w;
+    for_each_cell<kCull>(a.grid, c.start, c.end, c.hmax, c.hmax_ref, c.ex[0], c.ex[1], pi.x, pi.y, pi.z, R, 0.0f,
+                         body);
+}
+
+}  // namespace
+
+// Density pass, ordinary particles; heavy particles are queued for k_density_heavy.
+__global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
+    __shared__ uint32_t stage[256 * kStageStride];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const float4 pi = a.ph[i];
+    const float R = pi.w + pi.w;
+    if (box_cells(a.grid, pi, R) > kHeavyCells) {
+        nl.cnt[i] = kHeavyMark;
+        nl.heavy[atomicAdd(nl.heavy_n, 1u)] = i;
+        return;
+    }
+    const bool periodic = a.grid.periodic;
+    uint32_t* row = nl.idx + (size_t)i * nl.maxn;
+    uint32_t* st = stage + threadIdx.x * kStageStride;
+    const uint32_t maxn = nl.maxn;
+    uint32_t cnt = 0, staged = 0;
+    float rho = 0.0f;
+    fluid_candidates<true>(a, c, pi, [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
+        const uint32_t code = periodic ? (shift_code(shx, shy, shz) << kIdxBits) : 0u;
+        for (uint32_t j = jb; j < je; ++j) {
+            if (!density_term(a, pi, j, shx, shy, shz, rho)) continue;
+            if (cnt < maxn) {
+                st[staged++] = j | code;
+                if (staged == kStage) {
+                    uint4* dst = reinterpret_cast<uint4*>(row + (cnt + 1 - kStage));
+#pragma unroll
+                    for (int q = 0; q < kStage / 4; q++)
+                        dst[q] = make_uint4(st[4 * q], st[4 * q + 1], st[4 * q + 2], st[4 * q + 3]);
+                    staged = 0;
+                }
+            }
+            cnt++;
+        }
+    });
+    // remaining staged entries (fewer than a full segment)
+    const uint32_t kept = cnt < maxn ? cnt : maxn;
+    for (uint32_t q = 0; q < staged; ++q) row[kept - staged + q] = st[q];
+    nl.cnt[i] = cnt;
+    float rb = 0.0f;
+    if (boundary_near(a.grid, b, pi.x, pi.y, pi.z, R)) rb = boundary_density<1>(a, b, i, pi, 0);
+    const float rh = rho + rb;
+    if (!isfinite(rh)) atomicOr(a.err, 0x2u);
+    a.rp[i] = make_float2(rh, pressure_term(rh, a.phys.rho0, a.phys.B));
+}
+
+// Density of the heavy particles: one warp per particle.
+__global__ void __launch_bounds__(256, 1) k_density_heavy(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t nh = *nl.heavy_n;
+    for (uint32_t w = warp; w < nh; w += nwarps) {
+        const uint32_t i = nl.heavy[w];
+        const float4 pi = a.ph[i];
+        const float R = pi.w + pi.w;
+        float rho = 0.0f;
+        for_each_cell<true, 32>(
+            a.grid, c.start, c.end, c.hmax, c.hmax_ref, c.ex[0], c.ex[1], pi.x, pi.y, pi.z, R, 0.0f,
+            [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
+                for (uint32_t j = jb; j < je; ++j) density_term(a, pi, j, shx, shy, shz, rho);
+            },
+            lane);
+        rho = warp_sum_butterfly(rho);
+        float rb = 0.0f;
+        if (boundary_near(a.grid, b, pi.x, pi.y, pi.z, R)) rb = warp_sum_butterfly(boundary_density<32>(a, b, i, pi, lane));
+        if (lane == 0) {
+            const float rh = rho + rb;
+            if (!isfinite(rh)) atomicOr(a.err, 0x2u);
+            a.rp[i] = make_float2(rh, pressure_term(rh, a.phys.rho0, a.phys.B));
+        }
+    }
+}
+
+// Force pass, ordinary particles: walks the particle's neighbour list (or, if it overflowed, the cells again).
+template <bool kMorris>
+__global__ void __launch_bounds__(256, 3) k_forces(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const uint32_t cnt = nl.cnt[i];
+    if (cnt == kHeavyMark) return;
+    const ForceCtx x = force_ctx(a, i);
+    ForceAcc f = {};
+    if (cnt <= nl.maxn) {
+        const uint4* row = reinterpret_cast<const uint4*>(nl.idx + (size_t)i * nl.maxn);
+        for (uint32_t k = 0; k < cnt; k += 4) {
+            const uint4 e4 = __ldg(row + (k >> 2));
+            const uint32_t e[4] = {e4.x, e4.y, e4.z, e4.w};
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                if (k + q >= cnt) break;
+                uint32_t j;
+                float shx, shy, shz;
+                decode_entry(a.grid, e[q], j, shx, shy, shz);
+                if (j == i) continue;
+                force_term<kMorris>(a, x, j, shx, shy, shz, f);
+            }
+        }
+    } else {
+        fluid_candidates<true>(a, c, x.pi, [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
+            for (uint32_t j = jb; j < je; ++j) {
+                if (j == i) continue;
+                force_term<kMorris>(a, x, j, shx, shy, shz, f);
+            }
+        });
+    }
+    if (boundary_near(a.grid, b, x.pi.x, x.pi.y, x.pi.z, x.hi + x.hi)) boundary_forces<1>(a, b, i, x, f, 0);
+    finish_force(a, i, x, f);
+}
+
+// Forces of the heavy particles: one warp per particle.
+template <bool kMorris>
+__global__ void __launch_bounds__(256, 1) k_forces_heavy(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t nh = *nl.heavy_n;
+    for (uint32_t w = warp; w < nh; w += nwarps) {
+        const uint32_t i = nl.heavy[w];
+        const ForceCtx x = force_ctx(a, i);
+        ForceAcc f = {};
+        for_each_cell<true, 32>(
+            a.grid, c.start, c.end, c.hmax, c.hmax_ref, c.ex[0], c.ex[1], x.pi.x, x.pi.y, x.pi.z, x.hi + x.hi, 0.0f,
+            [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
+                for (uint32_t j = jb; j < je; ++j) {
+                    if (j == i) continue;
+                    force_term<kMorris>(a, x, j, shx, shy, shz, f);
+                }
+            },
+            lane);
+        if (boundary_near(a.grid, b, x.pi.x, x.pi.y, x.pi.z, x.hi + x.hi)) boundary_forces<32>(a, b, i, x, f, lane);
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            f.ap[q] = warp_sum_butterfly(f.ap[q]);
+            f.av[q] = warp_sum_butterfly(f.av[q]);
+            f.as[q] = warp_sum_butterfly(f.as[q]);
+            f.bp[q] = warp_sum_butterfly(f.bp[q]);
+            f.bf[q] = warp_sum_butterfly(f.bf[q]);
+        }
+        if (lane == 0) finish_force(a, i, x, f);
+    }
+}
+
+cudaError_t launch_density(uint32_t blocks, uint32_t heavy_blocks, cudaStream_t stream, StepArgs a, CellsDev c,
+                           BoundaryDev b, NbrDev nl) {
+    cudaError_t e = cudaMemsetAsync(nl.heavy_n, 0, sizeof(uint32_t), stream);
+    if (e != cudaSuccess) return e;
+    k_density<<<blocks, 256, 0, stream>>>(a, c, b, nl);
+    k_density_heavy<<<heavy_blocks, 256, 0, stream>>>(a, c, b, nl);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_forces(bool morris, uint32_t blocks, uint32_t heavy_blocks, cudaStream_t stream, StepArgs a,
+                          CellsDev c, BoundaryDev b, NbrDev nl) {
+    if (morris) {
+        k_forces<true><<<blocks, 256, 0, stream>>>(a, c, b, nl);
+        k_forces_heavy<true><<<heavy_blocks, 256, 0, stream>>>(a, c, b, nl);
+    } else {
+        k_forces<false><<<blocks, 256, 0, stream>>>(a, c, b, nl);
+        k_forces_heavy<false><<<heavy_blocks, 256, 0, stream>>>(a, c, b, nl);
+    }
+    return cudaGetLastError();
+}
+
+// Per-particle neighbour counts (sumAllNeighbors, cuda/src/algorithm/Algorithm.cu:234-268).
+__global__ void __launch_bounds__(256) k_neighbor_counts(StepArgs a, CellsDev c, uint32_t* counts,
+                                                         unsigned long long* total) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t cnt = 0;
+    if (i < a.n) {
+        const float4 pi = a.ph[i];
+        const bool periodic = a.grid.periodic;
+        fluid_candidates<true>(a, c, pi, [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
+            for (uint32_t j = jb; j < je; ++j) {
+                if (j == i) continue;
+                const float4 pj = __ldg(a.ph + j);
+                const float xj = periodic ? pj.x + shx : pj.x;
+                const float yj = periodic ? pj.y + shy : pj.y;
+                const float zj = periodic ? pj.z + shz : pj.z;
+                const float dx = xj - pi.x, dy = yj - pi.y, dz = zj - pi.z;
+                const float r2 = dist2(dx, dy, dz);
+                const float twoh = pj.w + pj.w;
+                if (r2 <= twoh * twoh) cnt++;
+            }
+        });
+        if (counts) counts[i] = cnt;
+    }
+    __shared__ unsigned long long s[8];
+    unsigned long long v = cnt;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += s[w];
+        atomicAdd(total, t);
+    }
+}
+
+}  // namespace asph

@@ -54,6 +54,9 @@ static asph_status cuda_fail(cudaError_t e, const char* what) {
 
 static inline uint32_t blocks_for(uint32_t n, uint32_t t = 256) { return n == 0 ? 1u : (n + t - 1) / t; }
 
+// blocks of 8 warps for the heavy-particle kernels (one warp per heavy particle, grid-stride over the queue)
+static constexpr uint32_t kHeavyBlocks = 304;
+
 // ------------------------------------------------------------------------------------------------ memory
 struct asph_memory {
     void* ptr = nullptr;
@@ -137,7 +140,9 @@ struct asph_simulation {
     float4* kc = nullptr;
     uint32_t* nbr_idx = nullptr;  // [maxn * cap] neighbour lists, one column per particle
     uint32_t* nbr_cnt = nullptr;  // [cap]
-    uint32_t maxn = 128;
+    uint32_t* heavy_idx = nullptr;  // [cap] queue of heavy particles of the current step
+    uint32_t* heavy_n = nullptr;
+    uint32_t maxn = 256;
     uint32_t* keys = nullptr;
     uint32_t* vals = nullptr;
     void* sort_mem = nullptr;
@@ -229,7 +234,7 @@ struct asph_simulation {
 
     CellsDev cells() const { return CellsDev{cell_start, cell_end, cell_hmax, hmax_ref, ex}; }
 
-    NbrDev nbrs() const { return NbrDev{nbr_idx, nbr_cnt, cap, maxn}; }
+    NbrDev nbrs() const { return NbrDev{nbr_idx, nbr_cnt, heavy_idx, heavy_n, maxn}; }
 
     BoundaryDev boundary() const {
         return BoundaryDev{bpos, bfric, bstart, bend, brefflag, bex[0], bex[1], nb};
@@ -509,17 +514,17 @@ asph_status build_grid(asph_simulation* s, bool integrate, float dt, bool carry_
 asph_status run_density(asph_simulation* s) {
     StepArgs a = s->args(s->cur);
     int h = s->tic();
-    k_density<<<blocks_for(s->n), 256, 0, s->stream>>>(a, s->cells(), s->boundary(), s->nbrs());
-    CK_LAUNCH("k_density");
+    CK(launch_density(blocks_for(s->n), kHeavyBlocks, s->stream, a, s->cells(), s->boundary(), s->nbrs()));
     s->toc(h, ASPH_KERNEL_DENSITY);
-    s->launches++;
+    s->launches += 2;
     return ASPH_OK;
 }
 
 asph_status run_forces(asph_simulation* s) {
     StepArgs a = s->args(s->cur);
     int h = s->tic();
-    CK(launch_forces(s->phys.morris != 0, blocks_for(s->n), s->stream, a, s->cells(), s->boundary(), s->nbrs()));
+    CK(launch_forces(s->phys.morris != 0, blocks_for(s->n), kHeavyBlocks, s->stream, a, s->cells(), s->boundary(),
+                     s->nbrs()));
     s->toc(h, ASPH_KERNEL_FORCES);
     s->launches++;
     return ASPH_OK;
@@ -727,6 +732,8 @@ void destroy(asph_simulation* s) {
     dfree(s->kc);
     dfree(s->nbr_idx);
     dfree(s->nbr_cnt);
+    dfree(s->heavy_idx);
+    dfree(s->heavy_n);
     dfree(s->keys);
     dfree(s->vals);
     dfree(s->sort_mem);
@@ -963,6 +970,8 @@ asph_status asph_simulation_create(const asph_parameters* parameters, const floa
     TRY(dalloc(s->kc, C));
     TRY(dalloc(s->nbr_idx, (size_t)s->maxn * C));
     TRY(dalloc(s->nbr_cnt, C));
+    TRY(dalloc(s->heavy_idx, C));
+    TRY(dalloc(s->heavy_n, 1));
     const uint32_t sort_items = std::max(C, std::max(boundary_count, max_boundary_capacity));
     TRY(dalloc(s->keys, sort_items));
     TRY(dalloc(s->vals, sort_items));

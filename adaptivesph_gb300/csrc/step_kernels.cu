@@ -212,354 +212,6 @@ __global__ void __launch_bounds__(256) k_boundary_reorder(GridDev g, const float
     refflag[(sx >> 1) + (uint32_t)g.gs[0] * ((sy >> 1) + (uint32_t)g.gs[1] * (sz >> 1))] = 1;
 }
 
-// True when any reference cell of the query box of p holds boundary particles.
-__device__ __forceinline__ bool boundary_near(const GridDev& g, const BoundaryDev& b, float px, float py, float pz,
-                                              float R) {
-    if (b.n == 0) return false;
-    int32_t lo[3], hi[3];
-    const float p[3] = {px, py, pz};
-    bool ok = true;
-#pragma unroll
-    for (int a = 0; a < 3; a++) ok &= box_axis(g, a, p[a], R, lo[a], hi[a]);
-    if (!ok) return false;
-    for (int32_t z = lo[2] >> 1; z <= (hi[2] >> 1); z++)
-        for (int32_t y = lo[1] >> 1; y <= (hi[1] >> 1); y++)
-            for (int32_t x = lo[0] >> 1; x <= (hi[0] >> 1); x++) {
-                int32_t cx = x, cy = y, cz = z;
-                if (g.periodic) {
-                    cx = (cx % g.gs[0] + g.gs[0]) % g.gs[0];
-                    cy = (cy % g.gs[1] + g.gs[1]) % g.gs[1];
-                    cz = (cz % g.gs[2] + g.gs[2]) % g.gs[2];
-                }
-                if (__ldg(b.refflag + cx + g.gs[0] * (cy + g.gs[1] * cz))) return true;
-            }
-    return false;
-}
-
-// Periodic image of a listed neighbour: the index keeps 27 bits, the cell's image offset (-1, 0, +1 per axis)
-// is packed into the top 5 bits.
-constexpr uint32_t kIdxBits = 27;
-constexpr uint32_t kIdxMask = (1u << kIdxBits) - 1u;
-
-__device__ __forceinline__ uint32_t shift_code(const GridDev& g, float shx, float shy, float shz) {
-    const int cx = shx < 0.0f ? 0 : (shx > 0.0f ? 2 : 1);
-    const int cy = shy < 0.0f ? 0 : (shy > 0.0f ? 2 : 1);
-    const int cz = shz < 0.0f ? 0 : (shz > 0.0f ? 2 : 1);
-    return (uint32_t)(cx + 3 * cy + 9 * cz);
-}
-
-__device__ __forceinline__ void decode_entry(const GridDev& g, uint32_t e, uint32_t& j, float& shx, float& shy,
-                                             float& shz) {
-    if (!g.periodic) {
-        j = e;
-        shx = shy = shz = 0.0f;
-        return;
-    }
-    j = e & kIdxMask;
-    const uint32_t code = e >> kIdxBits;
-    const int cx = (int)(code % 3u), cy = (int)((code / 3u) % 3u), cz = (int)(code / 9u);
-    shx = cx == 0 ? -g.scale[0] : (cx == 2 ? g.scale[0] : 0.0f);
-    shy = cy == 0 ? -g.scale[1] : (cy == 2 ? g.scale[1] : 0.0f);
-    shz = cz == 0 ? -g.scale[2] : (cz == 2 ? g.scale[2] : 0.0f);
-}
-
-// Fluid density term of neighbour j (computeDensities, cuda/src/algorithm/Algorithm.cu:17-54); returns false when j
-// fails the support test r^2 <= (2 h_j)^2.
-__device__ __forceinline__ bool density_term(const StepArgs& a, float4 pi, uint32_t j, float shx, float shy,
-                                             float shz, float& rho) {
-    const float4 pj = __ldg(a.ph + j);
-    const bool periodic = a.grid.periodic;
-    const float xj = periodic ? pj.x + shx : pj.x;
-    const float yj = periodic ? pj.y + shy : pj.y;
-    const float zj = periodic ? pj.z + shz : pj.z;
-    const float dx = xj - pi.x, dy = yj - pi.y, dz = zj - pi.z;
-    const float r2 = dist2(dx, dy, dz);
-    const float twoh = pj.w + pj.w;
-    if (r2 > twoh * twoh) return false;
-    const float4 kj = __ldg(a.kc + j);
-    const float w = kernel_w(sqrtf(r2), kj.x, kj.y);
-    rho = fmaf(kj.w, w, rho);
-    return true;
-}
-
-// The candidate cells of the density/force passes: reference cells of [x - 2h_i, x + 2h_i].
-template <class Body>
-__device__ __forceinline__ void fluid_candidates(const StepArgs& a, const CellsDev& c, float4 pi, Body&& body) {
-    const float R = pi.w + pi.w;
-    for_each_cell<true>(a.grid, c.start, c.end, c.hmax, c.hmax_ref, c.ex[0], c.ex[1], pi.x, pi.y, pi.z, R, 0.0f, body);
-}
-
-// computeDensities (cuda/src/algorithm/Algorithm.cu:17-54) + computeBoundaryDensityContribution
-// (cuda/src/algorithm/BoundaryAlgorithm.cu:15-51), then p/rho^2 for the force pass. The scan also records the
-// accepted neighbours (self included) in the particle's list, in candidate order, for the force pass.
-__global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
-    const float4 pi = a.ph[i];
-    const bool periodic = a.grid.periodic;
-    uint32_t cnt = 0;
-    uint32_t* col = nl.idx + i;
-    const uint32_t stride = nl.stride, maxn = nl.maxn;
-    float rho = 0.0f;
-    fluid_candidates(a, c, pi, [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
-        const uint32_t code = periodic ? (shift_code(a.grid, shx, shy, shz) << kIdxBits) : 0u;
-        for (uint32_t j = jb; j < je; ++j) {
-            if (!density_term(a, pi, j, shx, shy, shz, rho)) continue;
-            if (cnt < maxn) col[(size_t)cnt * stride] = j | code;
-            cnt++;
-        }
-    });
-    nl.cnt[i] = cnt;
-    const float R = pi.w + pi.w;
-    float rb = 0.0f;
-    if (boundary_near(a.grid, b, pi.x, pi.y, pi.z, R)) {
-        const float4 ki = a.kc[i];
-        const float cut = R * R;
-        for_each_cell<false>(a.grid, b.start, b.end, nullptr, nullptr, b.ex0, b.ex1, pi.x, pi.y, pi.z, R, 0.0f,
-                             [&](uint32_t kb, uint32_t ke, float shx, float shy, float shz) {
-                                 for (uint32_t k = kb; k < ke; ++k) {
-                                     const float4 pb = __ldg(b.pos + k);
-                                     const float xb = periodic ? pb.x + shx : pb.x;
-                                     const float yb = periodic ? pb.y + shy : pb.y;
-                                     const float zb = periodic ? pb.z + shz : pb.z;
-                                     const float dx = xb - pi.x, dy = yb - pi.y, dz = zb - pi.z;
-                                     const float r2 = dist2(dx, dy, dz);
-                                     if (r2 > cut) continue;
-                                     const float w = kernel_w(sqrtf(r2), ki.x, ki.y);
-                                     rb = fmaf(pb.w, w, rb);
-                                 }
-                             });
-    }
-    const float rh = rho + rb;
-    if (!isfinite(rh)) atomicOr(a.err, 0x2u);
-    a.rp[i] = make_float2(rh, pressure_term(rh, a.phys.rho0, a.phys.B));
-}
-
-// Per-particle constants and accumulators of the force pass.
-struct ForceAcc {
-    float apx, apy, apz, avx, avy, avz, asx, asy, asz;
-};
-
-// Pressure, viscosity and cohesion terms of fluid neighbour j (cuda/src/algorithm/Algorithm.cu:56-221).
-template <bool kMorris>
-__device__ __forceinline__ void force_term(const StepArgs& a, float4 pi, float4 vi, float rhoi, float pti, float Ki,
-                                           float ei, bool visc_on, bool sigma_on, uint32_t j, float shx, float shy,
-                                           float shz, ForceAcc& f) {
-    const bool periodic = a.grid.periodic;
-    const float4 pj = __ldg(a.ph + j);
-    const float xj = periodic ? pj.x + shx : pj.x;
-    const float yj = periodic ? pj.y + shy : pj.y;
-    const float zj = periodic ? pj.z + shz : pj.z;
-    const float dx = pi.x - xj, dy = pi.y - yj, dz = pi.z - zj;
-    const float r2 = dist2(dx, dy, dz);
-    const float twoh = pj.w + pj.w;
-    if (r2 > twoh * twoh) return;
-    const float4 kj = __ldg(a.kc + j);
-    const float2 rpj = __ldg(a.rp + j);
-    const float r = sqrtf(r2);
-    float ux, uy, uz;
-    if (r > 0.0f) {
-        const float ir = 1.0f / r;
-        ux = dx * ir;
-        uy = dy * ir;
-        uz = dz * ir;
-    } else {
-        ux = 0.0f;
-        uy = 1.0f;
-        uz = 0.0f;
-    }
-    const float dw = kernel_dw(r, kj.x, kj.z);
-    const float mj = kj.w;
-    {
-        const float sp = (mj * dw) * (pti + rpj.y);
-        f.apx = fmaf(-sp, ux, f.apx);
-        f.apy = fmaf(-sp, uy, f.apy);
-        f.apz = fmaf(-sp, uz, f.apz);
-    }
-    if (visc_on) {
-        const float4 vj = __ldg(a.vm + j);
-        const float vdx = vi.x - vj.x, vdy = vi.y - vj.y, vdz = vi.z - vj.z;
-        const float rhoj = rpj.x;
-        if (!kMorris) {
-            const float comp = fmaf(vdz, dz, fmaf(vdy, dy, vdx * dx));
-            if (comp < 0.0f) {
-                const float nuij = Ki / (rhoi + rhoj);
-                const float piv = (-nuij * comp) / (r2 + ei);
-                const float sv = (mj * piv) * dw;
-                f.avx = fmaf(-sv, ux, f.avx);
-                f.avy = fmaf(-sv, uy, f.avy);
-                f.avz = fmaf(-sv, uz, f.avz);
-            }
-        } else {
-            const float coef = ((mj * a.phys.nu) * (rhoi + rhoj)) / (rhoi * rhoj);
-            const float sv = coef * ((r * dw) / (r2 + ei));
-            f.avx = fmaf(sv, vdx, f.avx);
-            f.avy = fmaf(sv, vdy, f.avy);
-            f.avz = fmaf(sv, vdz, f.avz);
-        }
-    }
-    if (sigma_on) {
-        const float ss = mj * kernel_w(r, kj.x, kj.y);
-        f.asx = fmaf(ss, ux, f.asx);
-        f.asy = fmaf(ss, uy, f.asy);
-        f.asz = fmaf(ss, uz, f.asz);
-    }
-}
-
-// computeExternalAccelerations, computePressureAccelerations, computeViscosityAccelerations,
-// computeSurfaceTensionAccelerations (cuda/src/algorithm/Algorithm.cu:56-232) and
-// computeBoundaryPressureAcceleration / computeBoundaryFrictionAcceleration
-// (cuda/src/algorithm/BoundaryAlgorithm.cu:53-162) in one pass over the neighbour list; each term keeps its own
-// accumulator and they are added to gravity in the reference's kernel order.
-template <bool kMorris>
-__global__ void __launch_bounds__(256, 3) k_forces(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
-    const float4 pi = a.ph[i];
-    const float4 vi = a.vm[i];
-    const float2 rpi = a.rp[i];
-    const float hi = pi.w, mi = vi.w, rhoi = rpi.x, pti = rpi.y;
-    const float c0 = a.phys.c0;
-    const float Ki = ((2.0f * a.phys.alpha) * hi) * c0;
-    const float ei = (0.01f * hi) * hi;
-    const float R = hi + hi;
-    const bool visc_on = a.phys.visc_on, sigma_on = a.phys.sigma_on, periodic = a.grid.periodic;
-    ForceAcc f = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    const uint32_t cnt = nl.cnt[i];
-    if (cnt <= nl.maxn) {
-        const uint32_t* col = nl.idx + i;
-        for (uint32_t k = 0; k < cnt; ++k) {
-            uint32_t j;
-            float shx, shy, shz;
-            decode_entry(a.grid, __ldg(col + (size_t)k * nl.stride), j, shx, shy, shz);
-            if (j == i) continue;
-            force_term<kMorris>(a, pi, vi, rhoi, pti, Ki, ei, visc_on, sigma_on, j, shx, shy, shz, f);
-        }
-    } else {
-        fluid_candidates(a, c, pi, [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
-            for (uint32_t j = jb; j < je; ++j) {
-                if (j == i) continue;
-                force_term<kMorris>(a, pi, vi, rhoi, pti, Ki, ei, visc_on, sigma_on, j, shx, shy, shz, f);
-            }
-        });
-    }
-    float bpx = 0.f, bpy = 0.f, bpz = 0.f, bfx = 0.f, bfy = 0.f, bfz = 0.f;
-    if (boundary_near(a.grid, b, pi.x, pi.y, pi.z, R)) {
-        const float4 ki = a.kc[i];
-        const float cut = R * R;
-        for_each_cell<false>(a.grid, b.start, b.end, nullptr, nullptr, b.ex0, b.ex1, pi.x, pi.y, pi.z, R, 0.0f,
-                             [&](uint32_t kb, uint32_t ke, float shx, float shy, float shz) {
-                                 for (uint32_t k = kb; k < ke; ++k) {
-                                     const float4 pb = __ldg(b.pos + k);
-                                     const float xb = periodic ? pb.x + shx : pb.x;
-                                     const float yb = periodic ? pb.y + shy : pb.y;
-                                     const float zb = periodic ? pb.z + shz : pb.z;
-                                     const float dx = pi.x - xb, dy = pi.y - yb, dz = pi.z - zb;
-                                     const float r2 = dist2(dx, dy, dz);
-                                     if (r2 > cut) continue;
-                                     const float r = sqrtf(r2);
-                                     float ux, uy, uz;
-                                     if (r > 0.0f) {
-                                         const float ir = 1.0f / r;
-                                         ux = dx * ir;
-                                         uy = dy * ir;
-                                         uz = dz * ir;
-                                     } else {
-                                         ux = 0.0f;
-                                         uy = 1.0f;
-                                         uz = 0.0f;
-                                     }
-                                     const float dw = kernel_dw(r, ki.x, ki.z);
-                                     const float psi = pb.w;
-                                     const float sp = (psi * pti) * dw;
-                                     bpx = fmaf(-sp, ux, bpx);
-                                     bpy = fmaf(-sp, uy, bpy);
-                                     bpz = fmaf(-sp, uz, bpz);
-                                     const float comp = fmaf(vi.z, dz, fmaf(vi.y, dy, vi.x * dx));
-                                     if (comp < 0.0f) {
-                                         const float nub = ((__ldg(b.fric + k) * hi) * c0) / (2.0f * rhoi);
-                                         const float pib = (-nub * comp) / (r2 + ei);
-                                         const float sf = (psi * pib) * dw;
-                                         bfx = fmaf(-sf, ux, bfx);
-                                         bfy = fmaf(-sf, uy, bfy);
-                                         bfz = fmaf(-sf, uz, bfz);
-                                     }
-                                 }
-                             });
-    }
-    float ax = a.phys.gravity[0], ay = a.phys.gravity[1], az = a.phys.gravity[2];
-    ax = ax + f.apx;
-    ay = ay + f.apy;
-    az = az + f.apz;
-    if (visc_on) {
-        ax = ax + f.avx;
-        ay = ay + f.avy;
-        az = az + f.avz;
-    }
-    if (sigma_on) {
-        const float fs = a.phys.sigma / mi;
-        ax = ax + fs * f.asx;
-        ay = ay + fs * f.asy;
-        az = az + fs * f.asz;
-    }
-    ax = ax + bpx;
-    ay = ay + bpy;
-    az = az + bpz;
-    ax = ax + bfx;
-    ay = ay + bfy;
-    az = az + bfz;
-    if (!(isfinite(ax) && isfinite(ay) && isfinite(az))) atomicOr(a.err, 0x2u);
-    a.acc[i] = make_float4(ax, ay, az, 0.0f);
-}
-
-cudaError_t launch_forces(bool morris, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c, BoundaryDev b,
-                          NbrDev nl) {
-    if (morris)
-        k_forces<true><<<blocks, 256, 0, stream>>>(a, c, b, nl);
-    else
-        k_forces<false><<<blocks, 256, 0, stream>>>(a, c, b, nl);
-    return cudaGetLastError();
-}
-
-// Per-particle neighbour counts (sumAllNeighbors, cuda/src/algorithm/Algorithm.cu:234-268).
-__global__ void __launch_bounds__(256) k_neighbor_counts(StepArgs a, CellsDev c, uint32_t* counts,
-                                                         unsigned long long* total) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t cnt = 0;
-    if (i < a.n) {
-        const float4 pi = a.ph[i];
-        const float R = pi.w + pi.w;
-        const bool periodic = a.grid.periodic;
-        for_each_cell<true>(a.grid, c.start, c.end, c.hmax, c.hmax_ref, c.ex[0], c.ex[1], pi.x, pi.y, pi.z, R, 0.0f,
-                            [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
-                                for (uint32_t j = jb; j < je; ++j) {
-                                    if (j == i) continue;
-                                    const float4 pj = __ldg(a.ph + j);
-                                    const float xj = periodic ? pj.x + shx : pj.x;
-                                    const float yj = periodic ? pj.y + shy : pj.y;
-                                    const float zj = periodic ? pj.z + shz : pj.z;
-                                    const float dx = xj - pi.x, dy = yj - pi.y, dz = zj - pi.z;
-                                    const float r2 = dist2(dx, dy, dz);
-                                    const float twoh = pj.w + pj.w;
-                                    if (r2 <= twoh * twoh) cnt++;
-                                }
-                            });
-        if (counts) counts[i] = cnt;
-    }
-    // block sum then one atomic
-    __shared__ unsigned long long s[8];
-    unsigned long long v = cnt;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = v;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned long long t = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += s[w];
-        atomicAdd(total, t);
-    }
-}
-
 // Export: positions (w = 0), velocities with the pending closing half-kick, densities, radii.
 __global__ void __launch_bounds__(256) k_export(StepArgs a, float pending_half, int has_pending, float4* pos_out,
                                                 float4* vel_out, float* rho_out, float* rad_out, uint32_t* id_out) {

@@ -148,6 +148,8 @@ typedef struct orc_iter {
     float sh[3];                /* its periodic image offset */
     int q;                      /* next sub-cell of the current reference cell, 0..8 */
     int empty;
+    int32_t ord;                /* ordinal of the current reference cell in the box (z, y, x order) */
+    int lanes, lane;            /* visit only ordinals with ord % lanes == lane */
 } orc_iter;
 
 static float clampf(float x, float lo, float hi)
@@ -196,6 +198,30 @@ static void it_init(orc_iter* it, const orc_grid* g, const uint32_t* start, cons
     it->r[1] = it->lo[1];
     it->r[2] = it->lo[2];
     it->q = 8;
+    it->ord = -1;
+    it->lanes = 1;
+    it->lane = 0;
+}
+
+/* the same box, dealing its reference cells round-robin to `lanes` lanes by ordinal; this is lane `lane` */
+static void it_init_lane(orc_iter* it, const orc_grid* g, const uint32_t* start, const uint32_t* end,
+                         const uint32_t ex[2], const float* p, float R, int lanes, int lane)
+{
+    it_init(it, g, start, end, ex, p, R);
+    it->lanes = lanes;
+    it->lane = lane;
+}
+
+/* number of reference cells in the box of p with radius R (the heavy-particle criterion) */
+static int64_t box_cells(const orc_grid* g, const float* p, float R)
+{
+    orc_iter it;
+    static const uint32_t none[2] = {ORC_NONE, ORC_NONE};
+    it_init(&it, g, NULL, NULL, none, p, R);
+    if (it.empty) {
+        return 0;
+    }
+    return (int64_t)(it.hi[0] - it.lo[0] + 1) * (it.hi[1] - it.lo[1] + 1) * (it.hi[2] - it.lo[2] + 1);
 }
 
 /* moves to the next reference cell of the box that is neither excluded nor outside a periodic grid */
@@ -212,6 +238,10 @@ static int it_next_ref(orc_iter* it)
                     return 0;
                 }
             }
+        }
+        it->ord++;
+        if (it->lanes > 1 && it->ord % it->lanes != it->lane) {
+            continue;
         }
         int ok = 1;
         for (int a = 0; a < 3; a++) {
@@ -453,6 +483,8 @@ float orc_cbrtf(float xf)
 
 /* ------------------------------------------------------------------ FP32 / FP64 bodies */
 static const float ORC_PI_F = 3.141592653589793f;
+#define ORC_LANES 32       /* lanes of the warp that sums a heavy particle */
+#define ORC_HEAVY_CELLS 27 /* query boxes of more reference cells than this are heavy */
 
 #define REAL float
 #define F(name) name##_f32

@@ -17,6 +17,12 @@
  * B*d*(5+d*(10+d*(10+d*(5+d)))) with d = (rho-rho0)/rho0, algebraically (rho/rho0)^5-1 without
  * the cancellation of powf(...)-1; directions are offset * (1/r); per-pair force terms are a scalar
  * s times the direction, accumulated with fma.
+ *
+ * Summation order: neighbours are summed in the canonical visiting order of the candidate cells. A particle
+ * whose query box spans more than ORC_HEAVY_CELLS reference cells ("heavy", after merges made h large) is summed
+ * as the GPU sums it with one warp: the box's reference cells are dealt round-robin to 32 lanes by ordinal,
+ * each lane sums its cells in order, and the 32 partial sums are combined by the butterfly
+ * s_l <- s_l + s_(l xor o) for o = 16, 8, 4, 2, 1.
  */
 
 /* W(r, h) with precomputed 1/h and coef/h^3 */
@@ -72,62 +78,262 @@ static inline REAL F(dist2)(REAL dx, REAL dy, REAL dz)
     return FMA(dz, dz, FMA(dy, dy, dx * dx));
 }
 
+/* the warp's combination of 32 partial sums */
+static REAL F(butterfly)(REAL* s)
+{
+    REAL t[ORC_LANES];
+    for (int o = ORC_LANES / 2; o >= 1; o >>= 1) {
+        for (int l = 0; l < ORC_LANES; l++) {
+            t[l] = s[l] + s[l ^ o];
+        }
+        memcpy(s, t, sizeof(t));
+    }
+    return s[0];
+}
+
+/* fluid part of the density of particle i over the cells of lane `lane` of `lanes` */
+static REAL F(density_fluid)(const orc_grid* g, const orc_state* s, const orc_cells* c, int64_t i, int lanes,
+                             int lane)
+{
+    const float* pi = s->pos + 4 * i;
+    const REAL xi = pi[0], yi = pi[1], zi = pi[2];
+    const float R = s->h[i] + s->h[i];
+    REAL rho = 0;
+    orc_iter it;
+    uint32_t jb, je;
+    float sh[3];
+    it_init_lane(&it, g, c->start, c->end, c->ex, pi, R, lanes, lane);
+    while (it_next(&it, &jb, &je, sh)) {
+        for (uint32_t j = jb; j < je; j++) {
+            const float* pj = s->pos + 4 * (size_t)j;
+            const REAL dx = NBR(pj, 0) - xi;
+            const REAL dy = NBR(pj, 1) - yi;
+            const REAL dz = NBR(pj, 2) - zi;
+            const REAL r2 = F(dist2)(dx, dy, dz);
+            const REAL hj = s->h[j];
+            const REAL twoh = hj + hj;
+            if (r2 > twoh * twoh) {
+                continue;
+            }
+            REAL invh, wc, dwc;
+            F(kernel_consts)(hj, &invh, &wc, &dwc);
+            const REAL w = F(kernel_w)(SQRT(r2), invh, wc);
+            rho = FMA((REAL)s->m[j], w, rho);
+        }
+    }
+    return rho;
+}
+
+static REAL F(density_boundary)(const orc_grid* g, const orc_state* s, const orc_boundary* b, int64_t i,
+                                int lanes, int lane)
+{
+    if (b == NULL || b->n == 0) {
+        return 0;
+    }
+    const float* pi = s->pos + 4 * i;
+    const REAL xi = pi[0], yi = pi[1], zi = pi[2];
+    const REAL hi = s->h[i];
+    const float R = s->h[i] + s->h[i];
+    REAL invh, wc, dwc;
+    F(kernel_consts)(hi, &invh, &wc, &dwc);
+    const REAL twoh = hi + hi;
+    const REAL cut = twoh * twoh;
+    REAL rb = 0;
+    orc_iter it;
+    uint32_t jb, je;
+    float sh[3];
+    it_init_lane(&it, g, b->start, b->end, b->ex, pi, R, lanes, lane);
+    while (it_next(&it, &jb, &je, sh)) {
+        for (uint32_t k = jb; k < je; k++) {
+            const float* pb = b->pos + 4 * (size_t)k;
+            const REAL dx = NBR(pb, 0) - xi;
+            const REAL dy = NBR(pb, 1) - yi;
+            const REAL dz = NBR(pb, 2) - zi;
+            const REAL r2 = F(dist2)(dx, dy, dz);
+            if (r2 > cut) {
+                continue;
+            }
+            const REAL w = F(kernel_w)(SQRT(r2), invh, wc);
+            rb = FMA((REAL)b->psi[k], w, rb);
+        }
+    }
+    return rb;
+}
+
 void F(orc_density_impl)(const orc_grid* g, const orc_params* P, const orc_state* s, const orc_cells* c,
                          const orc_boundary* b, REAL* rho_out)
 {
+    (void)P;
     const int64_t n = s->n;
 #pragma omp parallel for schedule(dynamic, 256)
     for (int64_t i = 0; i < n; i++) {
-        const float* pi = s->pos + 4 * i;
-        const REAL xi = pi[0], yi = pi[1], zi = pi[2];
-        const REAL hi = s->h[i];
         const float R = s->h[i] + s->h[i];
-        REAL rho = 0;
-        orc_iter it;
-        uint32_t jb, je;
-        float sh[3];
-        it_init(&it, g, c->start, c->end, c->ex, pi, R);
-        while (it_next(&it, &jb, &je, sh)) {
-            for (uint32_t j = jb; j < je; j++) {
-                const float* pj = s->pos + 4 * (size_t)j;
-                const REAL dx = NBR(pj, 0) - xi;
-                const REAL dy = NBR(pj, 1) - yi;
-                const REAL dz = NBR(pj, 2) - zi;
-                const REAL r2 = F(dist2)(dx, dy, dz);
-                const REAL hj = s->h[j];
-                const REAL twoh = hj + hj;
-                if (r2 > twoh * twoh) {
-                    continue;
-                }
-                REAL invh, wc, dwc;
-                F(kernel_consts)(hj, &invh, &wc, &dwc);
-                const REAL w = F(kernel_w)(SQRT(r2), invh, wc);
-                rho = FMA((REAL)s->m[j], w, rho);
+        REAL rho, rb;
+        if (box_cells(g, s->pos + 4 * i, R) > ORC_HEAVY_CELLS) {
+            REAL pf[ORC_LANES], pb[ORC_LANES];
+            for (int l = 0; l < ORC_LANES; l++) {
+                pf[l] = F(density_fluid)(g, s, c, i, ORC_LANES, l);
+                pb[l] = F(density_boundary)(g, s, b, i, ORC_LANES, l);
             }
-        }
-        REAL rb = 0;
-        if (b != NULL && b->n > 0) {
-            REAL invh, wc, dwc;
-            F(kernel_consts)(hi, &invh, &wc, &dwc);
-            const REAL twoh = hi + hi;
-            const REAL cut = twoh * twoh;
-            it_init(&it, g, b->start, b->end, b->ex, pi, R);
-            while (it_next(&it, &jb, &je, sh)) {
-                for (uint32_t k = jb; k < je; k++) {
-                    const float* pb = b->pos + 4 * (size_t)k;
-                    const REAL dx = NBR(pb, 0) - xi;
-                    const REAL dy = NBR(pb, 1) - yi;
-                    const REAL dz = NBR(pb, 2) - zi;
-                    const REAL r2 = F(dist2)(dx, dy, dz);
-                    if (r2 > cut) {
-                        continue;
-                    }
-                    const REAL w = F(kernel_w)(SQRT(r2), invh, wc);
-                    rb = FMA((REAL)b->psi[k], w, rb);
-                }
-            }
+            rho = F(butterfly)(pf);
+            rb = F(butterfly)(pb);
+        } else {
+            rho = F(density_fluid)(g, s, c, i, 1, 0);
+            rb = F(density_boundary)(g, s, b, i, 1, 0);
         }
         rho_out[i] = rho + rb;
+    }
+}
+
+/* accumulators of the force pass: pressure, viscosity, cohesion; boundary pressure, boundary friction */
+typedef struct F(facc) {
+    REAL ap[3], av[3], as[3], bp[3], bf[3];
+    double scale;
+} F(facc);
+
+static void F(forces_part)(const orc_grid* g, const orc_params* P, const orc_state* s, const orc_cells* c,
+                           const orc_boundary* b, const float* rho_in, int64_t i, int lanes, int lane, F(facc) * f)
+{
+    const REAL rho0 = P->rho0, c0 = P->c0;
+    const REAL alpha = P->alpha, nu_k = P->nu;
+    const int morris = P->viscosity_model == 1u;
+    const int visc_on = morris ? (P->nu != 0.0f) : (P->alpha != 0.0f);
+    const int sigma_on = P->sigma != 0.0f;
+    const float* pi = s->pos + 4 * i;
+    const float* vi4 = s->vel + 4 * i;
+    const REAL xi = pi[0], yi = pi[1], zi = pi[2];
+    const REAL vxi = vi4[0], vyi = vi4[1], vzi = vi4[2];
+    const REAL hi = s->h[i], mi = s->m[i];
+    const REAL rhoi = rho_in[i];
+    const REAL pti = F(pressure_term)(rhoi, rho0, c0);
+    const REAL Ki = (((REAL)2 * alpha) * hi) * c0;
+    const REAL ei = ((REAL)0.01 * hi) * hi;
+    const float R = s->h[i] + s->h[i];
+    memset(f, 0, sizeof(*f));
+    orc_iter it;
+    uint32_t jb, je;
+    float sh[3];
+    it_init_lane(&it, g, c->start, c->end, c->ex, pi, R, lanes, lane);
+    while (it_next(&it, &jb, &je, sh)) {
+        for (uint32_t j = jb; j < je; j++) {
+            if ((int64_t)j == i) {
+                continue;
+            }
+            const float* pj = s->pos + 4 * (size_t)j;
+            const REAL dx = xi - NBR(pj, 0);
+            const REAL dy = yi - NBR(pj, 1);
+            const REAL dz = zi - NBR(pj, 2);
+            const REAL r2 = F(dist2)(dx, dy, dz);
+            const REAL hj = s->h[j];
+            const REAL twoh = hj + hj;
+            if (r2 > twoh * twoh) {
+                continue;
+            }
+            REAL invh, wc, dwc;
+            F(kernel_consts)(hj, &invh, &wc, &dwc);
+            const REAL r = SQRT(r2);
+            REAL u[3];
+            if (r > (REAL)0) {
+                const REAL ir = (REAL)1 / r;
+                u[0] = dx * ir;
+                u[1] = dy * ir;
+                u[2] = dz * ir;
+            } else {
+                u[0] = 0;
+                u[1] = 1;
+                u[2] = 0;
+            }
+            const REAL dw = F(kernel_dw)(r, invh, dwc);
+            const REAL mj = s->m[j];
+            const REAL rhoj = rho_in[j];
+            const REAL ptj = F(pressure_term)(rhoj, rho0, c0);
+            {
+                const REAL sp = (mj * dw) * (pti + ptj);
+                for (int a = 0; a < 3; a++) {
+                    f->ap[a] = FMA(-sp, u[a], f->ap[a]);
+                }
+                f->scale += fabs((double)sp);
+            }
+            if (visc_on) {
+                const float* vj4 = s->vel + 4 * (size_t)j;
+                const REAL vd[3] = {vxi - (REAL)vj4[0], vyi - (REAL)vj4[1], vzi - (REAL)vj4[2]};
+                if (!morris) {
+                    const REAL comp = FMA(vd[2], dz, FMA(vd[1], dy, vd[0] * dx));
+                    if (comp < (REAL)0) {
+                        const REAL nuij = Ki / (rhoi + rhoj);
+                        const REAL piv = (-nuij * comp) / (r2 + ei);
+                        const REAL sv = (mj * piv) * dw;
+                        for (int a = 0; a < 3; a++) {
+                            f->av[a] = FMA(-sv, u[a], f->av[a]);
+                        }
+                        f->scale += fabs((double)sv);
+                    }
+                } else {
+                    const REAL coef = ((mj * nu_k) * (rhoi + rhoj)) / (rhoi * rhoj);
+                    const REAL sv = coef * ((r * dw) / (r2 + ei));
+                    for (int a = 0; a < 3; a++) {
+                        f->av[a] = FMA(sv, vd[a], f->av[a]);
+                    }
+                    f->scale +=
+                        fabs((double)sv) * sqrt((double)vd[0] * vd[0] + (double)vd[1] * vd[1] + (double)vd[2] * vd[2]);
+                }
+            }
+            if (sigma_on) {
+                const REAL ss = mj * F(kernel_w)(r, invh, wc);
+                for (int a = 0; a < 3; a++) {
+                    f->as[a] = FMA(ss, u[a], f->as[a]);
+                }
+                f->scale += fabs((double)((REAL)P->sigma / mi) * (double)ss);
+            }
+        }
+    }
+    if (b != NULL && b->n > 0) {
+        REAL invh, wc, dwc;
+        F(kernel_consts)(hi, &invh, &wc, &dwc);
+        const REAL twoh = hi + hi;
+        const REAL cut = twoh * twoh;
+        it_init_lane(&it, g, b->start, b->end, b->ex, pi, R, lanes, lane);
+        while (it_next(&it, &jb, &je, sh)) {
+            for (uint32_t k = jb; k < je; k++) {
+                const float* pb = b->pos + 4 * (size_t)k;
+                const REAL dx = xi - NBR(pb, 0);
+                const REAL dy = yi - NBR(pb, 1);
+                const REAL dz = zi - NBR(pb, 2);
+                const REAL r2 = F(dist2)(dx, dy, dz);
+                if (r2 > cut) {
+                    continue;
+                }
+                const REAL r = SQRT(r2);
+                REAL u[3];
+                if (r > (REAL)0) {
+                    const REAL ir = (REAL)1 / r;
+                    u[0] = dx * ir;
+                    u[1] = dy * ir;
+                    u[2] = dz * ir;
+                } else {
+                    u[0] = 0;
+                    u[1] = 1;
+                    u[2] = 0;
+                }
+                const REAL dw = F(kernel_dw)(r, invh, dwc);
+                const REAL psi = b->psi[k];
+                const REAL sp = (psi * pti) * dw;
+                for (int a = 0; a < 3; a++) {
+                    f->bp[a] = FMA(-sp, u[a], f->bp[a]);
+                }
+                f->scale += fabs((double)sp);
+                const REAL comp = FMA(vzi, dz, FMA(vyi, dy, vxi * dx));
+                if (comp < (REAL)0) {
+                    const REAL nub = (((REAL)b->fric[k] * hi) * c0) / ((REAL)2 * rhoi);
+                    const REAL pib = (-nub * comp) / (r2 + ei);
+                    const REAL sf = (psi * pib) * dw;
+                    for (int a = 0; a < 3; a++) {
+                        f->bf[a] = FMA(-sf, u[a], f->bf[a]);
+                    }
+                    f->scale += fabs((double)sf);
+                }
+            }
+        }
     }
 }
 
@@ -136,173 +342,60 @@ void F(orc_forces_impl)(const orc_grid* g, const orc_params* P, const orc_state*
                         const orc_boundary* b, const float* rho_in, REAL* acc_out, double* scale_out)
 {
     const int64_t n = s->n;
-    const REAL rho0 = P->rho0, c0 = P->c0;
-    const REAL alpha = P->alpha, sigma = P->sigma, nu_k = P->nu;
     const int morris = P->viscosity_model == 1u;
     const int visc_on = morris ? (P->nu != 0.0f) : (P->alpha != 0.0f);
     const int sigma_on = P->sigma != 0.0f;
 #pragma omp parallel for schedule(dynamic, 256)
     for (int64_t i = 0; i < n; i++) {
-        const float* pi = s->pos + 4 * i;
-        const float* vi4 = s->vel + 4 * i;
-        const REAL xi = pi[0], yi = pi[1], zi = pi[2];
-        const REAL vxi = vi4[0], vyi = vi4[1], vzi = vi4[2];
-        const REAL hi = s->h[i], mi = s->m[i];
-        const REAL rhoi = rho_in[i];
-        const REAL pti = F(pressure_term)(rhoi, rho0, c0);
-        const REAL Ki = (((REAL)2 * alpha) * hi) * c0;
-        const REAL ei = ((REAL)0.01 * hi) * hi;
         const float R = s->h[i] + s->h[i];
-        REAL apx = 0, apy = 0, apz = 0, avx = 0, avy = 0, avz = 0, asx = 0, asy = 0, asz = 0;
-        double scale = 0.0;
-        orc_iter it;
-        uint32_t jb, je;
-        float sh[3];
-        it_init(&it, g, c->start, c->end, c->ex, pi, R);
-        while (it_next(&it, &jb, &je, sh)) {
-            for (uint32_t j = jb; j < je; j++) {
-                if ((int64_t)j == i) {
-                    continue;
-                }
-                const float* pj = s->pos + 4 * (size_t)j;
-                const REAL dx = xi - NBR(pj, 0);
-                const REAL dy = yi - NBR(pj, 1);
-                const REAL dz = zi - NBR(pj, 2);
-                const REAL r2 = F(dist2)(dx, dy, dz);
-                const REAL hj = s->h[j];
-                const REAL twoh = hj + hj;
-                if (r2 > twoh * twoh) {
-                    continue;
-                }
-                REAL invh, wc, dwc;
-                F(kernel_consts)(hj, &invh, &wc, &dwc);
-                const REAL r = SQRT(r2);
-                REAL ux, uy, uz;
-                if (r > (REAL)0) {
-                    const REAL ir = (REAL)1 / r;
-                    ux = dx * ir;
-                    uy = dy * ir;
-                    uz = dz * ir;
-                } else {
-                    ux = 0;
-                    uy = 1;
-                    uz = 0;
-                }
-                const REAL dw = F(kernel_dw)(r, invh, dwc);
-                const REAL mj = s->m[j];
-                const REAL rhoj = rho_in[j];
-                const REAL ptj = F(pressure_term)(rhoj, rho0, c0);
-                {
-                    const REAL sp = (mj * dw) * (pti + ptj);
-                    apx = FMA(-sp, ux, apx);
-                    apy = FMA(-sp, uy, apy);
-                    apz = FMA(-sp, uz, apz);
-                    scale += fabs((double)sp);
-                }
-                if (visc_on) {
-                    const float* vj4 = s->vel + 4 * (size_t)j;
-                    const REAL vdx = vxi - (REAL)vj4[0];
-                    const REAL vdy = vyi - (REAL)vj4[1];
-                    const REAL vdz = vzi - (REAL)vj4[2];
-                    if (!morris) {
-                        const REAL comp = FMA(vdz, dz, FMA(vdy, dy, vdx * dx));
-                        if (comp < (REAL)0) {
-                            const REAL nuij = Ki / (rhoi + rhoj);
-                            const REAL piv = (-nuij * comp) / (r2 + ei);
-                            const REAL sv = (mj * piv) * dw;
-                            avx = FMA(-sv, ux, avx);
-                            avy = FMA(-sv, uy, avy);
-                            avz = FMA(-sv, uz, avz);
-                            scale += fabs((double)sv);
-                        }
-                    } else {
-                        const REAL coef = ((mj * nu_k) * (rhoi + rhoj)) / (rhoi * rhoj);
-                        const REAL sv = coef * ((r * dw) / (r2 + ei));
-                        avx = FMA(sv, vdx, avx);
-                        avy = FMA(sv, vdy, avy);
-                        avz = FMA(sv, vdz, avz);
-                        scale += fabs((double)sv) * sqrt((double)vdx * vdx + (double)vdy * vdy + (double)vdz * vdz);
-                    }
-                }
-                if (sigma_on) {
-                    const REAL ss = mj * F(kernel_w)(r, invh, wc);
-                    asx = FMA(ss, ux, asx);
-                    asy = FMA(ss, uy, asy);
-                    asz = FMA(ss, uz, asz);
-                    scale += fabs((double)(sigma / mi) * (double)ss);
-                }
+        F(facc) f;
+        if (box_cells(g, s->pos + 4 * i, R) > ORC_HEAVY_CELLS) {
+            F(facc) part[ORC_LANES];
+            for (int l = 0; l < ORC_LANES; l++) {
+                F(forces_part)(g, P, s, c, b, rho_in, i, ORC_LANES, l, &part[l]);
             }
-        }
-        REAL bpx = 0, bpy = 0, bpz = 0, bfx = 0, bfy = 0, bfz = 0;
-        if (b != NULL && b->n > 0) {
-            REAL invh, wc, dwc;
-            F(kernel_consts)(hi, &invh, &wc, &dwc);
-            const REAL twoh = hi + hi;
-            const REAL cut = twoh * twoh;
-            it_init(&it, g, b->start, b->end, b->ex, pi, R);
-            while (it_next(&it, &jb, &je, sh)) {
-                for (uint32_t k = jb; k < je; k++) {
-                    const float* pb = b->pos + 4 * (size_t)k;
-                    const REAL dx = xi - NBR(pb, 0);
-                    const REAL dy = yi - NBR(pb, 1);
-                    const REAL dz = zi - NBR(pb, 2);
-                    const REAL r2 = F(dist2)(dx, dy, dz);
-                    if (r2 > cut) {
-                        continue;
-                    }
-                    const REAL r = SQRT(r2);
-                    REAL ux, uy, uz;
-                    if (r > (REAL)0) {
-                        const REAL ir = (REAL)1 / r;
-                        ux = dx * ir;
-                        uy = dy * ir;
-                        uz = dz * ir;
-                    } else {
-                        ux = 0;
-                        uy = 1;
-                        uz = 0;
-                    }
-                    const REAL dw = F(kernel_dw)(r, invh, dwc);
-                    const REAL psi = b->psi[k];
-                    const REAL sp = (psi * pti) * dw;
-                    bpx = FMA(-sp, ux, bpx);
-                    bpy = FMA(-sp, uy, bpy);
-                    bpz = FMA(-sp, uz, bpz);
-                    scale += fabs((double)sp);
-                    const REAL comp = FMA(vzi, dz, FMA(vyi, dy, vxi * dx));
-                    if (comp < (REAL)0) {
-                        const REAL nub = (((REAL)b->fric[k] * hi) * c0) / ((REAL)2 * rhoi);
-                        const REAL pib = (-nub * comp) / (r2 + ei);
-                        const REAL sf = (psi * pib) * dw;
-                        bfx = FMA(-sf, ux, bfx);
-                        bfy = FMA(-sf, uy, bfy);
-                        bfz = FMA(-sf, uz, bfz);
-                        scale += fabs((double)sf);
-                    }
-                }
+            memset(&f, 0, sizeof(f));
+            REAL t[ORC_LANES];
+#define ORC_REDUCE(field, a)                       \
+    for (int l = 0; l < ORC_LANES; l++) {          \
+        t[l] = part[l].field[a];                   \
+    }                                              \
+    f.field[a] = F(butterfly)(t);
+            for (int a = 0; a < 3; a++) {
+                ORC_REDUCE(ap, a)
+                ORC_REDUCE(av, a)
+                ORC_REDUCE(as, a)
+                ORC_REDUCE(bp, a)
+                ORC_REDUCE(bf, a)
             }
+#undef ORC_REDUCE
+            for (int l = 0; l < ORC_LANES; l++) {
+                f.scale += part[l].scale;
+            }
+        } else {
+            F(forces_part)(g, P, s, c, b, rho_in, i, 1, 0, &f);
         }
         REAL ax = P->gravity[0], ay = P->gravity[1], az = P->gravity[2];
-        ax = ax + apx;
-        ay = ay + apy;
-        az = az + apz;
+        ax = ax + f.ap[0];
+        ay = ay + f.ap[1];
+        az = az + f.ap[2];
         if (visc_on) {
-            ax = ax + avx;
-            ay = ay + avy;
-            az = az + avz;
+            ax = ax + f.av[0];
+            ay = ay + f.av[1];
+            az = az + f.av[2];
         }
         if (sigma_on) {
-            const REAL f = sigma / mi;
-            ax = ax + f * asx;
-            ay = ay + f * asy;
-            az = az + f * asz;
+            const REAL fs = (REAL)P->sigma / (REAL)s->m[i];
+            ax = ax + fs * f.as[0];
+            ay = ay + fs * f.as[1];
+            az = az + fs * f.as[2];
         }
-        ax = ax + bpx;
-        ay = ay + bpy;
-        az = az + bpz;
-        ax = ax + bfx;
-        ay = ay + bfy;
-        az = az + bfz;
+        ax = ax + f.bp[0];
+        ay = ay + f.bp[1];
+        az = az + f.bp[2];
+        ax = ax + f.bf[0];
+        ay = ay + f.bf[1];
+        az = az + f.bf[2];
         acc_out[4 * i + 0] = ax;
         acc_out[4 * i + 1] = ay;
         acc_out[4 * i + 2] = az;
@@ -310,7 +403,7 @@ void F(orc_forces_impl)(const orc_grid* g, const orc_params* P, const orc_state*
         if (scale_out != NULL) {
             const double g2 = (double)P->gravity[0] * P->gravity[0] + (double)P->gravity[1] * P->gravity[1] +
                               (double)P->gravity[2] * P->gravity[2];
-            scale_out[i] = scale + sqrt(g2);
+            scale_out[i] = f.scale + sqrt(g2);
         }
     }
 }
