@@ -21,14 +21,18 @@ struct StepArgs {
 };
 
 // Per-particle neighbour lists of the current step: row i holds the accepted neighbours of particle i in the
-// canonical candidate order, idx[i * maxn + k]. cnt[i] > maxn marks an overflowed row (the force pass scans the
-// cells again); cnt[i] == kHeavyMark marks a heavy particle, queued in heavy[0, *heavy_n) for the warp kernels.
+// canonical candidate order, idx[i * maxn + k]. cnt[i] == kHeavyMark marks a particle whose query box spans more
+// than 27 reference cells: queued in heavy[0, *heavy_n) for the warp density kernel. Those particles and every
+// particle with more than maxn neighbours (cnt[i] > maxn, the row overflowed) are queued in fheavy for the warp
+// force kernel.
 constexpr uint32_t kHeavyMark = 0xffffffffu;
 struct NbrDev {
     uint32_t* idx;
     uint32_t* cnt;
     uint32_t* heavy;
     uint32_t* heavy_n;
+    uint32_t* fheavy;
+    uint32_t* fheavy_n;
     uint32_t maxn;
 };
 

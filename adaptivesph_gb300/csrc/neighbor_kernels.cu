@@ -340,6 +340,7 @@ __global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, Boun
     const uint32_t kept = cnt < maxn ? cnt : maxn;
     for (uint32_t q = 0; q < staged; ++q) row[kept - staged + q] = st[q];
     nl.cnt[i] = cnt;
+    if (cnt > maxn) nl.fheavy[atomicAdd(nl.fheavy_n, 1u)] = i;  // too many neighbours for a row: warp force pass
     float rb = 0.0f;
     if (boundary_near(a.grid, b, pi.x, pi.y, pi.z, R)) rb = boundary_density<1>(a, b, i, pi, 0);
     const float rh = rho + rb;
@@ -371,41 +372,34 @@ __global__ void __launch_bounds__(256, 1) k_density_heavy(StepArgs a, CellsDev c
             const float rh = rho + rb;
             if (!isfinite(rh)) atomicOr(a.err, 0x2u);
             a.rp[i] = make_float2(rh, pressure_term(rh, a.phys.rho0, a.phys.B));
+            nl.fheavy[atomicAdd(nl.fheavy_n, 1u)] = i;
         }
     }
 }
 
-// Force pass, ordinary particles: walks the particle's neighbour list (or, if it overflowed, the cells again).
+// Force pass, ordinary particles: walks the particle's neighbour list. Heavy particles and particles whose row
+// overflowed are left to k_forces_heavy.
 template <bool kMorris>
 __global__ void __launch_bounds__(256, 3) k_forces(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     const uint32_t cnt = nl.cnt[i];
-    if (cnt == kHeavyMark) return;
+    if (cnt > nl.maxn) return;  // heavy or overflowed: k_forces_heavy
     const ForceCtx x = force_ctx(a, i);
     ForceAcc f = {};
-    if (cnt <= nl.maxn) {
-        const uint4* row = reinterpret_cast<const uint4*>(nl.idx + (size_t)i * nl.maxn);
-        for (uint32_t k = 0; k < cnt; k += 4) {
-            const uint4 e4 = __ldg(row + (k >> 2));
-            const uint32_t e[4] = {e4.x, e4.y, e4.z, e4.w};
+    const uint4* row = reinterpret_cast<const uint4*>(nl.idx + (size_t)i * nl.maxn);
+    for (uint32_t k = 0; k < cnt; k += 4) {
+        const uint4 e4 = __ldg(row + (k >> 2));
+        const uint32_t e[4] = {e4.x, e4.y, e4.z, e4.w};
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-                if (k + q >= cnt) break;
-                uint32_t j;
-                float shx, shy, shz;
-                decode_entry(a.grid, e[q], j, shx, shy, shz);
-                if (j == i) continue;
-                force_term<kMorris>(a, x, j, shx, shy, shz, f);
-            }
+        for (int q = 0; q < 4; q++) {
+            if (k + q >= cnt) break;
+            uint32_t j;
+            float shx, shy, shz;
+            decode_entry(a.grid, e[q], j, shx, shy, shz);
+            if (j == i) continue;
+            force_term<kMorris>(a, x, j, shx, shy, shz, f);
         }
-    } else {
-        fluid_candidates<true>(a, c, x.pi, [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
-            for (uint32_t j = jb; j < je; ++j) {
-                if (j == i) continue;
-                force_term<kMorris>(a, x, j, shx, shy, shz, f);
-            }
-        });
     }
     if (boundary_near(a.grid, b, x.pi.x, x.pi.y, x.pi.z, x.hi + x.hi)) boundary_forces<1>(a, b, i, x, f, 0);
     finish_force(a, i, x, f);
@@ -417,9 +411,9 @@ __global__ void __launch_bounds__(256, 1) k_forces_heavy(StepArgs a, CellsDev c,
     const int lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t nh = *nl.heavy_n;
+    const uint32_t nh = *nl.fheavy_n;
     for (uint32_t w = warp; w < nh; w += nwarps) {
-        const uint32_t i = nl.heavy[w];
+        const uint32_t i = nl.fheavy[w];
         const ForceCtx x = force_ctx(a, i);
         ForceAcc f = {};
         for_each_cell<true, 32>(
@@ -447,6 +441,7 @@ __global__ void __launch_bounds__(256, 1) k_forces_heavy(StepArgs a, CellsDev c,
 cudaError_t launch_density(uint32_t blocks, uint32_t heavy_blocks, cudaStream_t stream, StepArgs a, CellsDev c,
                            BoundaryDev b, NbrDev nl) {
     cudaError_t e = cudaMemsetAsync(nl.heavy_n, 0, sizeof(uint32_t), stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(nl.fheavy_n, 0, sizeof(uint32_t), stream);
     if (e != cudaSuccess) return e;
     k_density<<<blocks, 256, 0, stream>>>(a, c, b, nl);
     k_density_heavy<<<heavy_blocks, 256, 0, stream>>>(a, c, b, nl);

@@ -142,6 +142,8 @@ struct asph_simulation {
     uint32_t* nbr_cnt = nullptr;  // [cap]
     uint32_t* heavy_idx = nullptr;  // [cap] queue of heavy particles of the current step
     uint32_t* heavy_n = nullptr;
+    uint32_t* fheavy_idx = nullptr;  // [cap] queue of the force pass's warp kernel
+    uint32_t* fheavy_n = nullptr;
     uint32_t maxn = 256;
     uint32_t* keys = nullptr;
     uint32_t* vals = nullptr;
@@ -234,7 +236,7 @@ struct asph_simulation {
 
     CellsDev cells() const { return CellsDev{cell_start, cell_end, cell_hmax, hmax_ref, ex}; }
 
-    NbrDev nbrs() const { return NbrDev{nbr_idx, nbr_cnt, heavy_idx, heavy_n, maxn}; }
+    NbrDev nbrs() const { return NbrDev{nbr_idx, nbr_cnt, heavy_idx, heavy_n, fheavy_idx, fheavy_n, maxn}; }
 
     BoundaryDev boundary() const {
         return BoundaryDev{bpos, bfric, bstart, bend, brefflag, bex[0], bex[1], nb};
@@ -734,6 +736,8 @@ void destroy(asph_simulation* s) {
     dfree(s->nbr_cnt);
     dfree(s->heavy_idx);
     dfree(s->heavy_n);
+    dfree(s->fheavy_idx);
+    dfree(s->fheavy_n);
     dfree(s->keys);
     dfree(s->vals);
     dfree(s->sort_mem);
@@ -972,6 +976,8 @@ asph_status asph_simulation_create(const asph_parameters* parameters, const floa
     TRY(dalloc(s->nbr_cnt, C));
     TRY(dalloc(s->heavy_idx, C));
     TRY(dalloc(s->heavy_n, 1));
+    TRY(dalloc(s->fheavy_idx, C));
+    TRY(dalloc(s->fheavy_n, 1));
     const uint32_t sort_items = std::max(C, std::max(boundary_count, max_boundary_capacity));
     TRY(dalloc(s->keys, sort_items));
     TRY(dalloc(s->vals, sort_items));

@@ -485,6 +485,31 @@ float orc_cbrtf(float xf)
 static const float ORC_PI_F = 3.141592653589793f;
 #define ORC_LANES 32       /* lanes of the warp that sums a heavy particle */
 #define ORC_HEAVY_CELLS 27 /* query boxes of more reference cells than this are heavy */
+#define ORC_MAXN 256       /* neighbour-list row length; a particle with more neighbours is heavy in the force pass */
+
+/* neighbours accepted by the density pass (self included): r^2 <= (2 h_j)^2 over the candidate cells */
+static uint32_t accepted_count(const orc_grid* g, const orc_state* s, const orc_cells* c, int64_t i)
+{
+    const float* pi = s->pos + 4 * i;
+    const float R = s->h[i] + s->h[i];
+    uint32_t cnt = 0;
+    orc_iter it;
+    uint32_t jb, je;
+    float sh[3];
+    it_init(&it, g, c->start, c->end, c->ex, pi, R);
+    while (it_next(&it, &jb, &je, sh)) {
+        for (uint32_t j = jb; j < je; j++) {
+            const float* pj = s->pos + 4 * (size_t)j;
+            const float dx = (g->periodic ? pj[0] + sh[0] : pj[0]) - pi[0];
+            const float dy = (g->periodic ? pj[1] + sh[1] : pj[1]) - pi[1];
+            const float dz = (g->periodic ? pj[2] + sh[2] : pj[2]) - pi[2];
+            const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            const float twoh = s->h[j] + s->h[j];
+            cnt += r2 <= twoh * twoh;
+        }
+    }
+    return cnt;
+}
 
 #define REAL float
 #define F(name) name##_f32

@@ -22,7 +22,8 @@
  * whose query box spans more than ORC_HEAVY_CELLS reference cells ("heavy", after merges made h large) is summed
  * as the GPU sums it with one warp: the box's reference cells are dealt round-robin to 32 lanes by ordinal,
  * each lane sums its cells in order, and the 32 partial sums are combined by the butterfly
- * s_l <- s_l + s_(l xor o) for o = 16, 8, 4, 2, 1.
+ * s_l <- s_l + s_(l xor o) for o = 16, 8, 4, 2, 1. In the force pass a particle with more than ORC_MAXN accepted
+ * neighbours (more than a neighbour-list row holds) is summed the same way.
  */
 
 /* W(r, h) with precomputed 1/h and coef/h^3 */
@@ -349,7 +350,7 @@ void F(orc_forces_impl)(const orc_grid* g, const orc_params* P, const orc_state*
     for (int64_t i = 0; i < n; i++) {
         const float R = s->h[i] + s->h[i];
         F(facc) f;
-        if (box_cells(g, s->pos + 4 * i, R) > ORC_HEAVY_CELLS) {
+        if (box_cells(g, s->pos + 4 * i, R) > ORC_HEAVY_CELLS || accepted_count(g, s, c, i) > ORC_MAXN) {
             F(facc) part[ORC_LANES];
             for (int l = 0; l < ORC_LANES; l++) {
                 F(forces_part)(g, P, s, c, b, rho_in, i, ORC_LANES, l, &part[l]);

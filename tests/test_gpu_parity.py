@@ -91,6 +91,38 @@ def test_forces_bitexact_and_fp64():
     assert (err / scale).max() <= FORCE_RTOL, (err / scale).max()
 
 
+def _mixed_h_state(sim, orc, sc, seed=7):
+    """State with smoothing lengths h0, 1.5 h0, 3 h0 and 6 h0 mixed at random: large boxes (heavy particles, one
+    warp each) and neighbour counts above the list row length (overflow, warp force pass) both occur."""
+    st = sim.read_state()
+    rng = np.random.default_rng(seed)
+    h0 = np.float32(sc.parameters.base_smoothing_radius)
+    choice = rng.choice(4, size=st["h"].shape[0], p=[0.85, 0.08, 0.05, 0.02])
+    st["h"] = (h0 * np.array([1.0, 1.5, 3.0, 6.0], np.float32)[choice]).astype(np.float32)
+    sim.write_state(st, frame=5, next_id=int(st["id"].max()) + 1, pending_half=sc.dt / 2)
+    orc.load(st, frame=5, next_id=int(st["id"].max()) + 1, pending_half=sc.dt / 2)
+    return st
+
+
+def test_mixed_smoothing_lengths_bitexact():
+    sc = small_dam_break(counts=(16, 24, 16), dx=0.02, tank=(0.7, 0.7, 0.5))
+    sim, orc = make_pair(sc)
+    _advance(sim, orc, sc.dt, 2)
+    _mixed_h_state(sim, orc, sc)
+    sim.run_stages(sc.dt, _lib.STAGE_FORCES)
+    orc.integrate(sc.dt)
+    orc.grid_build()
+    nc = orc.neighbor_counts()
+    orc.rho[: orc.n] = orc.density32()
+    g = sim.read_state()
+    assert_bitexact("rho", g["rho"], orc.rho[: orc.n])
+    assert_bitexact("acc", g["acc"], orc.forces32())
+    assert (nc + 1).max() > 256, "the state must overflow a neighbour-list row"
+    a64, scale = orc.forces64()
+    err = np.abs(g["acc"][:, :3].astype(np.float64) - a64[:, :3]).max(axis=1)
+    assert (err / scale).max() <= FORCE_RTOL, (err / scale).max()
+
+
 def test_neighbor_counts_exact():
     sc = small_dam_break()
     sim, orc = make_pair(sc)
