@@ -203,14 +203,11 @@ __device__ __forceinline__ float gap1(float p, float lo, float w, float m) {
 // hold a member within reach of p is skipped: reach = Rfix when Rfix > 0, else 2 * (max h of the cell). Culling
 // never skips a member that passes a support test, so sums over the visited members are unchanged.
 // body(begin, end, shx, shy, shz) gets the member range and the periodic image offsets.
-// With kLanes = 32 the reference cells of the box are dealt round-robin to the lanes of a warp by their ordinal
-// in the box (z, y, x order): lane l visits ordinals o with o % 32 == l (the order of the heavy-particle passes).
-template <bool kCull, int kLanes = 1, class Body>
+template <bool kCull, class Body>
 __device__ __forceinline__ void for_each_cell(const GridDev& g, const uint32_t* __restrict__ start,
                                               const uint32_t* __restrict__ end, const float* __restrict__ hmax,
                                               const float* __restrict__ hmax_ref, uint32_t ex0, uint32_t ex1,
-                                              float px, float py, float pz, float R, float Rfix, Body&& body,
-                                              int lane = 0) {
+                                              float px, float py, float pz, float R, float Rfix, Body&& body) {
     int32_t lo[3], hi[3];
     const float p[3] = {px, py, pz};
     bool ok = true;
@@ -219,12 +216,9 @@ __device__ __forceinline__ void for_each_cell(const GridDev& g, const uint32_t* 
     if (!ok) return;
     const bool periodic = g.periodic;
     const float m = g.cull_margin;
-    int32_t ord = -1;
     for (int32_t rz = lo[2]; rz <= hi[2]; ++rz) {
         for (int32_t ry = lo[1]; ry <= hi[1]; ++ry) {
             for (int32_t rx = lo[0]; rx <= hi[0]; ++rx) {
-                ++ord;
-                if (kLanes > 1 && (ord & (kLanes - 1)) != lane) continue;
                 float shz, shy, shx;
                 const int32_t cz = wrap_cell(rz, g.gs[2], g.scale[2], periodic, shz);
                 if (cz < 0 || cz >= g.gs[2]) continue;
@@ -276,6 +270,90 @@ __device__ __forceinline__ void for_each_cell(const GridDev& g, const uint32_t* 
             }
         }
     }
+}
+
+// Warp-cooperative form of for_each_cell<true> for the 32 particles of a warp (one per lane; `active` lanes only).
+// The warp walks the union of the lanes' boxes in the canonical order (reference cells z, y, x; their sub-cells
+// z, y, x) and calls body(begin, end, shx, shy, shz, need) warp-uniformly for every sub-cell that some lane needs;
+// `need` tells the calling lane whether the sub-cell is one of its own candidate cells that survived its culling.
+// Restricted to one lane, the visited sequence is exactly that lane's for_each_cell<true> sequence, so per-lane
+// sums keep their order; lanes share every candidate load. Returns false (having visited nothing) when the union
+// spans more than max_union reference cells; the caller then falls back to for_each_cell per lane.
+template <class Body>
+__device__ __forceinline__ bool for_each_cell_warp(const GridDev& g, const uint32_t* __restrict__ start,
+                                                   const uint32_t* __restrict__ end, const float* __restrict__ hmax,
+                                                   const float* __restrict__ hmax_ref, uint32_t ex0, uint32_t ex1,
+                                                   bool active, float px, float py, float pz, float R,
+                                                   int32_t max_union, Body&& body) {
+    int32_t lo[3], hi[3];
+    const float p[3] = {px, py, pz};
+    bool ok = active;
+#pragma unroll
+    for (int a = 0; a < 3; a++) ok &= box_axis(g, a, p[a], R, lo[a], hi[a]);
+    int32_t ulo[3], uhi[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        ulo[a] = __reduce_min_sync(0xffffffffu, ok ? lo[a] : 0x7fffffff);
+        uhi[a] = __reduce_max_sync(0xffffffffu, ok ? hi[a] : (int32_t)0x80000000);
+    }
+    if (!__any_sync(0xffffffffu, ok)) return true;
+    const int64_t span = (int64_t)(uhi[0] - ulo[0] + 1) * (uhi[1] - ulo[1] + 1) * (uhi[2] - ulo[2] + 1);
+    if (span > max_union) return false;
+    const bool periodic = g.periodic;
+    const float m = g.cull_margin;
+    for (int32_t rz = ulo[2]; rz <= uhi[2]; ++rz) {
+        for (int32_t ry = ulo[1]; ry <= uhi[1]; ++ry) {
+            for (int32_t rx = ulo[0]; rx <= uhi[0]; ++rx) {
+                float shz, shy, shx;
+                const int32_t cz = wrap_cell(rz, g.gs[2], g.scale[2], periodic, shz);
+                const int32_t cy = wrap_cell(ry, g.gs[1], g.scale[1], periodic, shy);
+                const int32_t cx = wrap_cell(rx, g.gs[0], g.scale[0], periodic, shx);
+                if (cz < 0 || cz >= g.gs[2] || cy < 0 || cy >= g.gs[1] || cx < 0 || cx >= g.gs[0]) continue;
+                const uint32_t rk = (uint32_t)cx + (uint32_t)g.gs[0] * ((uint32_t)cy + (uint32_t)g.gs[1] * (uint32_t)cz);
+                if (!periodic && (rk == ex0 || rk == ex1)) continue;
+                const float hr = __ldg(hmax_ref + rk);
+                if (hr <= 0.0f) continue;
+                bool need = ok && rx >= lo[0] && rx <= hi[0] && ry >= lo[1] && ry <= hi[1] && rz >= lo[2] &&
+                            rz <= hi[2];
+                const float reach = 2.0f * hr * 1.00005f;
+                const float sh[3] = {shx, shy, shz};
+                const int32_t c3[3] = {cx, cy, cz};
+                bool k0[3], k1[3];
+                float d2 = 0.0f;
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    const float base = g.dmin[a] + (float)c3[a] * g.cs[a] + sh[a];
+                    const float d = gap1(p[a], base, g.cs[a], m);
+                    d2 += d * d;
+                    k0[a] = gap1(p[a], base, g.w[a], m) <= reach;
+                    k1[a] = gap1(p[a], base + g.w[a], g.w[a], m) <= reach;
+                    need &= (k0[a] || k1[a]);
+                }
+                need &= d2 <= reach * reach;
+                if (!__any_sync(0xffffffffu, need)) continue;
+#pragma unroll 1
+                for (int q = 0; q < 8; ++q) {
+                    const int dx = q & 1, dy = (q >> 1) & 1, dz = q >> 2;
+                    const int32_t sx = 2 * cx + dx, sy = 2 * cy + dy, sz = 2 * cz + dz;
+                    const uint32_t lin =
+                        (uint32_t)sx + (uint32_t)g.sgs[0] * ((uint32_t)sy + (uint32_t)g.sgs[1] * (uint32_t)sz);
+                    const uint32_t b = __ldg(start + lin);
+                    if (b == kEmpty) continue;
+                    bool ns = need && (dx ? k1[0] : k0[0]) && (dy ? k1[1] : k0[1]) && (dz ? k1[2] : k0[2]);
+                    if (ns) {
+                        const float rs = 2.0f * __ldg(hmax + lin) * 1.00005f;
+                        const float ex = gap1(px, g.dmin[0] + (float)sx * g.w[0] + shx, g.w[0], m);
+                        const float ey = gap1(py, g.dmin[1] + (float)sy * g.w[1] + shy, g.w[1], m);
+                        const float ez = gap1(pz, g.dmin[2] + (float)sz * g.w[2] + shz, g.w[2], m);
+                        ns = ex * ex + ey * ey + ez * ez <= rs * rs;
+                    }
+                    if (!__any_sync(0xffffffffu, ns)) continue;
+                    body(b, __ldg(end + lin), shx, shy, shz, ns);
+                }
+            }
+        }
+    }
+    return true;
 }
 
 }  // namespace asph

@@ -4,14 +4,15 @@
 // cuda/src/algorithm/BoundaryAlgorithm.cu:15-51) and the acceleration kernels (Algorithm.cu:56-232,
 // BoundaryAlgorithm.cu:53-162) of SphSimulation::update (cuda/src/simulation/SphSimulation.cu:101-120).
 //
-// Ordinary particles: one thread per particle. The density pass scans the candidate cells in the canonical order,
-// sums the density as it goes and records the accepted neighbours (self included) in the particle's row of the
-// neighbour list; rows are staged in shared memory and flushed 16 entries (64 bytes) at a time, so list writes are
-// whole-segment stores. The force pass walks the row (16-byte loads) instead of the cells.
-// Heavy particles (query box of more than 27 reference cells, i.e. smoothing lengths grown by merging): one warp
-// per particle, the box's reference cells dealt round-robin to the lanes, partial sums combined by a fixed
-// butterfly; they are queued by the density pass and handled by separate warp kernels, so a few large boxes do not
-// stall whole blocks.
+// Ordinary particles: one thread per particle. In the density pass the 32 particles of a warp (neighbours in the
+// cell order) walk the union of their candidate cells together in the canonical order, each lane testing every
+// candidate of its own cells (shared loads, no divergent loop control); each lane sums its density in its own
+// canonical order and records its accepted neighbours (self included) in its row of the neighbour list. Rows are
+// staged in shared memory and flushed 16 entries (64 bytes) at a time. The force pass walks the row.
+// Heavy particles (query box of more than 27 reference cells: smoothing lengths grown by merging) and, in the force
+// pass, particles with more neighbours than a row holds: one warp per particle; in every visited sub-cell member m
+// goes to lane m mod 32, lane sums are combined by a fixed butterfly. The density pass queues them for separate
+// warp kernels, so a few large boxes do not stall whole blocks.
 #include "asph_device.cuh"
 #include "asph_kernels.cuh"
 
@@ -24,6 +25,7 @@ constexpr uint32_t kIdxMask = (1u << kIdxBits) - 1u;
 constexpr int kStage = 16;         // list entries staged per thread before a flush
 constexpr int kStageStride = 17;   // padded row (no bank conflicts between threads)
 constexpr int kHeavyCells = 27;    // more reference cells than this in the query box: heavy particle
+constexpr int32_t kMaxUnion = 64;  // a warp walks its lanes' boxes together when their union is at most this big
 
 // Periodic image of a listed neighbour: the index keeps 27 bits, the cell's image offset (-1, 0, +1 per axis)
 // is packed into the top 5 bits.
@@ -119,10 +121,10 @@ __device__ __forceinline__ float boundary_density(const StepArgs& a, const Bound
     const float cut = R * R;
     const bool periodic = a.grid.periodic;
     float rb = 0.0f;
-    for_each_cell<false, kLanes>(
+    for_each_cell<false>(
         a.grid, b.start, b.end, nullptr, nullptr, b.ex0, b.ex1, pi.x, pi.y, pi.z, R, 0.0f,
         [&](uint32_t kb, uint32_t ke, float shx, float shy, float shz) {
-            for (uint32_t k = kb; k < ke; ++k) {
+            for (uint32_t k = kb + lane; k < ke; k += kLanes) {
                 const float4 pb = __ldg(b.pos + k);
                 const float xb = periodic ? pb.x + shx : pb.x;
                 const float yb = periodic ? pb.y + shy : pb.y;
@@ -133,8 +135,7 @@ __device__ __forceinline__ float boundary_density(const StepArgs& a, const Bound
                 const float w = kernel_w(sqrtf(r2), ki.x, ki.y);
                 rb = fmaf(pb.w, w, rb);
             }
-        },
-        lane);
+        });
     return rb;
 }
 
@@ -234,10 +235,10 @@ __device__ __forceinline__ void boundary_forces(const StepArgs& a, const Boundar
     const float cut = R * R;
     const bool periodic = a.grid.periodic;
     const float c0 = a.phys.c0;
-    for_each_cell<false, kLanes>(
+    for_each_cell<false>(
         a.grid, b.start, b.end, nullptr, nullptr, b.ex0, b.ex1, c.pi.x, c.pi.y, c.pi.z, R, 0.0f,
         [&](uint32_t kb, uint32_t ke, float shx, float shy, float shz) {
-            for (uint32_t k = kb; k < ke; ++k) {
+            for (uint32_t k = kb + lane; k < ke; k += kLanes) {
                 const float4 pb = __ldg(b.pos + k);
                 const float xb = periodic ? pb.x + shx : pb.x;
                 const float yb = periodic ? pb.y + shy : pb.y;
@@ -271,8 +272,7 @@ __device__ __forceinline__ void boundary_forces(const StepArgs& a, const Boundar
                     for (int q = 0; q < 3; q++) f.bf[q] = fmaf(-sf, u[q], f.bf[q]);
                 }
             }
-        },
-        lane);
+        });
 }
 
 // a = g + pressure + viscosity + cohesion + boundary pressure + boundary friction, in the reference's kernel order.
@@ -305,21 +305,23 @@ __device__ __forceinline__ void fluid_candidates(const StepArgs& a, const CellsD
 __global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
     __shared__ uint32_t stage[256 * kStageStride];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
-    const float4 pi = a.ph[i];
+    const bool in = i < a.n;
+    const float4 pi = in ? a.ph[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const float R = pi.w + pi.w;
-    if (box_cells(a.grid, pi, R) > kHeavyCells) {
+    bool active = in;
+    if (in && box_cells(a.grid, pi, R) > kHeavyCells) {
         nl.cnt[i] = kHeavyMark;
         nl.heavy[atomicAdd(nl.heavy_n, 1u)] = i;
-        return;
+        active = false;
     }
     const bool periodic = a.grid.periodic;
-    uint32_t* row = nl.idx + (size_t)i * nl.maxn;
+    uint32_t* row = nl.idx + (size_t)(in ? i : 0) * nl.maxn;
     uint32_t* st = stage + threadIdx.x * kStageStride;
     const uint32_t maxn = nl.maxn;
     uint32_t cnt = 0, staged = 0;
     float rho = 0.0f;
-    fluid_candidates<true>(a, c, pi, [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
+    auto scan = [&](uint32_t jb, uint32_t je, float shx, float shy, float shz, bool need) {
+        if (!need) return;
         const uint32_t code = periodic ? (shift_code(shx, shy, shz) << kIdxBits) : 0u;
         for (uint32_t j = jb; j < je; ++j) {
             if (!density_term(a, pi, j, shx, shy, shz, rho)) continue;
@@ -335,7 +337,16 @@ __global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, Boun
             }
             cnt++;
         }
-    });
+    };
+    // the warp's 32 particles are neighbours in the cell order: walk the union of their boxes together
+    const bool together = for_each_cell_warp(a.grid, c.start, c.end, c.hmax, c.hmax_ref, c.ex[0], c.ex[1], active,
+                                             pi.x, pi.y, pi.z, R, kMaxUnion, scan);
+    if (!together && active) {
+        fluid_candidates<true>(a, c, pi, [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
+            scan(jb, je, shx, shy, shz, true);
+        });
+    }
+    if (!active) return;
     // remaining staged entries (fewer than a full segment)
     const uint32_t kept = cnt < maxn ? cnt : maxn;
     for (uint32_t q = 0; q < staged; ++q) row[kept - staged + q] = st[q];
@@ -359,12 +370,11 @@ __global__ void __launch_bounds__(256, 1) k_density_heavy(StepArgs a, CellsDev c
         const float4 pi = a.ph[i];
         const float R = pi.w + pi.w;
         float rho = 0.0f;
-        for_each_cell<true, 32>(
+        for_each_cell<true>(
             a.grid, c.start, c.end, c.hmax, c.hmax_ref, c.ex[0], c.ex[1], pi.x, pi.y, pi.z, R, 0.0f,
             [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
-                for (uint32_t j = jb; j < je; ++j) density_term(a, pi, j, shx, shy, shz, rho);
-            },
-            lane);
+                for (uint32_t j = jb + lane; j < je; j += 32) density_term(a, pi, j, shx, shy, shz, rho);
+            });
         rho = warp_sum_butterfly(rho);
         float rb = 0.0f;
         if (boundary_near(a.grid, b, pi.x, pi.y, pi.z, R)) rb = warp_sum_butterfly(boundary_density<32>(a, b, i, pi, lane));
@@ -416,15 +426,14 @@ __global__ void __launch_bounds__(256, 1) k_forces_heavy(StepArgs a, CellsDev c,
         const uint32_t i = nl.fheavy[w];
         const ForceCtx x = force_ctx(a, i);
         ForceAcc f = {};
-        for_each_cell<true, 32>(
+        for_each_cell<true>(
             a.grid, c.start, c.end, c.hmax, c.hmax_ref, c.ex[0], c.ex[1], x.pi.x, x.pi.y, x.pi.z, x.hi + x.hi, 0.0f,
             [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
-                for (uint32_t j = jb; j < je; ++j) {
+                for (uint32_t j = jb + lane; j < je; j += 32) {
                     if (j == i) continue;
                     force_term<kMorris>(a, x, j, shx, shy, shz, f);
                 }
-            },
-            lane);
+            });
         if (boundary_near(a.grid, b, x.pi.x, x.pi.y, x.pi.z, x.hi + x.hi)) boundary_forces<32>(a, b, i, x, f, lane);
 #pragma unroll
         for (int q = 0; q < 3; q++) {

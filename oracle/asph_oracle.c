@@ -148,8 +148,6 @@ typedef struct orc_iter {
     float sh[3];                /* its periodic image offset */
     int q;                      /* next sub-cell of the current reference cell, 0..8 */
     int empty;
-    int32_t ord;                /* ordinal of the current reference cell in the box (z, y, x order) */
-    int lanes, lane;            /* visit only ordinals with ord % lanes == lane */
 } orc_iter;
 
 static float clampf(float x, float lo, float hi)
@@ -198,18 +196,6 @@ static void it_init(orc_iter* it, const orc_grid* g, const uint32_t* start, cons
     it->r[1] = it->lo[1];
     it->r[2] = it->lo[2];
     it->q = 8;
-    it->ord = -1;
-    it->lanes = 1;
-    it->lane = 0;
-}
-
-/* the same box, dealing its reference cells round-robin to `lanes` lanes by ordinal; this is lane `lane` */
-static void it_init_lane(orc_iter* it, const orc_grid* g, const uint32_t* start, const uint32_t* end,
-                         const uint32_t ex[2], const float* p, float R, int lanes, int lane)
-{
-    it_init(it, g, start, end, ex, p, R);
-    it->lanes = lanes;
-    it->lane = lane;
 }
 
 /* number of reference cells in the box of p with radius R (the heavy-particle criterion) */
@@ -238,10 +224,6 @@ static int it_next_ref(orc_iter* it)
                     return 0;
                 }
             }
-        }
-        it->ord++;
-        if (it->lanes > 1 && it->ord % it->lanes != it->lane) {
-            continue;
         }
         int ok = 1;
         for (int a = 0; a < 3; a++) {

@@ -20,8 +20,9 @@
  *
  * Summation order: neighbours are summed in the canonical visiting order of the candidate cells. A particle
  * whose query box spans more than ORC_HEAVY_CELLS reference cells ("heavy", after merges made h large) is summed
- * as the GPU sums it with one warp: the box's reference cells are dealt round-robin to 32 lanes by ordinal,
- * each lane sums its cells in order, and the 32 partial sums are combined by the butterfly
+ * as the GPU sums it with one warp: in every visited sub-cell, member m (counted from the sub-cell's first member)
+ * goes to lane m mod 32, each lane sums its members in the canonical order, and the 32 partial sums are combined
+ * by the butterfly
  * s_l <- s_l + s_(l xor o) for o = 16, 8, 4, 2, 1. In the force pass a particle with more than ORC_MAXN accepted
  * neighbours (more than a neighbour-list row holds) is summed the same way.
  */
@@ -103,9 +104,9 @@ static REAL F(density_fluid)(const orc_grid* g, const orc_state* s, const orc_ce
     orc_iter it;
     uint32_t jb, je;
     float sh[3];
-    it_init_lane(&it, g, c->start, c->end, c->ex, pi, R, lanes, lane);
+    it_init(&it, g, c->start, c->end, c->ex, pi, R);
     while (it_next(&it, &jb, &je, sh)) {
-        for (uint32_t j = jb; j < je; j++) {
+        for (uint32_t j = jb + (uint32_t)lane; j < je; j += (uint32_t)lanes) {
             const float* pj = s->pos + 4 * (size_t)j;
             const REAL dx = NBR(pj, 0) - xi;
             const REAL dy = NBR(pj, 1) - yi;
@@ -143,9 +144,9 @@ static REAL F(density_boundary)(const orc_grid* g, const orc_state* s, const orc
     orc_iter it;
     uint32_t jb, je;
     float sh[3];
-    it_init_lane(&it, g, b->start, b->end, b->ex, pi, R, lanes, lane);
+    it_init(&it, g, b->start, b->end, b->ex, pi, R);
     while (it_next(&it, &jb, &je, sh)) {
-        for (uint32_t k = jb; k < je; k++) {
+        for (uint32_t k = jb + (uint32_t)lane; k < je; k += (uint32_t)lanes) {
             const float* pb = b->pos + 4 * (size_t)k;
             const REAL dx = NBR(pb, 0) - xi;
             const REAL dy = NBR(pb, 1) - yi;
@@ -214,9 +215,9 @@ static void F(forces_part)(const orc_grid* g, const orc_params* P, const orc_sta
     orc_iter it;
     uint32_t jb, je;
     float sh[3];
-    it_init_lane(&it, g, c->start, c->end, c->ex, pi, R, lanes, lane);
+    it_init(&it, g, c->start, c->end, c->ex, pi, R);
     while (it_next(&it, &jb, &je, sh)) {
-        for (uint32_t j = jb; j < je; j++) {
+        for (uint32_t j = jb + (uint32_t)lane; j < je; j += (uint32_t)lanes) {
             if ((int64_t)j == i) {
                 continue;
             }
@@ -293,9 +294,9 @@ static void F(forces_part)(const orc_grid* g, const orc_params* P, const orc_sta
         F(kernel_consts)(hi, &invh, &wc, &dwc);
         const REAL twoh = hi + hi;
         const REAL cut = twoh * twoh;
-        it_init_lane(&it, g, b->start, b->end, b->ex, pi, R, lanes, lane);
+        it_init(&it, g, b->start, b->end, b->ex, pi, R);
         while (it_next(&it, &jb, &je, sh)) {
-            for (uint32_t k = jb; k < je; k++) {
+            for (uint32_t k = jb + (uint32_t)lane; k < je; k += (uint32_t)lanes) {
                 const float* pb = b->pos + 4 * (size_t)k;
                 const REAL dx = xi - NBR(pb, 0);
                 const REAL dy = yi - NBR(pb, 1);
