@@ -177,6 +177,19 @@ __device__ __forceinline__ bool box_axis(const GridDev& g, int a, float p, float
     return l <= h;
 }
 
+// Number of reference cells in the query box [x - R, x + R].
+__device__ __forceinline__ int box_cells(const GridDev& g, float4 p, float R) {
+    int32_t lo, hi;
+    int n = 1;
+    const float pp[3] = {p.x, p.y, p.z};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        if (!box_axis(g, a, pp[a], R, lo, hi)) return 0;
+        n *= (hi - lo + 1);
+    }
+    return n;
+}
+
 // Wraps a (possibly out-of-range) cell index of a periodic grid into [0, n) and returns the image offset.
 __device__ __forceinline__ int32_t wrap_cell(int32_t c, int32_t n, float L, bool periodic, float& sh) {
     sh = 0.0f;

@@ -49,6 +49,8 @@ struct ReorderArgs {
     uint32_t* end;
     float* hmax;
     float* hmax_ref;
+    uint32_t* heavy;    // queue of heavy particles (query box > kHeavyCells reference cells)
+    uint32_t* heavy_n;
 };
 
 __global__ void k_integrate_keys(StepArgs a, float dt, float pending_half, int has_pending, uint32_t* keys,
@@ -64,11 +66,14 @@ __global__ void k_boundary_reorder(GridDev g, const float4* pos_in, const float*
                                    const uint32_t* keys_sorted, const uint32_t* vals_sorted, uint32_t n,
                                    float4* pos_out, float* fric_out, uint32_t* start, uint32_t* end,
                                    uint8_t* refflag);
-// density pass (ordinary particles, then the heavy ones) and force pass (neighbour_kernels.cu)
-cudaError_t launch_density(uint32_t blocks, uint32_t heavy_blocks, cudaStream_t stream, StepArgs a, CellsDev c,
-                           BoundaryDev b, NbrDev nl);
-cudaError_t launch_forces(bool morris, uint32_t blocks, uint32_t heavy_blocks, cudaStream_t stream, StepArgs a,
-                          CellsDev c, BoundaryDev b, NbrDev nl);
+// density and force passes (neighbour_kernels.cu): the ordinary kernel (one thread per particle) or the heavy
+// kernel (one warp per queued particle)
+cudaError_t launch_density(bool heavy, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c, BoundaryDev b,
+                           NbrDev nl);
+cudaError_t launch_forces(bool heavy, bool morris, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c,
+                          BoundaryDev b, NbrDev nl);
+// number of reference cells of the query box [x - R, x + R] above which a particle is heavy
+constexpr int kHeavyCells = 27;
 __global__ void k_neighbor_counts(StepArgs a, CellsDev c, uint32_t* counts, unsigned long long* total);
 __global__ void k_export(StepArgs a, float pending_half, int has_pending, float4* pos_out, float4* vel_out,
                          float* rho_out, float* rad_out, uint32_t* id_out);

@@ -24,7 +24,6 @@ constexpr uint32_t kIdxBits = 27;
 constexpr uint32_t kIdxMask = (1u << kIdxBits) - 1u;
 constexpr int kStage = 16;         // list entries staged per thread before a flush
 constexpr int kStageStride = 17;   // padded row (no bank conflicts between threads)
-constexpr int kHeavyCells = 27;    // more reference cells than this in the query box: heavy particle
 constexpr int32_t kMaxUnion = 64;  // a warp walks its lanes' boxes together when their union is at most this big
 
 // Periodic image of a listed neighbour: the index keeps 27 bits, the cell's image offset (-1, 0, +1 per axis)
@@ -49,19 +48,6 @@ __device__ __forceinline__ void decode_entry(const GridDev& g, uint32_t e, uint3
     shx = cx == 0 ? -g.scale[0] : (cx == 2 ? g.scale[0] : 0.0f);
     shy = cy == 0 ? -g.scale[1] : (cy == 2 ? g.scale[1] : 0.0f);
     shz = cz == 0 ? -g.scale[2] : (cz == 2 ? g.scale[2] : 0.0f);
-}
-
-// Number of reference cells in the query box [x - R, x + R].
-__device__ __forceinline__ int box_cells(const GridDev& g, float4 p, float R) {
-    int32_t lo, hi;
-    int n = 1;
-    const float pp[3] = {p.x, p.y, p.z};
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-        if (!box_axis(g, a, pp[a], R, lo, hi)) return 0;
-        n *= (hi - lo + 1);
-    }
-    return n;
 }
 
 __device__ __forceinline__ float warp_sum_butterfly(float v) {
@@ -309,9 +295,8 @@ __global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, Boun
     const float4 pi = in ? a.ph[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const float R = pi.w + pi.w;
     bool active = in;
-    if (in && box_cells(a.grid, pi, R) > kHeavyCells) {
+    if (in && box_cells(a.grid, pi, R) > kHeavyCells) {  // queued by the reorder kernel for k_density_heavy
         nl.cnt[i] = kHeavyMark;
-        nl.heavy[atomicAdd(nl.heavy_n, 1u)] = i;
         active = false;
     }
     const bool periodic = a.grid.periodic;
@@ -447,24 +432,29 @@ __global__ void __launch_bounds__(256, 1) k_forces_heavy(StepArgs a, CellsDev c,
     }
 }
 
-cudaError_t launch_density(uint32_t blocks, uint32_t heavy_blocks, cudaStream_t stream, StepArgs a, CellsDev c,
-                           BoundaryDev b, NbrDev nl) {
-    cudaError_t e = cudaMemsetAsync(nl.heavy_n, 0, sizeof(uint32_t), stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(nl.fheavy_n, 0, sizeof(uint32_t), stream);
-    if (e != cudaSuccess) return e;
-    k_density<<<blocks, 256, 0, stream>>>(a, c, b, nl);
-    k_density_heavy<<<heavy_blocks, 256, 0, stream>>>(a, c, b, nl);
+// The ordinary and the heavy kernels of a pass are independent of each other (the heavy queue is filled by the
+// reorder kernel, the overflow part of the force queue by k_density), so the host runs them on two streams.
+cudaError_t launch_density(bool heavy, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c, BoundaryDev b,
+                           NbrDev nl) {
+    if (heavy)
+        k_density_heavy<<<blocks, 256, 0, stream>>>(a, c, b, nl);
+    else
+        k_density<<<blocks, 256, 0, stream>>>(a, c, b, nl);
     return cudaGetLastError();
 }
 
-cudaError_t launch_forces(bool morris, uint32_t blocks, uint32_t heavy_blocks, cudaStream_t stream, StepArgs a,
-                          CellsDev c, BoundaryDev b, NbrDev nl) {
-    if (morris) {
-        k_forces<true><<<blocks, 256, 0, stream>>>(a, c, b, nl);
-        k_forces_heavy<true><<<heavy_blocks, 256, 0, stream>>>(a, c, b, nl);
+cudaError_t launch_forces(bool heavy, bool morris, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c,
+                          BoundaryDev b, NbrDev nl) {
+    if (heavy) {
+        if (morris)
+            k_forces_heavy<true><<<blocks, 256, 0, stream>>>(a, c, b, nl);
+        else
+            k_forces_heavy<false><<<blocks, 256, 0, stream>>>(a, c, b, nl);
     } else {
-        k_forces<false><<<blocks, 256, 0, stream>>>(a, c, b, nl);
-        k_forces_heavy<false><<<heavy_blocks, 256, 0, stream>>>(a, c, b, nl);
+        if (morris)
+            k_forces<true><<<blocks, 256, 0, stream>>>(a, c, b, nl);
+        else
+            k_forces<false><<<blocks, 256, 0, stream>>>(a, c, b, nl);
     }
     return cudaGetLastError();
 }

@@ -205,6 +205,8 @@ struct asph_simulation {
 
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;
+    cudaStream_t aux = nullptr;  // heavy-particle kernels, forked from and joined back into `stream`
+    cudaEvent_t ev_fork = nullptr, ev_main = nullptr, ev_aux = nullptr;
     uint64_t launches = 0;
 
     // timing
@@ -486,6 +488,7 @@ asph_status build_grid(asph_simulation* s, bool integrate, float dt, bool carry_
     CK(cudaMemsetAsync(s->cell_end, 0, sizeof(uint32_t) * s->grid.ncells, s->stream));
     CK(cudaMemsetAsync(s->cell_hmax, 0, sizeof(float) * s->grid.ncells, s->stream));
     CK(cudaMemsetAsync(s->hmax_ref, 0, sizeof(float) * s->refcells_alloc, s->stream));
+    CK(cudaMemsetAsync(s->heavy_n, 0, sizeof(uint32_t), s->stream));
     k_excluded<<<1, 1, 0, s->stream>>>(s->q3, nullptr, n, s->ex, s->grid.periodic);
     CK_LAUNCH("k_excluded");
     ReorderArgs r;
@@ -501,6 +504,8 @@ asph_status build_grid(asph_simulation* s, bool integrate, float dt, bool carry_
     r.end = s->cell_end;
     r.hmax = s->cell_hmax;
     r.hmax_ref = s->hmax_ref;
+    r.heavy = s->heavy_idx;
+    r.heavy_n = s->heavy_n;
     const int nxt = 1 - s->cur;
     StepArgs b = s->args(nxt);
     h = s->tic();
@@ -513,10 +518,23 @@ asph_status build_grid(asph_simulation* s, bool integrate, float dt, bool carry_
     return ASPH_OK;
 }
 
+// The ordinary kernel of each neighbour pass runs on the simulation's stream, the heavy-particle kernel on the
+// auxiliary stream, concurrently:
+//   main: k_density ------------(wait heavy density)-- k_forces ------------(wait heavy forces)--
+//   aux : (wait reorder) k_density_heavy -- (wait k_density) k_forces_heavy
+// The force kernels read the densities of all particles, hence the cross waits; the heavy force queue also holds
+// the particles whose neighbour rows overflowed in k_density.
 asph_status run_density(asph_simulation* s) {
     StepArgs a = s->args(s->cur);
     int h = s->tic();
-    CK(launch_density(blocks_for(s->n), kHeavyBlocks, s->stream, a, s->cells(), s->boundary(), s->nbrs()));
+    CK(cudaMemsetAsync(s->fheavy_n, 0, sizeof(uint32_t), s->stream));
+    CK(cudaEventRecord(s->ev_fork, s->stream));
+    CK(cudaStreamWaitEvent(s->aux, s->ev_fork, 0));
+    CK(launch_density(false, blocks_for(s->n), s->stream, a, s->cells(), s->boundary(), s->nbrs()));
+    CK(launch_density(true, kHeavyBlocks, s->aux, a, s->cells(), s->boundary(), s->nbrs()));
+    CK(cudaEventRecord(s->ev_main, s->stream));
+    CK(cudaEventRecord(s->ev_aux, s->aux));
+    CK(cudaStreamWaitEvent(s->stream, s->ev_aux, 0));
     s->toc(h, ASPH_KERNEL_DENSITY);
     s->launches += 2;
     return ASPH_OK;
@@ -525,10 +543,14 @@ asph_status run_density(asph_simulation* s) {
 asph_status run_forces(asph_simulation* s) {
     StepArgs a = s->args(s->cur);
     int h = s->tic();
-    CK(launch_forces(s->phys.morris != 0, blocks_for(s->n), kHeavyBlocks, s->stream, a, s->cells(), s->boundary(),
+    CK(cudaStreamWaitEvent(s->aux, s->ev_main, 0));
+    CK(launch_forces(false, s->phys.morris != 0, blocks_for(s->n), s->stream, a, s->cells(), s->boundary(),
                      s->nbrs()));
+    CK(launch_forces(true, s->phys.morris != 0, kHeavyBlocks, s->aux, a, s->cells(), s->boundary(), s->nbrs()));
+    CK(cudaEventRecord(s->ev_aux, s->aux));
+    CK(cudaStreamWaitEvent(s->stream, s->ev_aux, 0));
     s->toc(h, ASPH_KERNEL_FORCES);
-    s->launches++;
+    s->launches += 2;
     return ASPH_OK;
 }
 
@@ -770,6 +792,11 @@ void destroy(asph_simulation* s) {
         cudaEventDestroy(e.b);
     }
     for (auto e : s->event_pool) cudaEventDestroy(e);
+    if (s->aux) cudaStreamSynchronize(s->aux);
+    if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+    if (s->ev_main) cudaEventDestroy(s->ev_main);
+    if (s->ev_aux) cudaEventDestroy(s->ev_aux);
+    if (s->aux) cudaStreamDestroy(s->aux);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
     delete s;
     (void)cudaGetLastError();
@@ -957,6 +984,14 @@ asph_status asph_simulation_create(const asph_parameters* parameters, const floa
         return cuda_fail(e, "cudaStreamCreate");
     }
     s->stream = s->own_stream;
+    e = cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_main, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_aux, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        destroy(s);
+        return cuda_fail(e, "aux stream");
+    }
 #define TRY(x)                     \
     if ((st = (x)) != ASPH_OK) {   \
         destroy(s);                \
