@@ -305,32 +305,55 @@ __global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, Boun
     const uint32_t maxn = nl.maxn;
     uint32_t cnt = 0, staged = 0;
     float rho = 0.0f;
+    auto append = [&](uint32_t j, uint32_t code) {
+        if (cnt < maxn) {
+            st[staged++] = j | code;
+            if (staged == kStage) {
+                uint4* dst = reinterpret_cast<uint4*>(row + (cnt + 1 - kStage));
+#pragma unroll
+                for (int q = 0; q < kStage / 4; q++)
+                    dst[q] = make_uint4(st[4 * q], st[4 * q + 1], st[4 * q + 2], st[4 * q + 3]);
+                staged = 0;
+            }
+        }
+        cnt++;
+    };
+    // Two phases per block of up to 32 members: a cheap support test of every member builds the lane's acceptance
+    // mask, then the lane evaluates the kernel for its accepted members in order. The expensive part then runs once
+    // per member this lane accepts instead of once per member any lane accepts.
     auto scan = [&](uint32_t jb, uint32_t je, float shx, float shy, float shz, bool need) {
         if (!need) return;
         const uint32_t code = periodic ? (shift_code(shx, shy, shz) << kIdxBits) : 0u;
-        for (uint32_t j = jb; j < je; ++j) {
-            if (!density_term(a, pi, j, shx, shy, shz, rho)) continue;
-            if (cnt < maxn) {
-                st[staged++] = j | code;
-                if (staged == kStage) {
-                    uint4* dst = reinterpret_cast<uint4*>(row + (cnt + 1 - kStage));
-#pragma unroll
-                    for (int q = 0; q < kStage / 4; q++)
-                        dst[q] = make_uint4(st[4 * q], st[4 * q + 1], st[4 * q + 2], st[4 * q + 3]);
-                    staged = 0;
-                }
+        for (uint32_t c0 = jb; c0 < je; c0 += 32) {
+            const uint32_t cn = je - c0 < 32u ? je - c0 : 32u;
+            uint32_t mask = 0;
+            for (uint32_t k = 0; k < cn; ++k) {
+                const float4 pj = __ldg(a.ph + c0 + k);
+                const float xj = periodic ? pj.x + shx : pj.x;
+                const float yj = periodic ? pj.y + shy : pj.y;
+                const float zj = periodic ? pj.z + shz : pj.z;
+                const float dx = xj - pi.x, dy = yj - pi.y, dz = zj - pi.z;
+                const float r2 = dist2(dx, dy, dz);
+                const float twoh = pj.w + pj.w;
+                mask |= (r2 <= twoh * twoh ? 1u : 0u) << k;
             }
-            cnt++;
+            while (mask != 0u) {
+                const uint32_t k = (uint32_t)(__ffs(mask) - 1);
+                mask &= mask - 1u;
+                density_term(a, pi, c0 + k, shx, shy, shz, rho);
+                append(c0 + k, code);
+            }
         }
+    };
+    auto scan_plain = [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
+        const uint32_t code = periodic ? (shift_code(shx, shy, shz) << kIdxBits) : 0u;
+        for (uint32_t j = jb; j < je; ++j)
+            if (density_term(a, pi, j, shx, shy, shz, rho)) append(j, code);
     };
     // the warp's 32 particles are neighbours in the cell order: walk the union of their boxes together
     const bool together = for_each_cell_warp(a.grid, c.start, c.end, c.hmax, c.hmax_ref, c.ex[0], c.ex[1], active,
                                              pi.x, pi.y, pi.z, R, kMaxUnion, scan);
-    if (!together && active) {
-        fluid_candidates<true>(a, c, pi, [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
-            scan(jb, je, shx, shy, shz, true);
-        });
-    }
+    if (!together && active) fluid_candidates<true>(a, c, pi, scan_plain);
     if (!active) return;
     // remaining staged entries (fewer than a full segment)
     const uint32_t kept = cnt < maxn ? cnt : maxn;
