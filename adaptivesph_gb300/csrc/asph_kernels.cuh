@@ -20,20 +20,23 @@ struct StepArgs {
     uint32_t* err;
 };
 
-// Per-particle neighbour lists of the current step: row i holds the accepted neighbours of particle i in the
-// canonical candidate order, idx[i * maxn + k]. cnt[i] == kHeavyMark marks a particle whose query box spans more
-// than 27 reference cells: queued in heavy[0, *heavy_n) for the warp density kernel. Those particles and every
-// particle with more than maxn neighbours (cnt[i] > maxn, the row overflowed) are queued in fheavy for the warp
-// force kernel.
+// Per-particle neighbour lists of the current step. The candidate cells are scanned in blocks of up to 32
+// consecutive members of a sub-cell; row i holds one entry per block in which particle i accepted a neighbour:
+// {first member index | periodic image code << 27, acceptance mask}, in the canonical candidate order, at
+// ent[i * maxe + k]. Expanding the masks in order gives the accepted neighbours (self included) in canonical order.
+// cnt[i] == kHeavyMark marks a particle whose query box spans more than 27 reference cells: queued in
+// heavy[0, *heavy_n) for the warp density kernel. Those particles and every particle with more than maxe entries
+// (cnt[i] > maxe, the row overflowed) are queued in fheavy for the warp force kernel.
 constexpr uint32_t kHeavyMark = 0xffffffffu;
+constexpr uint32_t kListEntries = 64;  // entries per row
 struct NbrDev {
-    uint32_t* idx;
+    uint2* ent;
     uint32_t* cnt;
     uint32_t* heavy;
     uint32_t* heavy_n;
     uint32_t* fheavy;
     uint32_t* fheavy_n;
-    uint32_t maxn;
+    uint32_t maxe;
 };
 
 struct ReorderArgs {

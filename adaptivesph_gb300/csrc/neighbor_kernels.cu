@@ -7,10 +7,12 @@
 // Ordinary particles: one thread per particle. In the density pass the 32 particles of a warp (neighbours in the
 // cell order) walk the union of their candidate cells together in the canonical order, each lane testing every
 // candidate of its own cells (shared loads, no divergent loop control); each lane sums its density in its own
-// canonical order and records its accepted neighbours (self included) in its row of the neighbour list. Rows are
-// staged in shared memory and flushed 16 entries (64 bytes) at a time. The force pass walks the row.
+// canonical order and records its accepted neighbours (self included) in its row of the neighbour list. A row entry
+// covers one block of up to 32 consecutive members of a sub-cell: (first member | periodic image code, 32-bit
+// acceptance mask), 8 bytes, written only for blocks holding an accepted neighbour. Entries are staged in shared
+// memory and flushed 8 at a time (64 bytes). The force pass expands each mask in member order.
 // Heavy particles (query box of more than 27 reference cells: smoothing lengths grown by merging) and, in the force
-// pass, particles with more neighbours than a row holds: one warp per particle; in every visited sub-cell member m
+// pass, particles with more entries than a row holds: one warp per particle; in every visited sub-cell member m
 // goes to lane m mod 32, lane sums are combined by a fixed butterfly. The density pass queues them for separate
 // warp kernels, so a few large boxes do not stall whole blocks.
 #include "asph_device.cuh"
@@ -22,8 +24,8 @@ namespace {
 
 constexpr uint32_t kIdxBits = 27;
 constexpr uint32_t kIdxMask = (1u << kIdxBits) - 1u;
-constexpr int kStage = 16;         // list entries staged per thread before a flush
-constexpr int kStageStride = 17;   // padded row (no bank conflicts between threads)
+constexpr int kStage = 8;          // list entries (8 bytes each) staged per thread before a 64-byte flush
+constexpr int kStageStride = 9;    // padded staging row
 constexpr int32_t kMaxUnion = 64;  // a warp walks its lanes' boxes together when their union is at most this big
 
 // Periodic image of a listed neighbour: the index keeps 27 bits, the cell's image offset (-1, 0, +1 per axis)
@@ -289,7 +291,7 @@ __device__ __forceinline__ void fluid_candidates(const StepArgs& a, const CellsD
 
 // Density pass, ordinary particles; heavy particles are queued for k_density_heavy.
 __global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
-    __shared__ uint32_t stage[256 * kStageStride];
+    __shared__ uint2 stage[256 * kStageStride];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool in = i < a.n;
     const float4 pi = in ? a.ph[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -300,66 +302,65 @@ __global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, Boun
         active = false;
     }
     const bool periodic = a.grid.periodic;
-    uint32_t* row = nl.idx + (size_t)(in ? i : 0) * nl.maxn;
-    uint32_t* st = stage + threadIdx.x * kStageStride;
-    const uint32_t maxn = nl.maxn;
+    uint2* row = nl.ent + (size_t)(in ? i : 0) * nl.maxe;
+    uint2* st = stage + threadIdx.x * kStageStride;
+    const uint32_t maxe = nl.maxe;
     uint32_t cnt = 0, staged = 0;
     float rho = 0.0f;
-    auto append = [&](uint32_t j, uint32_t code) {
-        if (cnt < maxn) {
-            st[staged++] = j | code;
+    auto append = [&](uint32_t first, uint32_t mask) {
+        if (cnt < maxe) {
+            st[staged++] = make_uint2(first, mask);
             if (staged == kStage) {
                 uint4* dst = reinterpret_cast<uint4*>(row + (cnt + 1 - kStage));
 #pragma unroll
-                for (int q = 0; q < kStage / 4; q++)
-                    dst[q] = make_uint4(st[4 * q], st[4 * q + 1], st[4 * q + 2], st[4 * q + 3]);
+                for (int q = 0; q < kStage / 2; q++)
+                    dst[q] = make_uint4(st[2 * q].x, st[2 * q].y, st[2 * q + 1].x, st[2 * q + 1].y);
                 staged = 0;
             }
         }
         cnt++;
     };
-    // Two phases per block of up to 32 members: a cheap support test of every member builds the lane's acceptance
-    // mask, then the lane evaluates the kernel for its accepted members in order. The expensive part then runs once
-    // per member this lane accepts instead of once per member any lane accepts.
+    // Per block of up to 32 members of a sub-cell: a cheap support test of every member builds the lane's
+    // acceptance mask; the lane then evaluates the kernel for its accepted members in order and records the block
+    // (first member, mask) in its list row.
+    auto scan_block = [&](uint32_t c0, uint32_t cn, uint32_t code, float shx, float shy, float shz) {
+        uint32_t mask = 0;
+        for (uint32_t k = 0; k < cn; ++k) {
+            const float4 pj = __ldg(a.ph + c0 + k);
+            const float xj = periodic ? pj.x + shx : pj.x;
+            const float yj = periodic ? pj.y + shy : pj.y;
+            const float zj = periodic ? pj.z + shz : pj.z;
+            const float dx = xj - pi.x, dy = yj - pi.y, dz = zj - pi.z;
+            const float r2 = dist2(dx, dy, dz);
+            const float twoh = pj.w + pj.w;
+            mask |= (r2 <= twoh * twoh ? 1u : 0u) << k;
+        }
+        if (mask == 0u) return;
+        append(c0 | code, mask);
+        while (mask != 0u) {
+            const uint32_t k = (uint32_t)(__ffs(mask) - 1);
+            mask &= mask - 1u;
+            density_term(a, pi, c0 + k, shx, shy, shz, rho);
+        }
+    };
     auto scan = [&](uint32_t jb, uint32_t je, float shx, float shy, float shz, bool need) {
         if (!need) return;
         const uint32_t code = periodic ? (shift_code(shx, shy, shz) << kIdxBits) : 0u;
-        for (uint32_t c0 = jb; c0 < je; c0 += 32) {
-            const uint32_t cn = je - c0 < 32u ? je - c0 : 32u;
-            uint32_t mask = 0;
-            for (uint32_t k = 0; k < cn; ++k) {
-                const float4 pj = __ldg(a.ph + c0 + k);
-                const float xj = periodic ? pj.x + shx : pj.x;
-                const float yj = periodic ? pj.y + shy : pj.y;
-                const float zj = periodic ? pj.z + shz : pj.z;
-                const float dx = xj - pi.x, dy = yj - pi.y, dz = zj - pi.z;
-                const float r2 = dist2(dx, dy, dz);
-                const float twoh = pj.w + pj.w;
-                mask |= (r2 <= twoh * twoh ? 1u : 0u) << k;
-            }
-            while (mask != 0u) {
-                const uint32_t k = (uint32_t)(__ffs(mask) - 1);
-                mask &= mask - 1u;
-                density_term(a, pi, c0 + k, shx, shy, shz, rho);
-                append(c0 + k, code);
-            }
-        }
-    };
-    auto scan_plain = [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
-        const uint32_t code = periodic ? (shift_code(shx, shy, shz) << kIdxBits) : 0u;
-        for (uint32_t j = jb; j < je; ++j)
-            if (density_term(a, pi, j, shx, shy, shz, rho)) append(j, code);
+        for (uint32_t c0 = jb; c0 < je; c0 += 32) scan_block(c0, je - c0 < 32u ? je - c0 : 32u, code, shx, shy, shz);
     };
     // the warp's 32 particles are neighbours in the cell order: walk the union of their boxes together
     const bool together = for_each_cell_warp(a.grid, c.start, c.end, c.hmax, c.hmax_ref, c.ex[0], c.ex[1], active,
                                              pi.x, pi.y, pi.z, R, kMaxUnion, scan);
-    if (!together && active) fluid_candidates<true>(a, c, pi, scan_plain);
+    if (!together && active)
+        fluid_candidates<true>(a, c, pi, [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
+            scan(jb, je, shx, shy, shz, true);
+        });
     if (!active) return;
     // remaining staged entries (fewer than a full segment)
-    const uint32_t kept = cnt < maxn ? cnt : maxn;
+    const uint32_t kept = cnt < maxe ? cnt : maxe;
     for (uint32_t q = 0; q < staged; ++q) row[kept - staged + q] = st[q];
     nl.cnt[i] = cnt;
-    if (cnt > maxn) nl.fheavy[atomicAdd(nl.fheavy_n, 1u)] = i;  // too many neighbours for a row: warp force pass
+    if (cnt > maxe) nl.fheavy[atomicAdd(nl.fheavy_n, 1u)] = i;  // row overflowed: warp force pass
     float rb = 0.0f;
     if (boundary_near(a.grid, b, pi.x, pi.y, pi.z, R)) rb = boundary_density<1>(a, b, i, pi, 0);
     const float rh = rho + rb;
@@ -402,21 +403,25 @@ __global__ void __launch_bounds__(256, 3) k_forces(StepArgs a, CellsDev c, Bound
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     const uint32_t cnt = nl.cnt[i];
-    if (cnt > nl.maxn) return;  // heavy or overflowed: k_forces_heavy
+    if (cnt > nl.maxe) return;  // heavy or overflowed: k_forces_heavy
     const ForceCtx x = force_ctx(a, i);
     ForceAcc f = {};
-    const uint4* row = reinterpret_cast<const uint4*>(nl.idx + (size_t)i * nl.maxn);
-    for (uint32_t k = 0; k < cnt; k += 4) {
-        const uint4 e4 = __ldg(row + (k >> 2));
-        const uint32_t e[4] = {e4.x, e4.y, e4.z, e4.w};
+    const uint4* row = reinterpret_cast<const uint4*>(nl.ent + (size_t)i * nl.maxe);
+    for (uint32_t k = 0; k < cnt; k += 2) {
+        const uint4 e2 = __ldg(row + (k >> 1));
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
+        for (int q = 0; q < 2; q++) {
             if (k + q >= cnt) break;
-            uint32_t j;
+            uint32_t first;
             float shx, shy, shz;
-            decode_entry(a.grid, e[q], j, shx, shy, shz);
-            if (j == i) continue;
-            force_term<kMorris>(a, x, j, shx, shy, shz, f);
+            decode_entry(a.grid, q == 0 ? e2.x : e2.z, first, shx, shy, shz);
+            uint32_t mask = q == 0 ? e2.y : e2.w;
+            while (mask != 0u) {
+                const uint32_t j = first + (uint32_t)(__ffs(mask) - 1);
+                mask &= mask - 1u;
+                if (j == i) continue;
+                force_term<kMorris>(a, x, j, shx, shy, shz, f);
+            }
         }
     }
     if (boundary_near(a.grid, b, x.pi.x, x.pi.y, x.pi.z, x.hi + x.hi)) boundary_forces<1>(a, b, i, x, f, 0);

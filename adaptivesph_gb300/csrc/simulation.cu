@@ -138,13 +138,12 @@ struct asph_simulation {
     BufferSet set[2];
     int cur = 0;
     float4* kc = nullptr;
-    uint32_t* nbr_idx = nullptr;  // [maxn * cap] neighbour lists, one column per particle
+    uint2* nbr_ent = nullptr;     // [kListEntries * cap] neighbour lists, one row per particle
     uint32_t* nbr_cnt = nullptr;  // [cap]
     uint32_t* heavy_idx = nullptr;  // [cap] queue of heavy particles of the current step
     uint32_t* heavy_n = nullptr;
     uint32_t* fheavy_idx = nullptr;  // [cap] queue of the force pass's warp kernel
     uint32_t* fheavy_n = nullptr;
-    uint32_t maxn = 256;
     uint32_t* keys = nullptr;
     uint32_t* vals = nullptr;
     void* sort_mem = nullptr;
@@ -238,7 +237,7 @@ struct asph_simulation {
 
     CellsDev cells() const { return CellsDev{cell_start, cell_end, cell_hmax, hmax_ref, ex}; }
 
-    NbrDev nbrs() const { return NbrDev{nbr_idx, nbr_cnt, heavy_idx, heavy_n, fheavy_idx, fheavy_n, maxn}; }
+    NbrDev nbrs() const { return NbrDev{nbr_ent, nbr_cnt, heavy_idx, heavy_n, fheavy_idx, fheavy_n, kListEntries}; }
 
     BoundaryDev boundary() const {
         return BoundaryDev{bpos, bfric, bstart, bend, brefflag, bex[0], bex[1], nb};
@@ -754,7 +753,7 @@ void destroy(asph_simulation* s) {
         dfree(s->set[k].id);
     }
     dfree(s->kc);
-    dfree(s->nbr_idx);
+    dfree(s->nbr_ent);
     dfree(s->nbr_cnt);
     dfree(s->heavy_idx);
     dfree(s->heavy_n);
@@ -1007,7 +1006,7 @@ asph_status asph_simulation_create(const asph_parameters* parameters, const floa
         TRY(dalloc(s->set[k].id, C));
     }
     TRY(dalloc(s->kc, C));
-    TRY(dalloc(s->nbr_idx, (size_t)s->maxn * C));
+    TRY(dalloc(s->nbr_ent, (size_t)kListEntries * C));
     TRY(dalloc(s->nbr_cnt, C));
     TRY(dalloc(s->heavy_idx, C));
     TRY(dalloc(s->heavy_n, 1));

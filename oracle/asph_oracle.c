@@ -467,30 +467,37 @@ float orc_cbrtf(float xf)
 static const float ORC_PI_F = 3.141592653589793f;
 #define ORC_LANES 32       /* lanes of the warp that sums a heavy particle */
 #define ORC_HEAVY_CELLS 27 /* query boxes of more reference cells than this are heavy */
-#define ORC_MAXN 256       /* neighbour-list row length; a particle with more neighbours is heavy in the force pass */
+#define ORC_LIST_ENTRIES 64 /* neighbour-list row length in entries; a particle needing more is heavy in the force pass */
 
-/* neighbours accepted by the density pass (self included): r^2 <= (2 h_j)^2 over the candidate cells */
-static uint32_t accepted_count(const orc_grid* g, const orc_state* s, const orc_cells* c, int64_t i)
+/* Entries of the particle's neighbour-list row: the candidate cells' members are scanned in blocks of up to 32
+ * (counted from each sub-cell's first member); a block in which the particle accepts a neighbour
+ * (r^2 <= (2 h_j)^2, self included) is one entry. */
+static uint32_t list_entries(const orc_grid* g, const orc_state* s, const orc_cells* c, int64_t i)
 {
     const float* pi = s->pos + 4 * i;
     const float R = s->h[i] + s->h[i];
-    uint32_t cnt = 0;
+    uint32_t entries = 0;
     orc_iter it;
     uint32_t jb, je;
     float sh[3];
     it_init(&it, g, c->start, c->end, c->ex, pi, R);
     while (it_next(&it, &jb, &je, sh)) {
-        for (uint32_t j = jb; j < je; j++) {
-            const float* pj = s->pos + 4 * (size_t)j;
-            const float dx = (g->periodic ? pj[0] + sh[0] : pj[0]) - pi[0];
-            const float dy = (g->periodic ? pj[1] + sh[1] : pj[1]) - pi[1];
-            const float dz = (g->periodic ? pj[2] + sh[2] : pj[2]) - pi[2];
-            const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-            const float twoh = s->h[j] + s->h[j];
-            cnt += r2 <= twoh * twoh;
+        for (uint32_t c0 = jb; c0 < je; c0 += 32) {
+            const uint32_t c1 = je - c0 < 32u ? je : c0 + 32u;
+            int any = 0;
+            for (uint32_t j = c0; j < c1 && !any; j++) {
+                const float* pj = s->pos + 4 * (size_t)j;
+                const float dx = (g->periodic ? pj[0] + sh[0] : pj[0]) - pi[0];
+                const float dy = (g->periodic ? pj[1] + sh[1] : pj[1]) - pi[1];
+                const float dz = (g->periodic ? pj[2] + sh[2] : pj[2]) - pi[2];
+                const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                const float twoh = s->h[j] + s->h[j];
+                any = r2 <= twoh * twoh;
+            }
+            entries += any;
         }
     }
-    return cnt;
+    return entries;
 }
 
 #define REAL float
@@ -1272,4 +1279,14 @@ uint32_t orc_boundary_generate(const float dmin[3], const float dmax[3], float s
     free(cid);
     free(tmp);
     return (uint32_t)n;
+}
+
+/* per-particle neighbour-list row entries (see list_entries); for tests */
+void orc_list_entries(const orc_grid* g, const orc_state* s, const orc_cells* c, uint32_t* out)
+{
+    const int64_t n = s->n;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < n; i++) {
+        out[i] = list_entries(g, s, c, i);
+    }
 }
