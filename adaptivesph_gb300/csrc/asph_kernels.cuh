@@ -25,8 +25,9 @@ struct StepArgs {
 // {first member index | periodic image code << 27, acceptance mask}, in the canonical candidate order, at
 // ent[i * maxe + k]. Expanding the masks in order gives the accepted neighbours (self included) in canonical order.
 // cnt[i] == kHeavyMark marks a particle whose query box spans more than 27 reference cells: queued in
-// heavy[0, *heavy_n) for the warp density kernel. Those particles and every particle with more than maxe entries
-// (cnt[i] > maxe, the row overflowed) are queued in fheavy for the warp force kernel.
+// heavy[0, *heavy_n) by the reorder kernel for the warp density kernel. A particle with more than maxe entries
+// (cnt[i] > maxe, the row overflowed) is queued in dover[0, *dover_n) by the density pass and its density summed by
+// the warp density kernel too. Both kinds are queued in fheavy for the warp force kernel.
 constexpr uint32_t kHeavyMark = 0xffffffffu;
 constexpr uint32_t kListEntries = 64;  // entries per row
 struct NbrDev {
@@ -36,6 +37,8 @@ struct NbrDev {
     uint32_t* heavy_n;
     uint32_t* fheavy;
     uint32_t* fheavy_n;
+    uint32_t* dover;
+    uint32_t* dover_n;
     uint32_t maxe;
 };
 
@@ -70,9 +73,10 @@ __global__ void k_boundary_reorder(GridDev g, const float4* pos_in, const float*
                                    float4* pos_out, float* fric_out, uint32_t* start, uint32_t* end,
                                    uint8_t* refflag);
 // density and force passes (neighbour_kernels.cu): the ordinary kernel (one thread per particle) or the heavy
-// kernel (one warp per queued particle)
-cudaError_t launch_density(bool heavy, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c, BoundaryDev b,
-                           NbrDev nl);
+// kernel (one warp per queued particle; for the density pass, over the box-heavy queue or the overflow queue)
+enum DensityKernel { kDensityOrdinary, kDensityHeavy, kDensityOverflow };
+cudaError_t launch_density(DensityKernel kind, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c,
+                           BoundaryDev b, NbrDev nl);
 cudaError_t launch_forces(bool heavy, bool morris, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c,
                           BoundaryDev b, NbrDev nl);
 // number of reference cells of the query box [x - R, x + R] above which a particle is heavy

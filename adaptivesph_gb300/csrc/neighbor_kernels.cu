@@ -6,15 +6,16 @@
 //
 // Ordinary particles: one thread per particle. In the density pass the 32 particles of a warp (neighbours in the
 // cell order) walk the union of their candidate cells together in the canonical order, each lane testing every
-// candidate of its own cells (shared loads, no divergent loop control); each lane sums its density in its own
-// canonical order and records its accepted neighbours (self included) in its row of the neighbour list. A row entry
-// covers one block of up to 32 consecutive members of a sub-cell: (first member | periodic image code, 32-bit
-// acceptance mask), 8 bytes, written only for blocks holding an accepted neighbour. Entries are staged in shared
-// memory and flushed 8 at a time (64 bytes). The force pass expands each mask in member order.
-// Heavy particles (query box of more than 27 reference cells: smoothing lengths grown by merging) and, in the force
-// pass, particles with more entries than a row holds: one warp per particle; in every visited sub-cell member m
-// goes to lane m mod 32, lane sums are combined by a fixed butterfly. The density pass queues them for separate
-// warp kernels, so a few large boxes do not stall whole blocks.
+// candidate of its own cells (shared loads, no divergent loop control) and recording its accepted neighbours (self
+// included) in its row of the neighbour list. A row entry covers one block of up to 32 consecutive members of a
+// sub-cell: (first member | periodic image code, 32-bit acceptance mask), 8 bytes, written only for blocks holding
+// an accepted neighbour. Entries are staged in shared memory and flushed 8 at a time (64 bytes). Each lane then sums
+// its density over its row, and the force pass sums over the same row: the masks expanded in member order give the
+// accepted neighbours in the canonical order, one per loop iteration.
+// Heavy particles (query box of more than 27 reference cells: smoothing lengths grown by merging) and particles
+// with more entries than a row holds: one warp per particle; in every visited sub-cell member m goes to lane
+// m mod 32, lane sums are combined by a fixed butterfly. They are queued for separate warp kernels, so a few large
+// boxes do not stall whole blocks.
 #include "asph_device.cuh"
 #include "asph_kernels.cuh"
 
@@ -320,9 +321,9 @@ __global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, Boun
         }
         cnt++;
     };
-    // Per block of up to 32 members of a sub-cell: a cheap support test of every member builds the lane's
-    // acceptance mask; the lane then evaluates the kernel for its accepted members in order and records the block
-    // (first member, mask) in its list row.
+    // Per block of up to 32 members of a sub-cell: a support test of every member builds the lane's acceptance
+    // mask, and the block (first member, mask) goes to the lane's list row. The kernel sums are formed afterwards
+    // from the row, one accepted neighbour per iteration.
     auto scan_block = [&](uint32_t c0, uint32_t cn, uint32_t code, float shx, float shy, float shz) {
         uint32_t mask = 0;
         for (uint32_t k = 0; k < cn; ++k) {
@@ -335,13 +336,7 @@ __global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, Boun
             const float twoh = pj.w + pj.w;
             mask |= (r2 <= twoh * twoh ? 1u : 0u) << k;
         }
-        if (mask == 0u) return;
-        append(c0 | code, mask);
-        while (mask != 0u) {
-            const uint32_t k = (uint32_t)(__ffs(mask) - 1);
-            mask &= mask - 1u;
-            density_term(a, pi, c0 + k, shx, shy, shz, rho);
-        }
+        if (mask != 0u) append(c0 | code, mask);
     };
     auto scan = [&](uint32_t jb, uint32_t je, float shx, float shy, float shz, bool need) {
         if (!need) return;
@@ -356,11 +351,31 @@ __global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, Boun
             scan(jb, je, shx, shy, shz, true);
         });
     if (!active) return;
-    // remaining staged entries (fewer than a full segment)
-    const uint32_t kept = cnt < maxe ? cnt : maxe;
-    for (uint32_t q = 0; q < staged; ++q) row[kept - staged + q] = st[q];
     nl.cnt[i] = cnt;
-    if (cnt > maxe) nl.fheavy[atomicAdd(nl.fheavy_n, 1u)] = i;  // row overflowed: warp force pass
+    if (cnt > maxe) {  // row overflowed: density and forces by the warp kernels
+        nl.dover[atomicAdd(nl.dover_n, 1u)] = i;
+        return;
+    }
+    // remaining staged entries (fewer than a full segment)
+    for (uint32_t q = 0; q < staged; ++q) row[cnt - staged + q] = st[q];
+    // the fluid sum over the row in canonical order (plain loads: the row was written by this thread)
+    {
+        uint2 next = cnt > 0u ? row[0] : make_uint2(0u, 0u);
+        uint32_t k = 1, first = 0, mask = 0;
+        float shx = 0.0f, shy = 0.0f, shz = 0.0f;
+        for (;;) {
+            if (mask == 0u) {
+                if (k > cnt) break;
+                decode_entry(a.grid, next.x, first, shx, shy, shz);
+                mask = next.y;
+                if (k < cnt) next = row[k];
+                k++;
+            }
+            const uint32_t j = first + (uint32_t)(__ffs(mask) - 1);
+            mask &= mask - 1u;
+            density_term(a, pi, j, shx, shy, shz, rho);
+        }
+    }
     float rb = 0.0f;
     if (boundary_near(a.grid, b, pi.x, pi.y, pi.z, R)) rb = boundary_density<1>(a, b, i, pi, 0);
     const float rh = rho + rb;
@@ -369,13 +384,14 @@ __global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, Boun
 }
 
 // Density of the heavy particles: one warp per particle.
-__global__ void __launch_bounds__(256, 1) k_density_heavy(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
+__global__ void __launch_bounds__(256, 1) k_density_heavy(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl,
+                                                          const uint32_t* queue, const uint32_t* queue_n) {
     const int lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t nh = *nl.heavy_n;
+    const uint32_t nh = *queue_n;
     for (uint32_t w = warp; w < nh; w += nwarps) {
-        const uint32_t i = nl.heavy[w];
+        const uint32_t i = queue[w];
         const float4 pi = a.ph[i];
         const float R = pi.w + pi.w;
         float rho = 0.0f;
@@ -406,23 +422,23 @@ __global__ void __launch_bounds__(256, 3) k_forces(StepArgs a, CellsDev c, Bound
     if (cnt > nl.maxe) return;  // heavy or overflowed: k_forces_heavy
     const ForceCtx x = force_ctx(a, i);
     ForceAcc f = {};
-    const uint4* row = reinterpret_cast<const uint4*>(nl.ent + (size_t)i * nl.maxe);
-    for (uint32_t k = 0; k < cnt; k += 2) {
-        const uint4 e2 = __ldg(row + (k >> 1));
-#pragma unroll
-        for (int q = 0; q < 2; q++) {
-            if (k + q >= cnt) break;
-            uint32_t first;
-            float shx, shy, shz;
-            decode_entry(a.grid, q == 0 ? e2.x : e2.z, first, shx, shy, shz);
-            uint32_t mask = q == 0 ? e2.y : e2.w;
-            while (mask != 0u) {
-                const uint32_t j = first + (uint32_t)(__ffs(mask) - 1);
-                mask &= mask - 1u;
-                if (j == i) continue;
-                force_term<kMorris>(a, x, j, shx, shy, shz, f);
-            }
+    // One neighbour per iteration (the row's masks expanded in order), so a warp runs as many iterations as its
+    // lane with the most neighbours; the next entry is fetched as soon as the current one is decoded.
+    const uint2* row = nl.ent + (size_t)i * nl.maxe;
+    uint2 next = cnt > 0u ? __ldg(row) : make_uint2(0u, 0u);
+    uint32_t k = 1, first = 0, mask = 0;
+    float shx = 0.0f, shy = 0.0f, shz = 0.0f;
+    for (;;) {
+        if (mask == 0u) {
+            if (k > cnt) break;
+            decode_entry(a.grid, next.x, first, shx, shy, shz);
+            mask = next.y;
+            if (k < cnt) next = __ldg(row + k);
+            k++;
         }
+        const uint32_t j = first + (uint32_t)(__ffs(mask) - 1);
+        mask &= mask - 1u;
+        if (j != i) force_term<kMorris>(a, x, j, shx, shy, shz, f);
     }
     if (boundary_near(a.grid, b, x.pi.x, x.pi.y, x.pi.z, x.hi + x.hi)) boundary_forces<1>(a, b, i, x, f, 0);
     finish_force(a, i, x, f);
@@ -460,12 +476,15 @@ __global__ void __launch_bounds__(256, 1) k_forces_heavy(StepArgs a, CellsDev c,
     }
 }
 
-// The ordinary and the heavy kernels of a pass are independent of each other (the heavy queue is filled by the
-// reorder kernel, the overflow part of the force queue by k_density), so the host runs them on two streams.
-cudaError_t launch_density(bool heavy, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c, BoundaryDev b,
-                           NbrDev nl) {
-    if (heavy)
-        k_density_heavy<<<blocks, 256, 0, stream>>>(a, c, b, nl);
+// The ordinary and the box-heavy kernels of a pass are independent of each other (the heavy queue is filled by the
+// reorder kernel), so the host runs them on two streams; the overflow queue is filled by k_density and summed
+// after it on its stream.
+cudaError_t launch_density(DensityKernel kind, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c,
+                           BoundaryDev b, NbrDev nl) {
+    if (kind == kDensityHeavy)
+        k_density_heavy<<<blocks, 256, 0, stream>>>(a, c, b, nl, nl.heavy, nl.heavy_n);
+    else if (kind == kDensityOverflow)
+        k_density_heavy<<<blocks, 256, 0, stream>>>(a, c, b, nl, nl.dover, nl.dover_n);
     else
         k_density<<<blocks, 256, 0, stream>>>(a, c, b, nl);
     return cudaGetLastError();

@@ -467,7 +467,7 @@ float orc_cbrtf(float xf)
 static const float ORC_PI_F = 3.141592653589793f;
 #define ORC_LANES 32       /* lanes of the warp that sums a heavy particle */
 #define ORC_HEAVY_CELLS 27 /* query boxes of more reference cells than this are heavy */
-#define ORC_LIST_ENTRIES 64 /* neighbour-list row length in entries; a particle needing more is heavy in the force pass */
+#define ORC_LIST_ENTRIES 64 /* neighbour-list row length in entries; a particle needing more is heavy */
 
 /* Entries of the particle's neighbour-list row: the candidate cells' members are scanned in blocks of up to 32
  * (counted from each sub-cell's first member); a block in which the particle accepts a neighbour

@@ -23,8 +23,8 @@
  * as the GPU sums it with one warp: in every visited sub-cell, member m (counted from the sub-cell's first member)
  * goes to lane m mod 32, each lane sums its members in the canonical order, and the 32 partial sums are combined
  * by the butterfly
- * s_l <- s_l + s_(l xor o) for o = 16, 8, 4, 2, 1. In the force pass a particle whose neighbour-list row would need
- * more than ORC_LIST_ENTRIES entries (see list_entries) is summed the same way.
+ * s_l <- s_l + s_(l xor o) for o = 16, 8, 4, 2, 1. A particle whose neighbour-list row would need more than
+ * ORC_LIST_ENTRIES entries (see list_entries) is summed the same way, in both passes.
  */
 
 /* W(r, h) with precomputed 1/h and coef/h^3 */
@@ -171,7 +171,7 @@ void F(orc_density_impl)(const orc_grid* g, const orc_params* P, const orc_state
     for (int64_t i = 0; i < n; i++) {
         const float R = s->h[i] + s->h[i];
         REAL rho, rb;
-        if (box_cells(g, s->pos + 4 * i, R) > ORC_HEAVY_CELLS) {
+        if (box_cells(g, s->pos + 4 * i, R) > ORC_HEAVY_CELLS || list_entries(g, s, c, i) > ORC_LIST_ENTRIES) {
             REAL pf[ORC_LANES], pb[ORC_LANES];
             for (int l = 0; l < ORC_LANES; l++) {
                 pf[l] = F(density_fluid)(g, s, c, i, ORC_LANES, l);
