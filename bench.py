@@ -162,6 +162,8 @@ def run_ours(args, rank: int, world: int, dist):
     torch.cuda.set_device(dev)
     sc, bd = build_scene()
     n0 = sc.positions.shape[0]
+    if args.capacity:
+        sc.refinement.max_particle_count = args.capacity
     cap = sc.refinement.max_particle_count
     stream = torch.cuda.Stream()
 
@@ -354,6 +356,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=10)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--capacity", type=int, default=0,
+                    help="particle capacity (default: the workload's 4M); a smaller one keeps profiling runs small")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
