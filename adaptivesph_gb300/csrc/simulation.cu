@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -1581,5 +1582,110 @@ extern "C" asph_status asph_debug_refinement_ids(asph_simulation* sim, uint32_t*
     if (keep && np) CK(cudaMemcpy(keep, sim->dbg_ids, 4 * (size_t)np, cudaMemcpyDeviceToHost));
     if (removed && np) CK(cudaMemcpy(removed, sim->dbg_ids + sim->cap, 4 * (size_t)np, cudaMemcpyDeviceToHost));
     if (split && ns) CK(cudaMemcpy(split, sim->dbg_ids + 2 * (size_t)sim->cap, 4 * (size_t)ns, cudaMemcpyDeviceToHost));
+    return ASPH_OK;
+}
+
+// ------------------------------------------------------------------------------------------------ no-alloc sort
+// asph_grid_sort_noalloc: the cell-key sort with its scratch in one fixed device array instead of cudaMalloc.
+// Callers that cannot allocate: hosts that own all device memory through their own allocator (a renderer that
+// imports its particle buffers under a fixed budget) and frame loops in which cudaMalloc/cudaFree would stall
+// other streams (cudaFree synchronises the device) or could fail mid-frame. Nothing here allocates: no
+// cudaMalloc/cudaFree, no allocating library. The scratch is shared by every call on a device, so calls that
+// may overlap race on it; the caller serialises them.
+
+namespace {
+constexpr uint32_t kNoAllocMax = ASPH_NOALLOC_MAX_PARTICLES;
+constexpr size_t kNoAllocTiles = (kNoAllocMax + kSortTile - 1) / kSortTile + 1;
+// the layout of sort_scratch_bytes(kNoAllocMax): ping-pong keys and values, digit counts, tile counters, look-back
+constexpr size_t kNoAllocSortBytes =
+    sizeof(uint32_t) * ((size_t)2 * kNoAllocMax + 4 * 256 + 4 + (size_t)4 * kNoAllocTiles * 256) + 256;
+constexpr size_t kNoAllocHead = 256;  // word 0: the particle count read by the sort kernels
+constexpr int kNoAllocMaxDevices = 64;
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocHead + kNoAllocSortBytes];
+
+namespace {
+
+std::mutex g_noalloc_mutex;
+void* g_noalloc_base[kNoAllocMaxDevices] = {};
+
+// Sub-cell keys of the caller's positions (the key of k_keys), identity values, and the count for the sort.
+__global__ void __launch_bounds__(256) k_noalloc_keys(GridDev g, const float4* __restrict__ pos, uint32_t n,
+                                                      uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                                                      uint32_t* d_n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) *d_n = n;
+    if (i >= n) return;
+    const float4 p = pos[i];
+    uint32_t key, refkey;
+    cell_of(g, p.x, p.y, p.z, key, refkey);
+    keys[i] = key;
+    vals[i] = i;
+}
+
+// Scratch address on the current device, looked up once per device.
+asph_status noalloc_base(void** out) {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(ASPH_ERR_UNSUPPORTED, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (g_noalloc_base[dev] == nullptr) CK(cudaGetSymbolAddress(&g_noalloc_base[dev], g_noalloc_scratch));
+    *out = g_noalloc_base[dev];
+    return ASPH_OK;
+}
+
+}  // namespace
+
+extern "C" asph_status asph_grid_sort_noalloc(const asph_parameters* params, const float* positions, uint32_t count,
+                                              uint32_t* sorted_keys, uint32_t* order, uint32_t* cell_start,
+                                              uint32_t* cell_end, uint32_t cell_capacity, uint32_t* device_errors,
+                                              void* stream) {
+    API_ENTRY();
+    if (!params || !device_errors) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
+    if (count > kNoAllocMax)
+        return fail(ASPH_ERR_CAPACITY, "asph_grid_sort_noalloc: count " + std::to_string(count) +
+                                           " exceeds the fixed scratch limit of " + std::to_string(kNoAllocMax) +
+                                           " particles");
+    if (count > 0 && (!positions || !sorted_keys || !order))
+        return fail(ASPH_ERR_INVALID_ARGUMENT, "null device array");
+    if ((cell_start == nullptr) != (cell_end == nullptr))
+        return fail(ASPH_ERR_INVALID_ARGUMENT, "cell_start and cell_end must both be given or both be NULL");
+    if (reinterpret_cast<uintptr_t>(positions) % 16 != 0)
+        return fail(ASPH_ERR_INVALID_ARGUMENT, "positions must be 16-byte aligned");
+    GridDev g;
+    asph_status st = make_grid(*params, g);
+    if (st != ASPH_OK) return st;
+    if (cell_start && cell_capacity < g.ncells)
+        return fail(ASPH_ERR_CAPACITY, "cell tables need " + std::to_string(g.ncells) + " entries");
+    if (sort_scratch_bytes(kNoAllocMax) > kNoAllocSortBytes)
+        return fail(ASPH_ERR_UNSUPPORTED, "sort scratch layout larger than the fixed array");
+    void* base = nullptr;
+    if ((st = noalloc_base(&base)) != ASPH_OK) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    uint32_t* d_n = static_cast<uint32_t*>(base);
+    SortScratch ss;
+    sort_scratch_bind(ss, static_cast<unsigned char*>(base) + kNoAllocHead, kNoAllocMax);
+    if (count > 0) {
+        k_noalloc_keys<<<blocks_for(count), 256, 0, s>>>(g, reinterpret_cast<const float4*>(positions), count,
+                                                         sorted_keys, order, d_n);
+        CK_LAUNCH("k_noalloc_keys");
+        uint32_t* keys = sorted_keys;
+        uint32_t* vals = order;
+        radix_sort_pairs(keys, vals, d_n, count, 3 * g.bits, ss, device_errors, s);
+        CK_LAUNCH("radix sort");
+        if (keys != sorted_keys) {  // odd number of digit passes: the result is in the scratch half
+            CK(cudaMemcpyAsync(sorted_keys, keys, sizeof(uint32_t) * count, cudaMemcpyDeviceToDevice, s));
+            CK(cudaMemcpyAsync(order, vals, sizeof(uint32_t) * count, cudaMemcpyDeviceToDevice, s));
+        }
+    }
+    if (cell_start) {
+        CK(cudaMemsetAsync(cell_start, 0xff, sizeof(uint32_t) * g.ncells, s));
+        CK(cudaMemsetAsync(cell_end, 0, sizeof(uint32_t) * g.ncells, s));
+        if (count > 0) {
+            k_cells_only<<<blocks_for(count), 256, 0, s>>>(g, sorted_keys, d_n, cell_start, cell_end);
+            CK_LAUNCH("k_cells_only");
+        }
+    }
     return ASPH_OK;
 }

@@ -371,6 +371,44 @@ asph_status asph_simulation_kernel_times(asph_simulation* sim, double* ms, uint3
 asph_status asph_simulation_launch_count(const asph_simulation* sim, uint64_t* out);
 
 /* ---------------------------------------------------------------------------------------------
+ * Cell sort without allocation. No counterpart in the reference: it is the cell-key computation and
+ * stable key sort of NeighborGrid::update (cuda/src/simulation/neighbors/NeighborGrid.cu:123-150)
+ * plus the cell tables, offered alone for callers that must not allocate device memory. Such
+ * callers own all device memory through their own allocator (a renderer that imports its particle
+ * buffers into CUDA under a fixed budget) or run in a frame loop where cudaMalloc/cudaFree would
+ * stall other streams (cudaFree synchronises the device) or could fail mid-frame.
+ *
+ * The call allocates nothing: its scratch is one fixed array of device memory inside this library
+ * (about 5.1 MB, sized for ASPH_NOALLOC_MAX_PARTICLES). count > ASPH_NOALLOC_MAX_PARTICLES is
+ * rejected with ASPH_ERR_CAPACITY. The first call on each device looks up the scratch address with
+ * that device current (and, with lazy module loading, loads the library's device code there); make
+ * that first call before any stream capture. The scratch is shared by all calls on a device: calls
+ * that may overlap (different streams, or several host threads) race on it and must be serialised
+ * by the caller. The sort's counters are zeroed by the call itself on `stream`; nothing in the
+ * scratch has to start at zero. The caller zeroes `device_errors` before its first use.
+ *
+ * params:        grid as asph_simulation_create builds it (domain, base_smoothing_radius, boundary_mode)
+ * positions:     device, 4 floats per particle (x, y, z, unused)
+ * sorted_keys:   device [count], sub-cell keys in sorted order (bit-identical to asph_simulation_read_grid)
+ * order:         device [count], order[k] = input index of the k-th particle (stable: equal keys keep
+ *                their input order)
+ * cell_start, cell_end: device [asph_grid_info.cell_count] or both NULL; cell_capacity their length
+ * device_errors: device word, OR-ed with ASPH_DEVERR_SPIN_LIMIT if a bounded wait of the sort gave up
+ * stream:        cudaStream_t (NULL: the legacy default stream); the call is asynchronous on it.
+ * ------------------------------------------------------------------------------------------- */
+#define ASPH_NOALLOC_MAX_PARTICLES 524288u
+asph_status asph_grid_sort_noalloc(const asph_parameters* params,
+                                   const float* positions,
+                                   uint32_t count,
+                                   uint32_t* sorted_keys,
+                                   uint32_t* order,
+                                   uint32_t* cell_start,
+                                   uint32_t* cell_end,
+                                   uint32_t cell_capacity,
+                                   uint32_t* device_errors,
+                                   void* stream);
+
+/* ---------------------------------------------------------------------------------------------
  * Misc
  * ------------------------------------------------------------------------------------------- */
 uint32_t asph_abi_version(void);
