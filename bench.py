@@ -152,6 +152,26 @@ def cpu_throughput(sc, bd, steps: int, warmup: int):
     return ps / dt, oracle.get_threads(), dt
 
 
+# ------------------------------------------------------------------------------------------------ replicas
+def gather_rows(local, dist, world: int, device: str) -> np.ndarray:
+    """Every rank's [particle-steps, seconds, e2e particle-steps, e2e seconds], one row per rank."""
+    import torch
+
+    t = torch.tensor(local, dtype=torch.float64, device=device)
+    gathered = [torch.zeros_like(t) for _ in range(world)]
+    dist.all_gather(gathered, t)
+    return torch.stack(gathered).cpu().numpy()
+
+
+def replica_throughput(rows: np.ndarray):
+    """Whole-job throughput of independent replicas: the work of all ranks over the slowest rank's time (device
+    timed and end to end)."""
+    value = float(rows[:, 0].sum()) / float(rows[:, 1].max())
+    e2e_time = float(rows[:, 3].max())
+    e2e = float(rows[:, 2].sum()) / e2e_time if e2e_time > 0 else 0.0
+    return value, e2e
+
+
 # ------------------------------------------------------------------------------------------------ GPU leg
 def run_ours(args, rank: int, world: int, dist):
     import torch
@@ -207,7 +227,7 @@ def run_ours(args, rank: int, world: int, dist):
     # 0 .. warmup + steps - 1 (the device-resident run times frames warmup .. warmup + steps - 1)
     e2e_counts = []
     d2h = 0
-    e2e_value = 0.0
+    e2e_s = 0.0
     h2d = 0.0
     if not args.no_e2e:
         torch.cuda.synchronize()
@@ -229,24 +249,14 @@ def run_ours(args, rank: int, world: int, dist):
             d2h += sum(v.nbytes for v in out.values())
         e2e_s = time.perf_counter() - t0
         sim2.close()
-        e2e_value = float(sum(e2e_counts)) / e2e_s
         h2d = (n0 * 16 + bd.get_particle_count() * 20) / len(e2e_counts)
 
-    local = np.array([particle_steps, ms, e2e_value], dtype=np.float64)
-    if dist is not None:
-        t = torch.tensor(local, device="cuda")
-        gathered = [torch.zeros_like(t) for _ in range(world)]
-        dist.all_gather(gathered, t)
-        allv = torch.stack(gathered).cpu().numpy()
-        total_ps = float(allv[:, 0].sum())
-        max_ms = float(allv[:, 1].max())
-        e2e_total = float(allv[:, 2].sum())
-    else:
-        total_ps, max_ms, e2e_total = particle_steps, ms, e2e_value
+    local = [particle_steps, ms / 1e3, float(sum(e2e_counts)), e2e_s]
+    rows = gather_rows(local, dist, world, "cuda") if dist is not None else np.array([local])
+    value, e2e_total = replica_throughput(rows)
     if rank != 0:
         return None
 
-    value = total_ps / (max_ms / 1e3)
     f_ms, f_launches = kt["forces"]
     avg_force_ms = f_ms / max(f_launches, 1)
     mean_n = particle_steps / max(args.steps, 1)

@@ -171,6 +171,13 @@ def lib():
         L.orc32_step.restype = ctypes.c_int
         L.orc_totals.argtypes = [P(OrcParams), P(OrcState), c_double_p]
         L.orc32_export_velocities.argtypes = [P(OrcParams), P(OrcState), c_float_p]
+        L.orc64_kernel_w.argtypes = [ctypes.c_double, ctypes.c_double]
+        L.orc64_kernel_w.restype = ctypes.c_double
+        L.orc64_kernel_dw.argtypes = [ctypes.c_double, ctypes.c_double]
+        L.orc64_kernel_dw.restype = ctypes.c_double
+        L.orc32_kernel_w.argtypes = [ctypes.c_float, ctypes.c_float]
+        L.orc32_kernel_w.restype = ctypes.c_float
+        L.orc_icosahedron.argtypes = [c_float_p]
         L.orc_set_threads.argtypes = [ctypes.c_int]
         L.orc_get_threads.restype = ctypes.c_int
         _lib = L

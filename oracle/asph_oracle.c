@@ -1290,3 +1290,32 @@ void orc_list_entries(const orc_grid* g, const orc_state* s, const orc_cells* c,
         out[i] = list_entries(g, s, c, i);
     }
 }
+
+/* kernel values and the split directions, for the known-answer tests */
+double orc64_kernel_w(double r, double h)
+{
+    double invh, wc, dwc;
+    kernel_consts_f64(h, &invh, &wc, &dwc);
+    return kernel_w_f64(r, invh, wc);
+}
+
+double orc64_kernel_dw(double r, double h)
+{
+    double invh, wc, dwc;
+    kernel_consts_f64(h, &invh, &wc, &dwc);
+    return kernel_dw_f64(r, invh, dwc);
+}
+
+float orc32_kernel_w(float r, float h)
+{
+    float invh, wc, dwc;
+    kernel_consts_f32(h, &invh, &wc, &dwc);
+    return kernel_w_f32(r, invh, wc);
+}
+
+void orc_icosahedron(float* out36)
+{
+    float v[12][3];
+    icosahedron(v);
+    memcpy(out36, v, sizeof(v));
+}

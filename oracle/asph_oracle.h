@@ -138,6 +138,13 @@ void orc64_density(const orc_grid* g, const orc_params* P, const orc_state* s, c
 void orc64_forces(const orc_grid* g, const orc_params* P, const orc_state* s, const orc_cells* c,
                   const orc_boundary* b, double* acc_out, double* scale_out);
 
+/* Wendland kernel W(r, h) and dW/dr (WendlandKernel.cuh:39-84) in both precisions; the 12 split directions
+ * (AdaptiveAlgorithm.cu:35-48) as 12 xyz triples */
+double orc64_kernel_w(double r, double h);
+double orc64_kernel_dw(double r, double h);
+float orc32_kernel_w(float r, float h);
+void orc_icosahedron(float* out36);
+
 /* FP64 totals: mass, momentum[3], kinetic energy (with the pending half-kick applied) */
 void orc_totals(const orc_params* P, const orc_state* s, double out[6]);
 /* velocities with the pending closing half-kick applied, as exported (vel4_out: 4n) */
