@@ -20,6 +20,7 @@ enum RefineCounter : int {
     kCtrSplits,         // parents split
     kCtrCountOut,       // final count
     kCtrNextId,         // next free particle id
+    kCtrMergeHeavy,     // merge candidates with query boxes of more than 27 reference cells (warp kernel)
     kCtrNum
 };
 
@@ -32,6 +33,7 @@ struct RefineArgs {
     uint32_t* keep_ids;         // optional lists for tests (may be null)
     uint32_t* removed_ids;
     uint32_t* split_ids;
+    uint32_t* mqueue;  // [cap] merge candidates for the warp kernel
     uint32_t* err;
     float min_mass, max_mass, max_batch_ratio;
     float eps, alpha, center_ratio, vertex_ratio;
@@ -49,6 +51,7 @@ __global__ void k_select_scores(const float* score, const uint32_t* n_ptr, int d
                                 uint32_t* keys);
 __global__ void k_merge_limits(RefineArgs r, uint32_t n);
 __global__ void k_cand_init(RefineArgs r, uint32_t n);
+__global__ void k_merge_candidates_heavy(StepArgs a, CellsDev c, RefineArgs r);
 __global__ void k_merge_candidates(StepArgs a, CellsDev c, RefineArgs r, const uint32_t* sel);
 __global__ void k_merge_pairs(StepArgs a, RefineArgs r);
 __global__ void k_compact_count(const uint32_t* flag, uint32_t n, uint32_t* block_counts);

@@ -291,6 +291,7 @@ __device__ __forceinline__ void fluid_candidates(const StepArgs& a, const CellsD
 }  // namespace
 
 // Density pass, ordinary particles; heavy particles are queued for k_density_heavy.
+template <bool kPeriodic>
 __global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
     __shared__ uint2 stage[256 * kStageStride];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -302,7 +303,7 @@ __global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, Boun
         nl.cnt[i] = kHeavyMark;
         active = false;
     }
-    const bool periodic = a.grid.periodic;
+    constexpr bool periodic = kPeriodic;
     uint2* row = nl.ent + (size_t)(in ? i : 0) * nl.maxe;
     uint2* st = stage + threadIdx.x * kStageStride;
     const uint32_t maxe = nl.maxe;
@@ -325,8 +326,10 @@ __global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, Boun
     // mask, and the block (first member, mask) goes to the lane's list row. The kernel sums are formed afterwards
     // from the row, one accepted neighbour per iteration.
     auto scan_block = [&](uint32_t c0, uint32_t cn, uint32_t code, float shx, float shy, float shz) {
+        // members from last to first, so the mask is built by shifts: bit k = member c0 + k
         uint32_t mask = 0;
-        for (uint32_t k = 0; k < cn; ++k) {
+#pragma unroll 4
+        for (int k = (int)cn - 1; k >= 0; --k) {
             const float4 pj = __ldg(a.ph + c0 + k);
             const float xj = periodic ? pj.x + shx : pj.x;
             const float yj = periodic ? pj.y + shy : pj.y;
@@ -334,7 +337,7 @@ __global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, Boun
             const float dx = xj - pi.x, dy = yj - pi.y, dz = zj - pi.z;
             const float r2 = dist2(dx, dy, dz);
             const float twoh = pj.w + pj.w;
-            mask |= (r2 <= twoh * twoh ? 1u : 0u) << k;
+            mask = (mask << 1) | (r2 <= twoh * twoh ? 1u : 0u);
         }
         if (mask != 0u) append(c0 | code, mask);
     };
@@ -485,8 +488,10 @@ cudaError_t launch_density(DensityKernel kind, uint32_t blocks, cudaStream_t str
         k_density_heavy<<<blocks, 256, 0, stream>>>(a, c, b, nl, nl.heavy, nl.heavy_n);
     else if (kind == kDensityOverflow)
         k_density_heavy<<<blocks, 256, 0, stream>>>(a, c, b, nl, nl.dover, nl.dover_n);
+    else if (a.grid.periodic)
+        k_density<true><<<blocks, 256, 0, stream>>>(a, c, b, nl);
     else
-        k_density<<<blocks, 256, 0, stream>>>(a, c, b, nl);
+        k_density<false><<<blocks, 256, 0, stream>>>(a, c, b, nl);
     return cudaGetLastError();
 }
 

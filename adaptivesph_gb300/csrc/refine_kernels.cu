@@ -224,6 +224,10 @@ __global__ void __launch_bounds__(256) k_merge_candidates(StepArgs a, CellsDev c
     const uint32_t e = sel[q];
     const float4 pe = a.ph[e];
     const float he = pe.w;
+    if (box_cells(a.grid, pe, he) > kHeavyCells) {  // large box: one warp (k_merge_candidates_heavy)
+        r.mqueue[atomicAdd(r.ctr + kCtrMergeHeavy, 1u)] = e;
+        return;
+    }
     float best = 3.402823466e38f;
     uint32_t bj = kNone, bid = 0xffffffffu;
     for_each_cell<true>(a.grid, c.start, c.end, c.hmax, c.hmax_ref, c.ex[0], c.ex[1], pe.x, pe.y, pe.z, he, he,
@@ -245,6 +249,53 @@ __global__ void __launch_bounds__(256) k_merge_candidates(StepArgs a, CellsDev c
                             }
                         });
     r.cand[e] = bj;
+}
+
+// identifyMergeCandidates for the queued large boxes: one warp per particle, member m of every visited sub-cell on
+// lane m mod 32. The nearest candidate is the minimum of (r^2, id) over the accepted members, which does not
+// depend on the visiting order, so the warp's reduction gives the sequential scan's result.
+__global__ void __launch_bounds__(256) k_merge_candidates_heavy(StepArgs a, CellsDev c, RefineArgs r) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t nq = r.ctr[kCtrMergeHeavy];
+    for (uint32_t w = warp; w < nq; w += nwarps) {
+        const uint32_t e = r.mqueue[w];
+        const float4 pe = a.ph[e];
+        const float he = pe.w;
+        float best = 3.402823466e38f;
+        uint32_t bj = kNone, bid = 0xffffffffu;
+        for_each_cell<true>(a.grid, c.start, c.end, c.hmax, c.hmax_ref, c.ex[0], c.ex[1], pe.x, pe.y, pe.z, he, he,
+                            [&](uint32_t jb, uint32_t je, float, float, float) {
+                                for (uint32_t j = jb + lane; j < je; j += 32) {
+                                    if (j == e) continue;
+                                    const float4 pj = a.ph[j];
+                                    const float dx = pj.x - pe.x, dy = pj.y - pe.y, dz = pj.z - pe.z;
+                                    const float r2 = dist2(dx, dy, dz);
+                                    const float hm = pj.w < he ? pj.w : he;
+                                    if (r2 < hm * hm && a.vm[j].w < r.max_mass) {
+                                        const uint32_t idj = a.id[j];
+                                        if (r2 < best || (r2 == best && idj < bid)) {
+                                            best = r2;
+                                            bj = j;
+                                            bid = idj;
+                                        }
+                                    }
+                                }
+                            });
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const uint32_t oj = __shfl_xor_sync(0xffffffffu, bj, o);
+            const uint32_t oid = __shfl_xor_sync(0xffffffffu, bid, o);
+            if (ob < best || (ob == best && oid < bid)) {
+                best = ob;
+                bj = oj;
+                bid = oid;
+            }
+        }
+        if (lane == 0) r.cand[e] = bj;
+    }
 }
 
 // resolveMergePairs + performMerges + calculateMergedSmoothingLength (AdaptiveAlgorithm.cu:50-67, 208-275)

@@ -568,6 +568,7 @@ RefineArgs refine_args(asph_simulation* s) {
     r.keep_ids = s->record_ids ? s->dbg_ids : nullptr;
     r.removed_ids = s->record_ids ? s->dbg_ids + s->cap : nullptr;
     r.split_ids = s->record_ids ? s->dbg_ids + 2 * (size_t)s->cap : nullptr;
+    r.mqueue = s->dover_idx;  // the density-overflow queue is dead after the force pass
     r.err = s->err;
     const asph_refinement_parameters& R = s->R;
     r.min_mass = R.min_mass_ratio * s->P.base_particle_mass;
@@ -628,6 +629,7 @@ asph_status run_refine(asph_simulation* s) {
     // candidates, pairs + merges
     k_cand_init<<<nbk, 256, 0, s->stream>>>(r, n);
     k_merge_candidates<<<nbk, 256, 0, s->stream>>>(a, s->cells(), r, s->vals);
+    k_merge_candidates_heavy<<<kHeavyBlocks, 256, 0, s->stream>>>(a, s->cells(), r);
     k_merge_pairs<<<nbk, 256, 0, s->stream>>>(a, r);
     CK_LAUNCH("merge");
     // stable compaction into the other buffer set (also carries the cell keys for the vorticity split pass)
@@ -640,7 +642,7 @@ asph_status run_refine(asph_simulation* s) {
     k_compact_scatter<<<nbk, 256, 0, s->stream>>>(a, b, s->flag, s->block_counts, vort ? s->rkeys : nullptr,
                                                    keys_c);
     CK_LAUNCH("compaction");
-    s->launches += 6;
+    s->launches += 7;
     s->cur = nxt;
     StepArgs c = s->args(s->cur);
     if (vort) {

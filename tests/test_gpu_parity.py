@@ -211,3 +211,34 @@ def test_adaptive_velocity_trajectory_bitexact():
             saw_split |= rep["splits"] > 0
         assert_state_bitexact(sim.read_state(), orc.arrays())
     assert saw_merge and saw_split, "the scene must exercise both merging and splitting"
+
+
+def test_refinement_with_large_smoothing_lengths_bitexact():
+    """A refinement frame on a state with h up to 6 h0: large merge-candidate boxes go to the warp kernel, whose
+    nearest-candidate choice must equal the oracle's sequential scan."""
+    ref = adaptive_refinement(max_mass_ratio=64.0)
+    sc = small_dam_break(counts=(16, 24, 16), dx=0.02, tank=(0.7, 0.7, 0.5), refinement=ref)
+    sim, orc = make_pair(sc)
+    sim.record_refinement_ids(True)
+    _advance(sim, orc, sc.dt, 2)
+    st = sim.read_state()
+    rng = np.random.default_rng(3)
+    h0 = np.float32(sc.parameters.base_smoothing_radius)
+    choice = rng.choice(4, size=st["h"].shape[0], p=[0.7, 0.1, 0.1, 0.1])
+    st["h"] = (h0 * np.array([1.0, 2.0, 4.5, 6.0], np.float32)[choice]).astype(np.float32)
+    st["m"] = (st["m"] * np.array([1.0, 8.0, 24.0, 40.0], np.float32)[choice]).astype(np.float32)
+    nid = int(st["id"].max()) + 1
+    sim.write_state(st, frame=6, next_id=nid, pending_half=sc.dt / 2)
+    orc.load(st, frame=6, next_id=nid, pending_half=sc.dt / 2)
+    sim.update(sc.dt)
+    assert orc.step(sc.dt), "the frame must run the refinement pass"
+    rep = sim.last_refinement()
+    o = orc.last_report()
+    for key in ("merge_eligible", "merge_pairs", "removed", "split_candidates", "split_budget", "splits",
+                "count_after"):
+        assert rep[key] == o[key], (key, rep[key], o[key])
+    assert rep["merge_pairs"] > 0
+    ids = sim.refinement_ids()
+    assert sorted(ids["keep_ids"].tolist()) == sorted(o["keep_ids"].tolist())
+    assert sorted(ids["removed_ids"].tolist()) == sorted(o["removed_ids"].tolist())
+    assert_state_bitexact(sim.read_state(), orc.arrays())
