@@ -285,6 +285,56 @@ __device__ __forceinline__ void for_each_cell(const GridDev& g, const uint32_t* 
     }
 }
 
+// One query walked by a whole warp: the sub-cells of the box [x-R, x+R] are numbered in the canonical order,
+// t = 8 * (index of the reference cell in z, y, x order within the box) + (sub-cell z, y, x bits), and lane l
+// visits those with t mod 32 == l, in increasing t. Excluded, empty and culled sub-cells are skipped (culling as in
+// for_each_cell<true>: reach = Rfix when Rfix > 0, else 2 * max h of the sub-cell); so the 32 lanes walk a large
+// box in 1/32 of the sequential walk, and each lane's visiting order is fixed by the box alone.
+template <class Body>
+__device__ __forceinline__ void for_each_subcell_lane(const GridDev& g, const uint32_t* __restrict__ start,
+                                                      const uint32_t* __restrict__ end,
+                                                      const float* __restrict__ hmax, uint32_t ex0, uint32_t ex1,
+                                                      float px, float py, float pz, float R, float Rfix, int lane,
+                                                      Body&& body) {
+    int32_t lo[3], hi[3];
+    const float p[3] = {px, py, pz};
+    bool ok = true;
+#pragma unroll
+    for (int a = 0; a < 3; a++) ok &= box_axis(g, a, p[a], R, lo[a], hi[a]);
+    if (!ok) return;
+    const uint32_t nx = (uint32_t)(hi[0] - lo[0] + 1), ny = (uint32_t)(hi[1] - lo[1] + 1);
+    const uint32_t nz = (uint32_t)(hi[2] - lo[2] + 1);
+    const uint32_t total = nx * ny * nz * 8u;
+    const bool periodic = g.periodic;
+    const float m = g.cull_margin;
+    for (uint32_t t = (uint32_t)lane; t < total; t += 32u) {
+        const uint32_t q = t & 7u, cell = t >> 3;
+        const uint32_t cxy = cell % (nx * ny);
+        float shx, shy, shz;
+        const int32_t cz = wrap_cell(lo[2] + (int32_t)(cell / (nx * ny)), g.gs[2], g.scale[2], periodic, shz);
+        const int32_t cy = wrap_cell(lo[1] + (int32_t)(cxy / nx), g.gs[1], g.scale[1], periodic, shy);
+        const int32_t cx = wrap_cell(lo[0] + (int32_t)(cxy % nx), g.gs[0], g.scale[0], periodic, shx);
+        if (cz < 0 || cz >= g.gs[2] || cy < 0 || cy >= g.gs[1] || cx < 0 || cx >= g.gs[0]) continue;
+        if (!periodic) {
+            const uint32_t rk =
+                (uint32_t)cx + (uint32_t)g.gs[0] * ((uint32_t)cy + (uint32_t)g.gs[1] * (uint32_t)cz);
+            if (rk == ex0 || rk == ex1) continue;
+        }
+        const int32_t sx = 2 * cx + (int32_t)(q & 1u), sy = 2 * cy + (int32_t)((q >> 1) & 1u),
+                      sz = 2 * cz + (int32_t)(q >> 2);
+        const uint32_t lin = (uint32_t)sx + (uint32_t)g.sgs[0] * ((uint32_t)sy + (uint32_t)g.sgs[1] * (uint32_t)sz);
+        const uint32_t b = __ldg(start + lin);
+        const float hs = __ldg(hmax + lin);
+        if (b == kEmpty) continue;
+        const float reach = (Rfix > 0.0f ? Rfix : 2.0f * hs) * 1.00005f;
+        const float dx = gap1(px, g.dmin[0] + (float)sx * g.w[0] + shx, g.w[0], m);
+        const float dy = gap1(py, g.dmin[1] + (float)sy * g.w[1] + shy, g.w[1], m);
+        const float dz = gap1(pz, g.dmin[2] + (float)sz * g.w[2] + shz, g.w[2], m);
+        if (dx * dx + dy * dy + dz * dz > reach * reach) continue;
+        body(b, __ldg(end + lin), shx, shy, shz);
+    }
+}
+
 // Warp-cooperative form of for_each_cell<true> for the 32 particles of a warp (one per lane; `active` lanes only).
 // The warp walks the union of the lanes' boxes in the canonical order (reference cells z, y, x; their sub-cells
 // z, y, x) and calls body(begin, end, shx, shy, shz, need) warp-uniformly for every sub-cell that some lane needs;

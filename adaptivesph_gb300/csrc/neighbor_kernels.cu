@@ -13,9 +13,10 @@
 // its density over its row, and the force pass sums over the same row: the masks expanded in member order give the
 // accepted neighbours in the canonical order, one per loop iteration.
 // Heavy particles (query box of more than 27 reference cells: smoothing lengths grown by merging) and particles
-// with more entries than a row holds: one warp per particle; in every visited sub-cell member m goes to lane
-// m mod 32, lane sums are combined by a fixed butterfly. They are queued for separate warp kernels, so a few large
-// boxes do not stall whole blocks.
+// with more entries than a row holds: one warp per particle; the box's sub-cells are dealt to the lanes by their
+// canonical index (for_each_subcell_lane), each lane sums its sub-cells' members in order, and the lane sums are
+// combined by a fixed butterfly. They are queued for separate warp kernels, so a few large boxes do not stall
+// whole blocks.
 #include "asph_device.cuh"
 #include "asph_kernels.cuh"
 
@@ -398,11 +399,10 @@ __global__ void __launch_bounds__(256, 1) k_density_heavy(StepArgs a, CellsDev c
         const float4 pi = a.ph[i];
         const float R = pi.w + pi.w;
         float rho = 0.0f;
-        for_each_cell<true>(
-            a.grid, c.start, c.end, c.hmax, c.hmax_ref, c.ex[0], c.ex[1], pi.x, pi.y, pi.z, R, 0.0f,
-            [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
-                for (uint32_t j = jb + lane; j < je; j += 32) density_term(a, pi, j, shx, shy, shz, rho);
-            });
+        for_each_subcell_lane(a.grid, c.start, c.end, c.hmax, c.ex[0], c.ex[1], pi.x, pi.y, pi.z, R, 0.0f, lane,
+                              [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
+                                  for (uint32_t j = jb; j < je; ++j) density_term(a, pi, j, shx, shy, shz, rho);
+                              });
         rho = warp_sum_butterfly(rho);
         float rb = 0.0f;
         if (boundary_near(a.grid, b, pi.x, pi.y, pi.z, R)) rb = warp_sum_butterfly(boundary_density<32>(a, b, i, pi, lane));
@@ -458,14 +458,13 @@ __global__ void __launch_bounds__(256, 1) k_forces_heavy(StepArgs a, CellsDev c,
         const uint32_t i = nl.fheavy[w];
         const ForceCtx x = force_ctx(a, i);
         ForceAcc f = {};
-        for_each_cell<true>(
-            a.grid, c.start, c.end, c.hmax, c.hmax_ref, c.ex[0], c.ex[1], x.pi.x, x.pi.y, x.pi.z, x.hi + x.hi, 0.0f,
-            [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
-                for (uint32_t j = jb + lane; j < je; j += 32) {
-                    if (j == i) continue;
-                    force_term<kMorris>(a, x, j, shx, shy, shz, f);
-                }
-            });
+        for_each_subcell_lane(a.grid, c.start, c.end, c.hmax, c.ex[0], c.ex[1], x.pi.x, x.pi.y, x.pi.z,
+                              x.hi + x.hi, 0.0f, lane, [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
+                                  for (uint32_t j = jb; j < je; ++j) {
+                                      if (j == i) continue;
+                                      force_term<kMorris>(a, x, j, shx, shy, shz, f);
+                                  }
+                              });
         if (boundary_near(a.grid, b, x.pi.x, x.pi.y, x.pi.z, x.hi + x.hi)) boundary_forces<32>(a, b, i, x, f, lane);
 #pragma unroll
         for (int q = 0; q < 3; q++) {
@@ -512,7 +511,7 @@ cudaError_t launch_forces(bool heavy, bool morris, uint32_t blocks, cudaStream_t
 }
 
 // Per-particle neighbour counts (sumAllNeighbors, cuda/src/algorithm/Algorithm.cu:234-268).
-__global__ void __launch_bounds__(256) k_neighbor_counts(StepArgs a, CellsDev c, uint32_t* counts,
+__global__ void __launch_bounds__(256, 4) k_neighbor_counts(StepArgs a, CellsDev c, uint32_t* counts,
                                                          unsigned long long* total) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t cnt = 0;

@@ -115,7 +115,7 @@ __device__ __forceinline__ float compmin3(const float v[3]) {
 
 // merge criterion per particle (VelocityCriterion.cuh:208-227, InterfaceCriterion.cuh:97-115,
 // VorticityCriterion.cuh:248-312); slot-0 particle (smallest id) found on the way.
-__global__ void __launch_bounds__(256) k_merge_score(StepArgs a, CellsDev c, RefineArgs r) {
+__global__ void __launch_bounds__(256, 2) k_merge_score(StepArgs a, CellsDev c, RefineArgs r) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     float s = -1.0f;
     uint64_t slot = ~0ull;
@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(256) k_merge_score(StepArgs a, CellsDev c, Ref
 
 // split criterion per particle of the compacted set (VelocityCriterion.cuh:180-206,
 // InterfaceCriterion.cuh:69-95, VorticityCriterion.cuh:170-246)
-__global__ void __launch_bounds__(256) k_split_score(StepArgs a, CellsDev c, RefineArgs r) {
+__global__ void __launch_bounds__(256, 2) k_split_score(StepArgs a, CellsDev c, RefineArgs r) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t n = (r.ctr[kCtrRemoved] > 0u) ? r.ctr[kCtrCount2] : 0u;
     float s = -1.0f;
@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(256) k_cand_init(RefineArgs r, uint32_t n) {
 }
 
 // identifyMergeCandidates (AdaptiveAlgorithm.cu:159-206)
-__global__ void __launch_bounds__(256) k_merge_candidates(StepArgs a, CellsDev c, RefineArgs r,
+__global__ void __launch_bounds__(256, 4) k_merge_candidates(StepArgs a, CellsDev c, RefineArgs r,
                                                           const uint32_t* sel) {
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= r.ctr[kCtrEligible]) return;
@@ -251,10 +251,10 @@ __global__ void __launch_bounds__(256) k_merge_candidates(StepArgs a, CellsDev c
     r.cand[e] = bj;
 }
 
-// identifyMergeCandidates for the queued large boxes: one warp per particle, member m of every visited sub-cell on
-// lane m mod 32. The nearest candidate is the minimum of (r^2, id) over the accepted members, which does not
+// identifyMergeCandidates for the queued large boxes: one warp per particle, the box's sub-cells dealt to the lanes
+// (for_each_subcell_lane). The nearest candidate is the minimum of (r^2, id) over the accepted members, which does not
 // depend on the visiting order, so the warp's reduction gives the sequential scan's result.
-__global__ void __launch_bounds__(256) k_merge_candidates_heavy(StepArgs a, CellsDev c, RefineArgs r) {
+__global__ void __launch_bounds__(256, 4) k_merge_candidates_heavy(StepArgs a, CellsDev c, RefineArgs r) {
     const int lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -265,9 +265,9 @@ __global__ void __launch_bounds__(256) k_merge_candidates_heavy(StepArgs a, Cell
         const float he = pe.w;
         float best = 3.402823466e38f;
         uint32_t bj = kNone, bid = 0xffffffffu;
-        for_each_cell<true>(a.grid, c.start, c.end, c.hmax, c.hmax_ref, c.ex[0], c.ex[1], pe.x, pe.y, pe.z, he, he,
-                            [&](uint32_t jb, uint32_t je, float, float, float) {
-                                for (uint32_t j = jb + lane; j < je; j += 32) {
+        for_each_subcell_lane(a.grid, c.start, c.end, c.hmax, c.ex[0], c.ex[1], pe.x, pe.y, pe.z, he, he, lane,
+                              [&](uint32_t jb, uint32_t je, float, float, float) {
+                                for (uint32_t j = jb; j < je; ++j) {
                                     if (j == e) continue;
                                     const float4 pj = a.ph[j];
                                     const float dx = pj.x - pe.x, dy = pj.y - pe.y, dz = pj.z - pe.z;

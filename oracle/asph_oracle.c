@@ -148,6 +148,8 @@ typedef struct orc_iter {
     float sh[3];                /* its periodic image offset */
     int q;                      /* next sub-cell of the current reference cell, 0..8 */
     int empty;
+    uint32_t t; /* canonical index in the box of the sub-cell it_next returned: 8 * (reference cell in z, y, x
+                   order within the box) + sub-cell; a heavy particle's sub-cell t is summed on lane t mod 32 */
 } orc_iter;
 
 static float clampf(float x, float lo, float hi)
@@ -269,6 +271,11 @@ static int it_next(orc_iter* it, uint32_t* b, uint32_t* e, float sh[3])
             return 0;
         }
         const int q = it->q++;
+        it->t = (uint32_t)((((it->r[2] - it->lo[2]) * (it->hi[1] - it->lo[1] + 1) + (it->r[1] - it->lo[1])) *
+                                (it->hi[0] - it->lo[0] + 1) +
+                            (it->r[0] - it->lo[0])) *
+                               8 +
+                           q);
         const int32_t sx = 2 * it->c[0] + (q & 1), sy = 2 * it->c[1] + ((q >> 1) & 1), sz = 2 * it->c[2] + (q >> 2);
         const uint32_t lin = (uint32_t)(sx + g->sgs[0] * (sy + g->sgs[1] * sz));
         if (it->start[lin] == ORC_EMPTY) {

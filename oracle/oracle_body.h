@@ -20,11 +20,13 @@
  *
  * Summation order: neighbours are summed in the canonical visiting order of the candidate cells. A particle
  * whose query box spans more than ORC_HEAVY_CELLS reference cells ("heavy", after merges made h large) is summed
- * as the GPU sums it with one warp: in every visited sub-cell, member m (counted from the sub-cell's first member)
- * goes to lane m mod 32, each lane sums its members in the canonical order, and the 32 partial sums are combined
- * by the butterfly
- * s_l <- s_l + s_(l xor o) for o = 16, 8, 4, 2, 1. A particle whose neighbour-list row would need more than
- * ORC_LIST_ENTRIES entries (see list_entries) is summed the same way, in both passes.
+ * as the GPU sums it with one warp: the box's sub-cell with canonical index t (see orc_iter.t) goes to lane
+ * t mod 32, each lane sums the members of its sub-cells in the canonical order, and the 32 partial sums are
+ * combined by the butterfly
+ * s_l <- s_l + s_(l xor o) for o = 16, 8, 4, 2, 1. Its boundary terms are dealt by member instead: member k of
+ * each visited boundary cell (counted from the cell's first member) goes to lane k mod 32. A particle whose
+ * neighbour-list row would need more than ORC_LIST_ENTRIES entries (see list_entries) is summed the same way, in
+ * both passes.
  */
 
 /* W(r, h) with precomputed 1/h and coef/h^3 */
@@ -106,7 +108,10 @@ static REAL F(density_fluid)(const orc_grid* g, const orc_state* s, const orc_ce
     float sh[3];
     it_init(&it, g, c->start, c->end, c->ex, pi, R);
     while (it_next(&it, &jb, &je, sh)) {
-        for (uint32_t j = jb + (uint32_t)lane; j < je; j += (uint32_t)lanes) {
+        if (it.t % (uint32_t)lanes != (uint32_t)lane) {
+            continue;
+        }
+        for (uint32_t j = jb; j < je; j++) {
             const float* pj = s->pos + 4 * (size_t)j;
             const REAL dx = NBR(pj, 0) - xi;
             const REAL dy = NBR(pj, 1) - yi;
@@ -217,7 +222,10 @@ static void F(forces_part)(const orc_grid* g, const orc_params* P, const orc_sta
     float sh[3];
     it_init(&it, g, c->start, c->end, c->ex, pi, R);
     while (it_next(&it, &jb, &je, sh)) {
-        for (uint32_t j = jb + (uint32_t)lane; j < je; j += (uint32_t)lanes) {
+        if (it.t % (uint32_t)lanes != (uint32_t)lane) {
+            continue;
+        }
+        for (uint32_t j = jb; j < je; j++) {
             if ((int64_t)j == i) {
                 continue;
             }
