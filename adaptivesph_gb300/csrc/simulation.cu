@@ -533,8 +533,8 @@ asph_status run_density(asph_simulation* s) {
     CK(cudaMemsetAsync(s->fheavy_n, 0, 2 * sizeof(uint32_t), s->stream));
     CK(cudaEventRecord(s->ev_fork, s->stream));
     CK(cudaStreamWaitEvent(s->aux, s->ev_fork, 0));
-    CK(launch_density(kDensityOrdinary, blocks_for(s->n), s->stream, a, s->cells(), s->boundary(), s->nbrs()));
     CK(launch_density(kDensityHeavy, kHeavyBlocks, s->aux, a, s->cells(), s->boundary(), s->nbrs()));
+    CK(launch_density(kDensityOrdinary, blocks_for(s->n), s->stream, a, s->cells(), s->boundary(), s->nbrs()));
     CK(launch_density(kDensityOverflow, kHeavyBlocks, s->stream, a, s->cells(), s->boundary(), s->nbrs()));
     CK(cudaEventRecord(s->ev_main, s->stream));
     CK(cudaEventRecord(s->ev_aux, s->aux));
@@ -548,9 +548,9 @@ asph_status run_forces(asph_simulation* s) {
     StepArgs a = s->args(s->cur);
     int h = s->tic();
     CK(cudaStreamWaitEvent(s->aux, s->ev_main, 0));
+    CK(launch_forces(true, s->phys.morris != 0, kHeavyBlocks, s->aux, a, s->cells(), s->boundary(), s->nbrs()));
     CK(launch_forces(false, s->phys.morris != 0, blocks_for(s->n), s->stream, a, s->cells(), s->boundary(),
                      s->nbrs()));
-    CK(launch_forces(true, s->phys.morris != 0, kHeavyBlocks, s->aux, a, s->cells(), s->boundary(), s->nbrs()));
     CK(cudaEventRecord(s->ev_aux, s->aux));
     CK(cudaStreamWaitEvent(s->stream, s->ev_aux, 0));
     s->toc(h, ASPH_KERNEL_FORCES);
@@ -991,7 +991,11 @@ asph_status asph_simulation_create(const asph_parameters* parameters, const floa
         return cuda_fail(e, "cudaStreamCreate");
     }
     s->stream = s->own_stream;
-    e = cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking);
+    // the heavy-particle kernels run few, long warps: their stream gets the highest priority so that their blocks
+    // are dispatched ahead of the ordinary kernels' and their latency overlaps the ordinary work
+    int prio_least = 0, prio_greatest = 0;
+    e = cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s->aux, cudaStreamNonBlocking, prio_greatest);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_main, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_aux, cudaEventDisableTiming);
