@@ -58,6 +58,9 @@ static inline uint32_t blocks_for(uint32_t n, uint32_t t = 256) { return n == 0 
 // blocks of 8 warps for the heavy-particle kernels (one warp per heavy particle, grid-stride over the queue)
 static constexpr uint32_t kHeavyBlocks = 304;
 
+// bytes of the per-simulation reduction scratch (totals, CFL minimum, density info)
+static constexpr size_t kRedBytes = 256;
+
 // ------------------------------------------------------------------------------------------------ memory
 struct asph_memory {
     void* ptr = nullptr;
@@ -160,6 +163,7 @@ struct asph_simulation {
     unsigned long long* q3 = nullptr;
     uint32_t* err = nullptr;
     uint32_t* d_count = nullptr;
+    uint8_t* red = nullptr;  // [kRedBytes] reduction scratch of totals, CFL and density info
 
     // boundary
     float4* bpos = nullptr;
@@ -778,6 +782,7 @@ void destroy(asph_simulation* s) {
     dfree(s->q3);
     dfree(s->err);
     dfree(s->d_count);
+    dfree(s->red);
     dfree(s->bpos);
     dfree(s->bfric);
     dfree(s->bstart);
@@ -1038,6 +1043,7 @@ asph_status asph_simulation_create(const asph_parameters* parameters, const floa
     TRY(dalloc(s->q3, 2));
     TRY(dalloc(s->err, 1));
     TRY(dalloc(s->d_count, 2));
+    TRY(dalloc(s->red, kRedBytes));
     TRY(alloc_cells(s));
     if (adaptive) {
         TRY(dalloc(s->score, C));
@@ -1126,9 +1132,7 @@ asph_status asph_simulation_totals(asph_simulation* sim, asph_totals* out) {
     std::memset(out, 0, sizeof(*out));
     out->count = sim->n;
     if (sim->n == 0) return ASPH_OK;
-    double* d = nullptr;
-    asph_status st;
-    if ((st = dalloc(d, 6)) != ASPH_OK) return st;
+    double* d = reinterpret_cast<double*>(sim->red);
     CK(cudaMemsetAsync(d, 0, sizeof(double) * 6, sim->stream));
     k_totals<<<blocks_for(sim->n), 256, 0, sim->stream>>>(sim->args(sim->cur), sim->pending_half,
                                                           sim->has_pending ? 1 : 0, d, nullptr);
@@ -1137,7 +1141,6 @@ asph_status asph_simulation_totals(asph_simulation* sim, asph_totals* out) {
     double h[6];
     CK(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, sim->stream));
     CK(cudaStreamSynchronize(sim->stream));
-    dfree(d);
     out->mass = h[0];
     out->momentum[0] = h[1];
     out->momentum[1] = h[2];
@@ -1152,9 +1155,7 @@ asph_status asph_simulation_step_cfl(asph_simulation* sim, float cfl, float dt_m
     if (!sim || !(cfl > 0.0f)) return fail(ASPH_ERR_INVALID_ARGUMENT, "simulation and cfl > 0 required");
     float dt = dt_max > 0.0f ? dt_max : 3.402823466e38f;
     if (sim->n > 0) {
-        double* d = nullptr;
-        asph_status st;
-        if ((st = dalloc(d, 8)) != ASPH_OK) return st;
+        double* d = reinterpret_cast<double*>(sim->red);
         CK(cudaMemsetAsync(d, 0, sizeof(double) * 8, sim->stream));
         unsigned int* bits = reinterpret_cast<unsigned int*>(d + 6);
         CK(cudaMemsetAsync(bits, 0x7f, sizeof(unsigned int), sim->stream));
@@ -1165,7 +1166,6 @@ asph_status asph_simulation_step_cfl(asph_simulation* sim, float cfl, float dt_m
         unsigned int hb = 0;
         CK(cudaMemcpyAsync(&hb, bits, sizeof(hb), cudaMemcpyDeviceToHost, sim->stream));
         CK(cudaStreamSynchronize(sim->stream));
-        dfree(d);
         float m;
         std::memcpy(&m, &hb, sizeof(m));
         const float c = cfl * m;
@@ -1269,9 +1269,7 @@ asph_status asph_simulation_density_info(asph_simulation* sim, float threshold, 
         out->average_density = NAN;  // 0 / 0 as in the reference (SphSimulation.cu:283)
         return ASPH_OK;
     }
-    uint8_t* d = nullptr;
-    asph_status st;
-    if ((st = dalloc(d, 64)) != ASPH_OK) return st;
+    uint8_t* d = sim->red;
     double* sum = reinterpret_cast<double*>(d);
     unsigned int* mm = reinterpret_cast<unsigned int*>(d + 8);
     unsigned int* cnt = reinterpret_cast<unsigned int*>(d + 16);
@@ -1284,7 +1282,6 @@ asph_status asph_simulation_density_info(asph_simulation* sim, float threshold, 
     uint8_t h[64];
     CK(cudaMemcpyAsync(h, d, 64, cudaMemcpyDeviceToHost, sim->stream));
     CK(cudaStreamSynchronize(sim->stream));
-    dfree(d);
     double hs;
     unsigned int hm[2], hc[3];
     std::memcpy(&hs, h, 8);

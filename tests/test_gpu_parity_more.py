@@ -1,0 +1,159 @@
+"""More GPU parity cases through the C ABI: the other refinement criteria, the periodic Taylor-Green box with Morris
+viscosity, the CFL step, tiny particle counts (the reference's excluded-cell quirk), an empty boundary and the split
+capacity limit. The oracle is the checker; FP32 results are compared bit for bit."""
+import dataclasses
+
+import numpy as np
+import pytest
+
+from adaptivesph_gb300 import StaticBoundaryDomain, create_simulation, scenes
+from adaptivesph_gb300.parameters import Criterion
+import oracle
+from helpers import adaptive_refinement, assert_bitexact, assert_state_bitexact, make_pair, small_dam_break
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("criterion", [Criterion.VORTICITY, Criterion.INTERFACE])
+def test_criterion_trajectory_bitexact(criterion):
+    ref = adaptive_refinement(criterion=criterion, velocity_split_min_speed=2.0, velocity_merge_max_speed=0.1)
+    sc = small_dam_break(refinement=ref)
+    sim, orc = make_pair(sc)
+    sim.record_refinement_ids(True)
+    merges = splits = 0
+    for k in range(30):
+        sim.update(sc.dt)
+        if orc.step(sc.dt):
+            rep, o = sim.last_refinement(), orc.last_report()
+            for key in ("merge_eligible", "merge_pairs", "split_candidates", "split_budget", "splits", "count_after"):
+                assert rep[key] == o[key], (k, key, rep[key], o[key])
+            assert sim.refinement_ids()["split_ids"].tolist() == o["split_ids"].tolist()
+            merges += rep["merge_pairs"]
+            splits += rep["splits"]
+        assert_state_bitexact(sim.read_state(), orc.arrays())
+    assert merges > 0 and splits > 0
+
+
+def _taylor_green_pair(n=16):
+    sc = scenes.taylor_green(n)
+    bd = StaticBoundaryDomain.empty(sc.parameters.domain)
+    N = sc.positions.shape[0]
+    sim = create_simulation(sc.parameters, sc.positions, None, None, bd, None, N, 1)
+    orc = oracle.OracleSim(sc.parameters, sc.positions, None, None, None, capacity=N)
+    st = sim.read_state()
+    st["vel"] = sc.velocities.copy()
+    sim.write_state(st, next_id=N)
+    a = orc.arrays()
+    a["vel"] = sc.velocities.copy()
+    orc.load(a, next_id=N)
+    return sc, sim, orc
+
+
+def test_taylor_green_periodic_morris_bitexact():
+    sc, sim, orc = _taylor_green_pair()
+    ke = []
+    for k in range(12):
+        sim.update(sc.dt)
+        orc.step(sc.dt)
+        if k % 4 == 3:
+            assert_state_bitexact(sim.read_state(), orc.arrays())
+        ke.append(sim.totals()["kinetic_energy"])
+    # viscous decay: kinetic energy falls monotonically in a periodic box without forcing
+    assert all(b < a for a, b in zip(ke, ke[1:]))
+    assert sim.device_errors() == 0
+
+
+def test_taylor_green_forces_against_fp64():
+    sc, sim, orc = _taylor_green_pair()
+    for _ in range(3):
+        sim.update(sc.dt)
+        orc.step(sc.dt)
+    from adaptivesph_gb300 import _lib
+
+    sim.run_stages(sc.dt, _lib.STAGE_FORCES)
+    orc.integrate(sc.dt)
+    orc.grid_build()
+    orc.rho[: orc.n] = orc.density32()
+    a32 = orc.forces32()
+    a64, scale = orc.forces64()
+    g = sim.read_state()
+    assert_bitexact("acc", g["acc"], a32)
+    err = np.abs(g["acc"][:, :3].astype(np.float64) - a64[:, :3]).max(axis=1)
+    assert (err / scale).max() <= 1e-5
+    rho64 = orc.density64()
+    assert (np.abs(g["rho"] - rho64) / rho64).max() <= 1e-5
+
+
+def test_cfl_step_matches_definition():
+    sc = small_dam_break()
+    sim, orc = make_pair(sc)
+    for _ in range(5):
+        sim.update(sc.dt)
+        orc.step(sc.dt)
+    v = orc.export_velocities()[:, :3].astype(np.float64)
+    h = orc.arrays()["h"].astype(np.float64)
+    want = 0.25 * np.min(h / (sc.parameters.speed_of_sound + np.linalg.norm(v, axis=1)))
+    dt = sim.step_cfl(0.25)
+    assert dt == pytest.approx(want, rel=1e-6)
+    orc.step(dt)
+    sim.synchronize()
+    assert_state_bitexact(sim.read_state(), orc.arrays())
+    # dt_max caps the step
+    dt2 = sim.step_cfl(0.25, dt_max=1e-7)
+    assert dt2 == np.float32(1e-7)
+
+
+def _tiny_pair(positions):
+    sc = small_dam_break()
+    p = dataclasses.replace(sc.parameters)
+    pos = np.zeros((len(positions), 4), np.float32)
+    pos[:, :3] = np.asarray(positions, np.float32)
+    bd = StaticBoundaryDomain.empty(p.domain)
+    n = pos.shape[0]
+    sim = create_simulation(p, pos, None, None, bd, None, n, 1)
+    orc = oracle.OracleSim(p, pos, None, None, None, capacity=n)
+    return sc, sim, orc
+
+
+@pytest.mark.parametrize("positions", [
+    [(0.30, 0.30, 0.20)],                            # one particle: its cell is skipped (density 0)
+    [(0.30, 0.30, 0.20), (0.31, 0.30, 0.20)],        # two particles in one cell: see each other
+    [(0.10, 0.30, 0.20), (0.50, 0.30, 0.20)],        # two cells: both skipped by the reference's quirk
+])
+def test_tiny_particle_counts_bitexact(positions):
+    sc, sim, orc = _tiny_pair(positions)
+    for _ in range(4):
+        sim.update(sc.dt)
+        orc.step(sc.dt)
+        assert_state_bitexact(sim.read_state(), orc.arrays())
+    info = sim.grid_info()
+    assert tuple(info["excluded_cells"]) == orc.excluded()
+
+
+def test_empty_boundary_bitexact():
+    sc = small_dam_break(walls=False)
+    sim, orc = make_pair(sc)
+    assert sim.get_boundary_particles_count() == 0
+    for _ in range(10):
+        sim.update(sc.dt)
+        orc.step(sc.dt)
+    assert_state_bitexact(sim.read_state(), orc.arrays())
+
+
+def test_split_capacity_limit_bitexact():
+    """A fluid capacity only a little above the particle count: splits stop at the capacity, like the oracle."""
+    sc0 = small_dam_break()
+    n = sc0.positions.shape[0]
+    ref = adaptive_refinement(capacity=n + 60)
+    sc = small_dam_break(refinement=ref)
+    sim, orc = make_pair(sc)
+    hit = False
+    for k in range(20):
+        sim.update(sc.dt)
+        if orc.step(sc.dt):
+            rep, o = sim.last_refinement(), orc.last_report()
+            assert rep["splits"] == o["splits"] and rep["count_after"] == o["count_after"]
+            hit |= bool(o["capacity_hit"])
+        assert_state_bitexact(sim.read_state(), orc.arrays())
+    assert hit, "the scene must reach the capacity"
+    assert sim.get_fluid_particles_count() <= n + 60
