@@ -27,9 +27,12 @@ struct StepArgs {
 // cnt[i] == kHeavyMark marks a particle whose query box spans more than 27 reference cells: queued in
 // heavy[0, *heavy_n) by the reorder kernel for the warp density kernel. A particle with more than maxe entries
 // (cnt[i] > maxe, the row overflowed) is queued in dover[0, *dover_n) by the density pass and its density summed by
-// the warp density kernel too. Both kinds are queued in fheavy for the warp force kernel.
+// the warp density kernel too. Both kinds are queued in fheavy for the warp force kernel, which walks their cells.
+// A particle with kRowHeavy < cnt[i] <= maxe entries (many neighbours) is summed over its row by one warp in both
+// passes (row entry e on lane e mod 32): queued in drow by the density pass and in frow by the row density kernel.
 constexpr uint32_t kHeavyMark = 0xffffffffu;
-constexpr uint32_t kListEntries = 64;  // entries per row
+constexpr uint32_t kListEntries = 256;  // entries per row
+constexpr uint32_t kRowHeavy = 32;      // rows longer than this are summed by a warp
 struct NbrDev {
     uint2* ent;
     uint32_t* cnt;
@@ -39,6 +42,10 @@ struct NbrDev {
     uint32_t* fheavy_n;
     uint32_t* dover;
     uint32_t* dover_n;
+    uint32_t* drow;
+    uint32_t* drow_n;
+    uint32_t* frow;
+    uint32_t* frow_n;
     uint32_t maxe;
 };
 
@@ -74,10 +81,11 @@ __global__ void k_boundary_reorder(GridDev g, const float4* pos_in, const float*
                                    uint8_t* refflag);
 // density and force passes (neighbour_kernels.cu): the ordinary kernel (one thread per particle) or the heavy
 // kernel (one warp per queued particle; for the density pass, over the box-heavy queue or the overflow queue)
-enum DensityKernel { kDensityOrdinary, kDensityHeavy, kDensityOverflow };
+enum DensityKernel { kDensityOrdinary, kDensityHeavy, kDensityOverflow, kDensityRow };
 cudaError_t launch_density(DensityKernel kind, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c,
                            BoundaryDev b, NbrDev nl);
-cudaError_t launch_forces(bool heavy, bool morris, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c,
+enum ForceKernel { kForcesOrdinary, kForcesHeavy, kForcesRow };
+cudaError_t launch_forces(ForceKernel kind, bool morris, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c,
                           BoundaryDev b, NbrDev nl);
 // number of reference cells of the query box [x - R, x + R] above which a particle is heavy
 constexpr int kHeavyCells = 27;

@@ -362,6 +362,10 @@ __global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, Boun
     }
     // remaining staged entries (fewer than a full segment)
     for (uint32_t q = 0; q < staged; ++q) row[cnt - staged + q] = st[q];
+    if (cnt > kRowHeavy) {  // many neighbours: summed over the row by a warp (k_density_row)
+        nl.drow[atomicAdd(nl.drow_n, 1u)] = i;
+        return;
+    }
     // the fluid sum over the row in canonical order (plain loads: the row was written by this thread)
     {
         uint2 next = cnt > 0u ? row[0] : make_uint2(0u, 0u);
@@ -422,7 +426,7 @@ __global__ void __launch_bounds__(256, 3) k_forces(StepArgs a, CellsDev c, Bound
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     const uint32_t cnt = nl.cnt[i];
-    if (cnt > nl.maxe) return;  // heavy or overflowed: k_forces_heavy
+    if (cnt > kRowHeavy) return;  // long row (k_forces_row), overflowed or heavy (k_forces_heavy)
     const ForceCtx x = force_ctx(a, i);
     ForceAcc f = {};
     // One neighbour per iteration (the row's masks expanded in order), so a warp runs as many iterations as its
@@ -478,6 +482,83 @@ __global__ void __launch_bounds__(256, 1) k_forces_heavy(StepArgs a, CellsDev c,
     }
 }
 
+// Particles with long rows (kRowHeavy < cnt <= maxe): one warp per particle, row entry e on lane e mod 32, each
+// lane expanding its entries' masks in order; lane sums combined by the butterfly.
+__device__ __forceinline__ void row_entry(const GridDev& g, uint2 en, uint32_t& first, uint32_t& mask, float& shx,
+                                          float& shy, float& shz) {
+    decode_entry(g, en.x, first, shx, shy, shz);
+    mask = en.y;
+}
+
+__global__ void __launch_bounds__(256, 2) k_density_row(StepArgs a, BoundaryDev b, NbrDev nl) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t nq = *nl.drow_n;
+    for (uint32_t w = warp; w < nq; w += nwarps) {
+        const uint32_t i = nl.drow[w];
+        const float4 pi = a.ph[i];
+        const uint32_t cnt = nl.cnt[i];
+        const uint2* row = nl.ent + (size_t)i * nl.maxe;
+        float rho = 0.0f;
+        for (uint32_t e = lane; e < cnt; e += 32) {
+            uint32_t first, mask;
+            float shx, shy, shz;
+            row_entry(a.grid, row[e], first, mask, shx, shy, shz);
+            while (mask != 0u) {
+                const uint32_t j = first + (uint32_t)(__ffs(mask) - 1);
+                mask &= mask - 1u;
+                density_term(a, pi, j, shx, shy, shz, rho);
+            }
+        }
+        rho = warp_sum_butterfly(rho);
+        const float R = pi.w + pi.w;
+        float rb = 0.0f;
+        if (boundary_near(a.grid, b, pi.x, pi.y, pi.z, R)) rb = warp_sum_butterfly(boundary_density<32>(a, b, i, pi, lane));
+        if (lane == 0) {
+            const float rh = rho + rb;
+            if (!isfinite(rh)) atomicOr(a.err, 0x2u);
+            a.rp[i] = make_float2(rh, pressure_term(rh, a.phys.rho0, a.phys.B));
+            nl.frow[atomicAdd(nl.frow_n, 1u)] = i;
+        }
+    }
+}
+
+template <bool kMorris>
+__global__ void __launch_bounds__(256, 2) k_forces_row(StepArgs a, BoundaryDev b, NbrDev nl) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t nq = *nl.frow_n;
+    for (uint32_t w = warp; w < nq; w += nwarps) {
+        const uint32_t i = nl.frow[w];
+        const ForceCtx x = force_ctx(a, i);
+        const uint32_t cnt = nl.cnt[i];
+        const uint2* row = nl.ent + (size_t)i * nl.maxe;
+        ForceAcc f = {};
+        for (uint32_t e = lane; e < cnt; e += 32) {
+            uint32_t first, mask;
+            float shx, shy, shz;
+            row_entry(a.grid, row[e], first, mask, shx, shy, shz);
+            while (mask != 0u) {
+                const uint32_t j = first + (uint32_t)(__ffs(mask) - 1);
+                mask &= mask - 1u;
+                if (j != i) force_term<kMorris>(a, x, j, shx, shy, shz, f);
+            }
+        }
+        if (boundary_near(a.grid, b, x.pi.x, x.pi.y, x.pi.z, x.hi + x.hi)) boundary_forces<32>(a, b, i, x, f, lane);
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            f.ap[q] = warp_sum_butterfly(f.ap[q]);
+            f.av[q] = warp_sum_butterfly(f.av[q]);
+            f.as[q] = warp_sum_butterfly(f.as[q]);
+            f.bp[q] = warp_sum_butterfly(f.bp[q]);
+            f.bf[q] = warp_sum_butterfly(f.bf[q]);
+        }
+        if (lane == 0) finish_force(a, i, x, f);
+    }
+}
+
 // The ordinary and the box-heavy kernels of a pass are independent of each other (the heavy queue is filled by the
 // reorder kernel), so the host runs them on two streams; the overflow queue is filled by k_density and summed
 // after it on its stream.
@@ -487,6 +568,8 @@ cudaError_t launch_density(DensityKernel kind, uint32_t blocks, cudaStream_t str
         k_density_heavy<<<blocks, 256, 0, stream>>>(a, c, b, nl, nl.heavy, nl.heavy_n);
     else if (kind == kDensityOverflow)
         k_density_heavy<<<blocks, 256, 0, stream>>>(a, c, b, nl, nl.dover, nl.dover_n);
+    else if (kind == kDensityRow)
+        k_density_row<<<blocks, 256, 0, stream>>>(a, b, nl);
     else if (a.grid.periodic)
         k_density<true><<<blocks, 256, 0, stream>>>(a, c, b, nl);
     else
@@ -494,13 +577,18 @@ cudaError_t launch_density(DensityKernel kind, uint32_t blocks, cudaStream_t str
     return cudaGetLastError();
 }
 
-cudaError_t launch_forces(bool heavy, bool morris, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c,
+cudaError_t launch_forces(ForceKernel kind, bool morris, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c,
                           BoundaryDev b, NbrDev nl) {
-    if (heavy) {
+    if (kind == kForcesHeavy) {
         if (morris)
             k_forces_heavy<true><<<blocks, 256, 0, stream>>>(a, c, b, nl);
         else
             k_forces_heavy<false><<<blocks, 256, 0, stream>>>(a, c, b, nl);
+    } else if (kind == kForcesRow) {
+        if (morris)
+            k_forces_row<true><<<blocks, 256, 0, stream>>>(a, b, nl);
+        else
+            k_forces_row<false><<<blocks, 256, 0, stream>>>(a, b, nl);
     } else {
         if (morris)
             k_forces<true><<<blocks, 256, 0, stream>>>(a, c, b, nl);

@@ -147,8 +147,10 @@ struct asph_simulation {
     uint32_t* heavy_idx = nullptr;  // [cap] queue of heavy particles of the current step
     uint32_t* heavy_n = nullptr;
     uint32_t* fheavy_idx = nullptr;  // [cap] queue of the force pass's warp kernel
-    uint32_t* fheavy_n = nullptr;  // [2]: force queue length, density overflow queue length
+    uint32_t* fheavy_n = nullptr;  // [4]: lengths of the fheavy, dover, drow and frow queues
     uint32_t* dover_idx = nullptr;  // [cap] particles whose list row overflowed in the density pass
+    uint32_t* drow_idx = nullptr;   // [cap] particles with long rows, density pass
+    uint32_t* frow_idx = nullptr;   // [cap] particles with long rows, force pass
     uint32_t* keys = nullptr;
     uint32_t* vals = nullptr;
     void* sort_mem = nullptr;
@@ -244,7 +246,8 @@ struct asph_simulation {
     CellsDev cells() const { return CellsDev{cell_start, cell_end, cell_hmax, hmax_ref, ex}; }
 
     NbrDev nbrs() const {
-        return NbrDev{nbr_ent, nbr_cnt, heavy_idx, heavy_n, fheavy_idx, fheavy_n, dover_idx, fheavy_n + 1, kListEntries};
+        return NbrDev{nbr_ent,  nbr_cnt,      heavy_idx, heavy_n,  fheavy_idx,   fheavy_n,    dover_idx,
+                      fheavy_n + 1, drow_idx, fheavy_n + 2, frow_idx, fheavy_n + 3, kListEntries};
     }
 
     BoundaryDev boundary() const {
@@ -534,17 +537,18 @@ asph_status build_grid(asph_simulation* s, bool integrate, float dt, bool carry_
 asph_status run_density(asph_simulation* s) {
     StepArgs a = s->args(s->cur);
     int h = s->tic();
-    CK(cudaMemsetAsync(s->fheavy_n, 0, 2 * sizeof(uint32_t), s->stream));
+    CK(cudaMemsetAsync(s->fheavy_n, 0, 4 * sizeof(uint32_t), s->stream));
     CK(cudaEventRecord(s->ev_fork, s->stream));
     CK(cudaStreamWaitEvent(s->aux, s->ev_fork, 0));
     CK(launch_density(kDensityHeavy, kHeavyBlocks, s->aux, a, s->cells(), s->boundary(), s->nbrs()));
     CK(launch_density(kDensityOrdinary, blocks_for(s->n), s->stream, a, s->cells(), s->boundary(), s->nbrs()));
     CK(launch_density(kDensityOverflow, kHeavyBlocks, s->stream, a, s->cells(), s->boundary(), s->nbrs()));
+    CK(launch_density(kDensityRow, kHeavyBlocks, s->stream, a, s->cells(), s->boundary(), s->nbrs()));
     CK(cudaEventRecord(s->ev_main, s->stream));
     CK(cudaEventRecord(s->ev_aux, s->aux));
     CK(cudaStreamWaitEvent(s->stream, s->ev_aux, 0));
     s->toc(h, ASPH_KERNEL_DENSITY);
-    s->launches += 3;
+    s->launches += 4;
     return ASPH_OK;
 }
 
@@ -552,13 +556,16 @@ asph_status run_forces(asph_simulation* s) {
     StepArgs a = s->args(s->cur);
     int h = s->tic();
     CK(cudaStreamWaitEvent(s->aux, s->ev_main, 0));
-    CK(launch_forces(true, s->phys.morris != 0, kHeavyBlocks, s->aux, a, s->cells(), s->boundary(), s->nbrs()));
-    CK(launch_forces(false, s->phys.morris != 0, blocks_for(s->n), s->stream, a, s->cells(), s->boundary(),
+    CK(launch_forces(kForcesHeavy, s->phys.morris != 0, kHeavyBlocks, s->aux, a, s->cells(), s->boundary(),
+                     s->nbrs()));
+    CK(launch_forces(kForcesOrdinary, s->phys.morris != 0, blocks_for(s->n), s->stream, a, s->cells(), s->boundary(),
+                     s->nbrs()));
+    CK(launch_forces(kForcesRow, s->phys.morris != 0, kHeavyBlocks, s->stream, a, s->cells(), s->boundary(),
                      s->nbrs()));
     CK(cudaEventRecord(s->ev_aux, s->aux));
     CK(cudaStreamWaitEvent(s->stream, s->ev_aux, 0));
     s->toc(h, ASPH_KERNEL_FORCES);
-    s->launches += 2;
+    s->launches += 3;
     return ASPH_OK;
 }
 
@@ -771,6 +778,8 @@ void destroy(asph_simulation* s) {
     dfree(s->fheavy_idx);
     dfree(s->fheavy_n);
     dfree(s->dover_idx);
+    dfree(s->drow_idx);
+    dfree(s->frow_idx);
     dfree(s->keys);
     dfree(s->vals);
     dfree(s->sort_mem);
@@ -1028,8 +1037,10 @@ asph_status asph_simulation_create(const asph_parameters* parameters, const floa
     TRY(dalloc(s->heavy_idx, C));
     TRY(dalloc(s->heavy_n, 1));
     TRY(dalloc(s->fheavy_idx, C));
-    TRY(dalloc(s->fheavy_n, 2));
+    TRY(dalloc(s->fheavy_n, 4));
     TRY(dalloc(s->dover_idx, C));
+    TRY(dalloc(s->drow_idx, C));
+    TRY(dalloc(s->frow_idx, C));
     const uint32_t sort_items = std::max(C, std::max(boundary_count, max_boundary_capacity));
     TRY(dalloc(s->keys, sort_items));
     TRY(dalloc(s->vals, sort_items));

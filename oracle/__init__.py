@@ -165,6 +165,7 @@ def lib():
                                    c_double_p]
         L.orc_neighbor_counts.argtypes = [P(OrcGrid), P(OrcState), P(OrcCells), c_u32_p]
         L.orc_list_entries.argtypes = [P(OrcGrid), P(OrcState), P(OrcCells), c_u32_p]
+        L.orc_sum_kinds.argtypes = [P(OrcGrid), P(OrcState), P(OrcCells), c_u32_p]
         L.orc32_refine.argtypes = [P(OrcGrid), P(OrcParams), P(OrcRefine), P(OrcState), P(OrcCells), P(OrcReport)]
         L.orc32_step.argtypes = [P(OrcGrid), P(OrcParams), P(OrcRefine), P(OrcState), P(OrcCells), P(OrcBoundary),
                                  ctypes.c_float, P(OrcReport)]
@@ -377,6 +378,11 @@ class OracleSim:
         out = np.zeros(max(self.n, 1), np.uint32)
         self.L.orc_list_entries(ctypes.byref(self.grid), ctypes.byref(self.state), ctypes.byref(self.cells),
                                 uptr(out))
+        return out[: self.n]
+
+    def sum_kinds(self) -> np.ndarray:
+        out = np.zeros(max(self.n, 1), np.uint32)
+        self.L.orc_sum_kinds(ctypes.byref(self.grid), ctypes.byref(self.state), ctypes.byref(self.cells), uptr(out))
         return out[: self.n]
 
     def _report_buffers(self):

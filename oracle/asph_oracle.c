@@ -474,7 +474,8 @@ float orc_cbrtf(float xf)
 static const float ORC_PI_F = 3.141592653589793f;
 #define ORC_LANES 32       /* lanes of the warp that sums a heavy particle */
 #define ORC_HEAVY_CELLS 27 /* query boxes of more reference cells than this are heavy */
-#define ORC_LIST_ENTRIES 64 /* neighbour-list row length in entries; a particle needing more is heavy */
+#define ORC_LIST_ENTRIES 256 /* neighbour-list row length in entries; a particle needing more is summed by cells */
+#define ORC_ROW_HEAVY 32     /* a particle with more row entries than this is summed over its row by a warp */
 
 /* Entries of the particle's neighbour-list row: the candidate cells' members are scanned in blocks of up to 32
  * (counted from each sub-cell's first member); a block in which the particle accepts a neighbour
@@ -505,6 +506,22 @@ static uint32_t list_entries(const orc_grid* g, const orc_state* s, const orc_ce
         }
     }
     return entries;
+}
+
+/* how a particle's sums are dealt to the lanes of a warp (see oracle_body.h) */
+enum { ORC_DEAL_NONE = 0, ORC_DEAL_SUBCELL = 1, ORC_DEAL_ENTRY = 2 };
+
+static int sum_kind(const orc_grid* g, const orc_state* s, const orc_cells* c, int64_t i)
+{
+    const float R = s->h[i] + s->h[i];
+    if (box_cells(g, s->pos + 4 * i, R) > ORC_HEAVY_CELLS) {
+        return ORC_DEAL_SUBCELL;
+    }
+    const uint32_t n = list_entries(g, s, c, i);
+    if (n > ORC_LIST_ENTRIES) {
+        return ORC_DEAL_SUBCELL;
+    }
+    return n > ORC_ROW_HEAVY ? ORC_DEAL_ENTRY : ORC_DEAL_NONE;
 }
 
 #define REAL float
@@ -1325,4 +1342,14 @@ void orc_icosahedron(float* out36)
     float v[12][3];
     icosahedron(v);
     memcpy(out36, v, sizeof(v));
+}
+
+/* how each particle's sums are dealt (0 sequential, 1 by sub-cell, 2 by row entry); for tests */
+void orc_sum_kinds(const orc_grid* g, const orc_state* s, const orc_cells* c, uint32_t* out)
+{
+    const int64_t n = s->n;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < n; i++) {
+        out[i] = (uint32_t)sum_kind(g, s, c, i);
+    }
 }

@@ -123,6 +123,9 @@ void orc32_forces(const orc_grid* g, const orc_params* P, const orc_state* s, co
 void orc_neighbor_counts(const orc_grid* g, const orc_state* s, const orc_cells* c, uint32_t* counts);
 /* entries of each particle's neighbour-list row (blocks of <= 32 sub-cell members holding an accepted neighbour) */
 void orc_list_entries(const orc_grid* g, const orc_state* s, const orc_cells* c, uint32_t* out);
+/* how each particle's sums are dealt to a warp's lanes: 0 sequential, 1 by sub-cell (heavy box or overflowed
+ * row), 2 by row entry (long row) */
+void orc_sum_kinds(const orc_grid* g, const orc_state* s, const orc_cells* c, uint32_t* out);
 /* one refinement pass (AdaptiveSphSimulation.cu:102-252); s must be cell-sorted with valid c */
 void orc32_refine(const orc_grid* g, const orc_params* P, const orc_refine* R, orc_state* s, orc_cells* c,
                   orc_report* rep);

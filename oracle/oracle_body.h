@@ -18,15 +18,15 @@
  * the cancellation of powf(...)-1; directions are offset * (1/r); per-pair force terms are a scalar
  * s times the direction, accumulated with fma.
  *
- * Summation order: neighbours are summed in the canonical visiting order of the candidate cells. A particle
- * whose query box spans more than ORC_HEAVY_CELLS reference cells ("heavy", after merges made h large) is summed
- * as the GPU sums it with one warp: the box's sub-cell with canonical index t (see orc_iter.t) goes to lane
- * t mod 32, each lane sums the members of its sub-cells in the canonical order, and the 32 partial sums are
- * combined by the butterfly
- * s_l <- s_l + s_(l xor o) for o = 16, 8, 4, 2, 1. Its boundary terms are dealt by member instead: member k of
- * each visited boundary cell (counted from the cell's first member) goes to lane k mod 32. A particle whose
- * neighbour-list row would need more than ORC_LIST_ENTRIES entries (see list_entries) is summed the same way, in
- * both passes.
+ * Summation order (sum_kind): neighbours are summed in the canonical visiting order of the candidate cells. Three
+ * kinds of particles are summed as the GPU sums them with one warp, each lane summing its share in the canonical
+ * order and the 32 partial sums combined by the butterfly s_l <- s_l + s_(l xor o) for o = 16, 8, 4, 2, 1:
+ *   - a particle whose query box spans more than ORC_HEAVY_CELLS reference cells ("heavy", after merges made h
+ *     large), or whose neighbour-list row would need more than ORC_LIST_ENTRIES entries: the box's sub-cell with
+ *     canonical index t (see orc_iter.t) goes to lane t mod 32;
+ *   - a particle whose row has more than ORC_ROW_HEAVY entries (many neighbours): row entry e goes to lane e mod 32.
+ * Their boundary terms are dealt by member: member k of each visited boundary cell (counted from the cell's first
+ * member) goes to lane k mod 32.
  */
 
 /* W(r, h) with precomputed 1/h and coef/h^3 */
@@ -95,47 +95,61 @@ static REAL F(butterfly)(REAL* s)
     return s[0];
 }
 
-/* fluid part of the density of particle i over the cells of lane `lane` of `lanes` */
-static REAL F(density_fluid)(const orc_grid* g, const orc_state* s, const orc_cells* c, int64_t i, int lanes,
-                             int lane)
+/* Fluid part of the density of particle i into out[lanes]. The members of each visited sub-cell are taken in blocks
+ * of up to 32 (the blocks of the neighbour-list row, see list_entries). deal = ORC_DEAL_SUBCELL: the box's sub-cell
+ * t goes to lane t mod lanes; ORC_DEAL_ENTRY: the e-th block holding an accepted neighbour (row entry e) goes to
+ * lane e mod lanes; lanes = 1 is the sequential sum. */
+static void F(density_fluid)(const orc_grid* g, const orc_state* s, const orc_cells* c, int64_t i, int deal,
+                             int lanes, REAL* out)
 {
     const float* pi = s->pos + 4 * i;
     const REAL xi = pi[0], yi = pi[1], zi = pi[2];
     const float R = s->h[i] + s->h[i];
-    REAL rho = 0;
+    for (int l = 0; l < lanes; l++) {
+        out[l] = 0;
+    }
+    uint32_t e = 0;
     orc_iter it;
     uint32_t jb, je;
     float sh[3];
     it_init(&it, g, c->start, c->end, c->ex, pi, R);
     while (it_next(&it, &jb, &je, sh)) {
-        if (it.t % (uint32_t)lanes != (uint32_t)lane) {
-            continue;
-        }
-        for (uint32_t j = jb; j < je; j++) {
-            const float* pj = s->pos + 4 * (size_t)j;
-            const REAL dx = NBR(pj, 0) - xi;
-            const REAL dy = NBR(pj, 1) - yi;
-            const REAL dz = NBR(pj, 2) - zi;
-            const REAL r2 = F(dist2)(dx, dy, dz);
-            const REAL hj = s->h[j];
-            const REAL twoh = hj + hj;
-            if (r2 > twoh * twoh) {
-                continue;
+        for (uint32_t blk0 = jb; blk0 < je; blk0 += 32) {
+            const uint32_t blk1 = je - blk0 < 32u ? je : blk0 + 32u;
+            REAL* rho = out + (deal == ORC_DEAL_ENTRY ? e : it.t) % (uint32_t)lanes;
+            int any = 0;
+            for (uint32_t j = blk0; j < blk1; j++) {
+                const float* pj = s->pos + 4 * (size_t)j;
+                const REAL dx = NBR(pj, 0) - xi;
+                const REAL dy = NBR(pj, 1) - yi;
+                const REAL dz = NBR(pj, 2) - zi;
+                const REAL r2 = F(dist2)(dx, dy, dz);
+                const REAL hj = s->h[j];
+                const REAL twoh = hj + hj;
+                if (r2 > twoh * twoh) {
+                    continue;
+                }
+                any = 1;
+                REAL invh, wc, dwc;
+                F(kernel_consts)(hj, &invh, &wc, &dwc);
+                const REAL w = F(kernel_w)(SQRT(r2), invh, wc);
+                *rho = FMA((REAL)s->m[j], w, *rho);
             }
-            REAL invh, wc, dwc;
-            F(kernel_consts)(hj, &invh, &wc, &dwc);
-            const REAL w = F(kernel_w)(SQRT(r2), invh, wc);
-            rho = FMA((REAL)s->m[j], w, rho);
+            e += (uint32_t)any;
         }
     }
-    return rho;
 }
 
-static REAL F(density_boundary)(const orc_grid* g, const orc_state* s, const orc_boundary* b, int64_t i,
-                                int lanes, int lane)
+/* boundary part of the density into out[lanes]: member k of each boundary cell (counted from its first member) on
+ * lane k mod lanes */
+static void F(density_boundary)(const orc_grid* g, const orc_state* s, const orc_boundary* b, int64_t i,
+                                int lanes, REAL* out)
 {
+    for (int l = 0; l < lanes; l++) {
+        out[l] = 0;
+    }
     if (b == NULL || b->n == 0) {
-        return 0;
+        return;
     }
     const float* pi = s->pos + 4 * i;
     const REAL xi = pi[0], yi = pi[1], zi = pi[2];
@@ -145,13 +159,13 @@ static REAL F(density_boundary)(const orc_grid* g, const orc_state* s, const orc
     F(kernel_consts)(hi, &invh, &wc, &dwc);
     const REAL twoh = hi + hi;
     const REAL cut = twoh * twoh;
-    REAL rb = 0;
     orc_iter it;
     uint32_t jb, je;
     float sh[3];
     it_init(&it, g, b->start, b->end, b->ex, pi, R);
     while (it_next(&it, &jb, &je, sh)) {
-        for (uint32_t k = jb + (uint32_t)lane; k < je; k += (uint32_t)lanes) {
+        for (uint32_t k = jb; k < je; k++) {
+            REAL* rb = out + (k - jb) % (uint32_t)lanes;
             const float* pb = b->pos + 4 * (size_t)k;
             const REAL dx = NBR(pb, 0) - xi;
             const REAL dy = NBR(pb, 1) - yi;
@@ -161,10 +175,9 @@ static REAL F(density_boundary)(const orc_grid* g, const orc_state* s, const orc
                 continue;
             }
             const REAL w = F(kernel_w)(SQRT(r2), invh, wc);
-            rb = FMA((REAL)b->psi[k], w, rb);
+            *rb = FMA((REAL)b->psi[k], w, *rb);
         }
     }
-    return rb;
 }
 
 void F(orc_density_impl)(const orc_grid* g, const orc_params* P, const orc_state* s, const orc_cells* c,
@@ -174,19 +187,17 @@ void F(orc_density_impl)(const orc_grid* g, const orc_params* P, const orc_state
     const int64_t n = s->n;
 #pragma omp parallel for schedule(dynamic, 256)
     for (int64_t i = 0; i < n; i++) {
-        const float R = s->h[i] + s->h[i];
         REAL rho, rb;
-        if (box_cells(g, s->pos + 4 * i, R) > ORC_HEAVY_CELLS || list_entries(g, s, c, i) > ORC_LIST_ENTRIES) {
+        const int deal = sum_kind(g, s, c, i);
+        if (deal != ORC_DEAL_NONE) {
             REAL pf[ORC_LANES], pb[ORC_LANES];
-            for (int l = 0; l < ORC_LANES; l++) {
-                pf[l] = F(density_fluid)(g, s, c, i, ORC_LANES, l);
-                pb[l] = F(density_boundary)(g, s, b, i, ORC_LANES, l);
-            }
+            F(density_fluid)(g, s, c, i, deal, ORC_LANES, pf);
+            F(density_boundary)(g, s, b, i, ORC_LANES, pb);
             rho = F(butterfly)(pf);
             rb = F(butterfly)(pb);
         } else {
-            rho = F(density_fluid)(g, s, c, i, 1, 0);
-            rb = F(density_boundary)(g, s, b, i, 1, 0);
+            F(density_fluid)(g, s, c, i, ORC_DEAL_NONE, 1, &rho);
+            F(density_boundary)(g, s, b, i, 1, &rb);
         }
         rho_out[i] = rho + rb;
     }
@@ -198,8 +209,10 @@ typedef struct F(facc) {
     double scale;
 } F(facc);
 
+/* force terms of particle i into fl[lanes], the fluid blocks dealt as in density_fluid, boundary member k of each
+ * boundary cell on lane k mod lanes */
 static void F(forces_part)(const orc_grid* g, const orc_params* P, const orc_state* s, const orc_cells* c,
-                           const orc_boundary* b, const float* rho_in, int64_t i, int lanes, int lane, F(facc) * f)
+                           const orc_boundary* b, const float* rho_in, int64_t i, int deal, int lanes, F(facc) * fl)
 {
     const REAL rho0 = P->rho0, c0 = P->c0;
     const REAL alpha = P->alpha, nu_k = P->nu;
@@ -216,85 +229,91 @@ static void F(forces_part)(const orc_grid* g, const orc_params* P, const orc_sta
     const REAL Ki = (((REAL)2 * alpha) * hi) * c0;
     const REAL ei = ((REAL)0.01 * hi) * hi;
     const float R = s->h[i] + s->h[i];
-    memset(f, 0, sizeof(*f));
+    memset(fl, 0, sizeof(*fl) * (size_t)lanes);
+    uint32_t e = 0;
     orc_iter it;
     uint32_t jb, je;
     float sh[3];
     it_init(&it, g, c->start, c->end, c->ex, pi, R);
     while (it_next(&it, &jb, &je, sh)) {
-        if (it.t % (uint32_t)lanes != (uint32_t)lane) {
-            continue;
-        }
-        for (uint32_t j = jb; j < je; j++) {
-            if ((int64_t)j == i) {
-                continue;
-            }
-            const float* pj = s->pos + 4 * (size_t)j;
-            const REAL dx = xi - NBR(pj, 0);
-            const REAL dy = yi - NBR(pj, 1);
-            const REAL dz = zi - NBR(pj, 2);
-            const REAL r2 = F(dist2)(dx, dy, dz);
-            const REAL hj = s->h[j];
-            const REAL twoh = hj + hj;
-            if (r2 > twoh * twoh) {
-                continue;
-            }
-            REAL invh, wc, dwc;
-            F(kernel_consts)(hj, &invh, &wc, &dwc);
-            const REAL r = SQRT(r2);
-            REAL u[3];
-            if (r > (REAL)0) {
-                const REAL ir = (REAL)1 / r;
-                u[0] = dx * ir;
-                u[1] = dy * ir;
-                u[2] = dz * ir;
-            } else {
-                u[0] = 0;
-                u[1] = 1;
-                u[2] = 0;
-            }
-            const REAL dw = F(kernel_dw)(r, invh, dwc);
-            const REAL mj = s->m[j];
-            const REAL rhoj = rho_in[j];
-            const REAL ptj = F(pressure_term)(rhoj, rho0, c0);
-            {
-                const REAL sp = (mj * dw) * (pti + ptj);
-                for (int a = 0; a < 3; a++) {
-                    f->ap[a] = FMA(-sp, u[a], f->ap[a]);
+        for (uint32_t blk0 = jb; blk0 < je; blk0 += 32) {
+            const uint32_t blk1 = je - blk0 < 32u ? je : blk0 + 32u;
+            F(facc)* f = fl + (deal == ORC_DEAL_ENTRY ? e : it.t) % (uint32_t)lanes;
+            int any = 0;
+            for (uint32_t j = blk0; j < blk1; j++) {
+                if ((int64_t)j == i) {
+                    any = 1; /* the particle itself is accepted (its row holds it) but adds no force */
+                    continue;
                 }
-                f->scale += fabs((double)sp);
-            }
-            if (visc_on) {
-                const float* vj4 = s->vel + 4 * (size_t)j;
-                const REAL vd[3] = {vxi - (REAL)vj4[0], vyi - (REAL)vj4[1], vzi - (REAL)vj4[2]};
-                if (!morris) {
-                    const REAL comp = FMA(vd[2], dz, FMA(vd[1], dy, vd[0] * dx));
-                    if (comp < (REAL)0) {
-                        const REAL nuij = Ki / (rhoi + rhoj);
-                        const REAL piv = (-nuij * comp) / (r2 + ei);
-                        const REAL sv = (mj * piv) * dw;
-                        for (int a = 0; a < 3; a++) {
-                            f->av[a] = FMA(-sv, u[a], f->av[a]);
-                        }
-                        f->scale += fabs((double)sv);
-                    }
+                const float* pj = s->pos + 4 * (size_t)j;
+                const REAL dx = xi - NBR(pj, 0);
+                const REAL dy = yi - NBR(pj, 1);
+                const REAL dz = zi - NBR(pj, 2);
+                const REAL r2 = F(dist2)(dx, dy, dz);
+                const REAL hj = s->h[j];
+                const REAL twoh = hj + hj;
+                if (r2 > twoh * twoh) {
+                    continue;
+                }
+                any = 1;
+                REAL invh, wc, dwc;
+                F(kernel_consts)(hj, &invh, &wc, &dwc);
+                const REAL r = SQRT(r2);
+                REAL u[3];
+                if (r > (REAL)0) {
+                    const REAL ir = (REAL)1 / r;
+                    u[0] = dx * ir;
+                    u[1] = dy * ir;
+                    u[2] = dz * ir;
                 } else {
-                    const REAL coef = ((mj * nu_k) * (rhoi + rhoj)) / (rhoi * rhoj);
-                    const REAL sv = coef * ((r * dw) / (r2 + ei));
+                    u[0] = 0;
+                    u[1] = 1;
+                    u[2] = 0;
+                }
+                const REAL dw = F(kernel_dw)(r, invh, dwc);
+                const REAL mj = s->m[j];
+                const REAL rhoj = rho_in[j];
+                const REAL ptj = F(pressure_term)(rhoj, rho0, c0);
+                {
+                    const REAL sp = (mj * dw) * (pti + ptj);
                     for (int a = 0; a < 3; a++) {
-                        f->av[a] = FMA(sv, vd[a], f->av[a]);
+                        f->ap[a] = FMA(-sp, u[a], f->ap[a]);
                     }
-                    f->scale +=
-                        fabs((double)sv) * sqrt((double)vd[0] * vd[0] + (double)vd[1] * vd[1] + (double)vd[2] * vd[2]);
+                    f->scale += fabs((double)sp);
+                }
+                if (visc_on) {
+                    const float* vj4 = s->vel + 4 * (size_t)j;
+                    const REAL vd[3] = {vxi - (REAL)vj4[0], vyi - (REAL)vj4[1], vzi - (REAL)vj4[2]};
+                    if (!morris) {
+                        const REAL comp = FMA(vd[2], dz, FMA(vd[1], dy, vd[0] * dx));
+                        if (comp < (REAL)0) {
+                            const REAL nuij = Ki / (rhoi + rhoj);
+                            const REAL piv = (-nuij * comp) / (r2 + ei);
+                            const REAL sv = (mj * piv) * dw;
+                            for (int a = 0; a < 3; a++) {
+                                f->av[a] = FMA(-sv, u[a], f->av[a]);
+                            }
+                            f->scale += fabs((double)sv);
+                        }
+                    } else {
+                        const REAL coef = ((mj * nu_k) * (rhoi + rhoj)) / (rhoi * rhoj);
+                        const REAL sv = coef * ((r * dw) / (r2 + ei));
+                        for (int a = 0; a < 3; a++) {
+                            f->av[a] = FMA(sv, vd[a], f->av[a]);
+                        }
+                        f->scale +=
+                            fabs((double)sv) * sqrt((double)vd[0] * vd[0] + (double)vd[1] * vd[1] + (double)vd[2] * vd[2]);
+                    }
+                }
+                if (sigma_on) {
+                    const REAL ss = mj * F(kernel_w)(r, invh, wc);
+                    for (int a = 0; a < 3; a++) {
+                        f->as[a] = FMA(ss, u[a], f->as[a]);
+                    }
+                    f->scale += fabs((double)((REAL)P->sigma / mi) * (double)ss);
                 }
             }
-            if (sigma_on) {
-                const REAL ss = mj * F(kernel_w)(r, invh, wc);
-                for (int a = 0; a < 3; a++) {
-                    f->as[a] = FMA(ss, u[a], f->as[a]);
-                }
-                f->scale += fabs((double)((REAL)P->sigma / mi) * (double)ss);
-            }
+            e += (uint32_t)any;
         }
     }
     if (b != NULL && b->n > 0) {
@@ -304,7 +323,8 @@ static void F(forces_part)(const orc_grid* g, const orc_params* P, const orc_sta
         const REAL cut = twoh * twoh;
         it_init(&it, g, b->start, b->end, b->ex, pi, R);
         while (it_next(&it, &jb, &je, sh)) {
-            for (uint32_t k = jb + (uint32_t)lane; k < je; k += (uint32_t)lanes) {
+            for (uint32_t k = jb; k < je; k++) {
+                F(facc)* f = fl + (k - jb) % (uint32_t)lanes;
                 const float* pb = b->pos + 4 * (size_t)k;
                 const REAL dx = xi - NBR(pb, 0);
                 const REAL dy = yi - NBR(pb, 1);
@@ -357,13 +377,11 @@ void F(orc_forces_impl)(const orc_grid* g, const orc_params* P, const orc_state*
     const int sigma_on = P->sigma != 0.0f;
 #pragma omp parallel for schedule(dynamic, 256)
     for (int64_t i = 0; i < n; i++) {
-        const float R = s->h[i] + s->h[i];
         F(facc) f;
-        if (box_cells(g, s->pos + 4 * i, R) > ORC_HEAVY_CELLS || list_entries(g, s, c, i) > ORC_LIST_ENTRIES) {
+        const int deal = sum_kind(g, s, c, i);
+        if (deal != ORC_DEAL_NONE) {
             F(facc) part[ORC_LANES];
-            for (int l = 0; l < ORC_LANES; l++) {
-                F(forces_part)(g, P, s, c, b, rho_in, i, ORC_LANES, l, &part[l]);
-            }
+            F(forces_part)(g, P, s, c, b, rho_in, i, deal, ORC_LANES, part);
             memset(&f, 0, sizeof(f));
             REAL t[ORC_LANES];
 #define ORC_REDUCE(field, a)                       \
@@ -383,7 +401,7 @@ void F(orc_forces_impl)(const orc_grid* g, const orc_params* P, const orc_state*
                 f.scale += part[l].scale;
             }
         } else {
-            F(forces_part)(g, P, s, c, b, rho_in, i, 1, 0, &f);
+            F(forces_part)(g, P, s, c, b, rho_in, i, ORC_DEAL_NONE, 1, &f);
         }
         REAL ax = P->gravity[0], ay = P->gravity[1], az = P->gravity[2];
         ax = ax + f.ap[0];

@@ -10,7 +10,7 @@ as well; in addition FP32 results are checked against the FP64 restatement:
 import numpy as np
 import pytest
 
-from adaptivesph_gb300 import _lib
+from adaptivesph_gb300 import _lib, scenes
 from helpers import (adaptive_refinement, assert_bitexact, assert_state_bitexact, make_pair, small_dam_break)
 
 pytestmark = pytest.mark.gpu
@@ -93,7 +93,7 @@ def test_forces_bitexact_and_fp64():
 
 def _mixed_h_state(sim, orc, sc, seed=7):
     """State with smoothing lengths h0, 1.5 h0, 3 h0 and 6 h0 mixed at random: large boxes (heavy particles, one
-    warp each) and neighbour counts above the list row length (overflow, warp force pass) both occur."""
+    warp each walking the cells) and long neighbour rows (one warp each over the row) both occur."""
     st = sim.read_state()
     rng = np.random.default_rng(seed)
     h0 = np.float32(sc.parameters.base_smoothing_radius)
@@ -112,12 +112,12 @@ def test_mixed_smoothing_lengths_bitexact():
     sim.run_stages(sc.dt, _lib.STAGE_FORCES)
     orc.integrate(sc.dt)
     orc.grid_build()
-    entries = orc.list_entries()
+    kinds = np.bincount(orc.sum_kinds(), minlength=3)
     orc.rho[: orc.n] = orc.density32()
     g = sim.read_state()
     assert_bitexact("rho", g["rho"], orc.rho[: orc.n])
     assert_bitexact("acc", g["acc"], orc.forces32())
-    assert entries.max() > 64, "the state must overflow a neighbour-list row"
+    assert kinds[1] > 0 and kinds[2] > 0, ("heavy boxes and long rows must both occur", kinds)
     a64, scale = orc.forces64()
     err = np.abs(g["acc"][:, :3].astype(np.float64) - a64[:, :3]).max(axis=1)
     assert (err / scale).max() <= FORCE_RTOL, (err / scale).max()
@@ -242,3 +242,30 @@ def test_refinement_with_large_smoothing_lengths_bitexact():
     assert sorted(ids["keep_ids"].tolist()) == sorted(o["keep_ids"].tolist())
     assert sorted(ids["removed_ids"].tolist()) == sorted(o["removed_ids"].tolist())
     assert_state_bitexact(sim.read_state(), orc.arrays())
+
+
+def test_every_summation_kind_bitexact():
+    """A dense lattice (h = 2.6 dx, so sub-cells hold over 100 members) with mostly 3 h0 particles: heavy boxes,
+    overflowed rows (more than 256 entries), long rows and ordinary particles all occur in one pass."""
+    sc = scenes.dam_break((24, 24, 24), 0.02, seed=11, tank=(0.7, 0.7, 0.7), h_ratio=2.6)
+    sim, orc = make_pair(sc)
+    st = sim.read_state()
+    rng = np.random.default_rng(7)
+    h0 = np.float32(sc.parameters.base_smoothing_radius)
+    choice = rng.choice(4, size=st["h"].shape[0], p=[0.3, 0.1, 0.5, 0.1])
+    st["h"] = (h0 * np.array([1.0, 2.0, 3.0, 1.5], np.float32)[choice]).astype(np.float32)
+    sim.write_state(st, frame=5, next_id=int(st["id"].max()) + 1, pending_half=sc.dt / 2)
+    orc.load(st, frame=5, next_id=int(st["id"].max()) + 1, pending_half=sc.dt / 2)
+    sim.run_stages(sc.dt, _lib.STAGE_FORCES)
+    orc.integrate(sc.dt)
+    orc.grid_build()
+    kinds = np.bincount(orc.sum_kinds(), minlength=3)
+    entries = orc.list_entries()
+    assert kinds.min() > 10 and (entries > 256).sum() > 10, (kinds, int((entries > 256).sum()))
+    orc.rho[: orc.n] = orc.density32()
+    g = sim.read_state()
+    assert_bitexact("rho", g["rho"], orc.rho[: orc.n])
+    assert_bitexact("acc", g["acc"], orc.forces32())
+    a64, scale = orc.forces64()
+    err = np.abs(g["acc"][:, :3].astype(np.float64) - a64[:, :3]).max(axis=1)
+    assert (err / scale).max() <= FORCE_RTOL, (err / scale).max()
