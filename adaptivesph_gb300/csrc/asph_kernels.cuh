@@ -32,7 +32,7 @@ struct StepArgs {
 // passes (row entry e on lane e mod 32): queued in drow by the density pass and in frow by the row density kernel.
 constexpr uint32_t kHeavyMark = 0xffffffffu;
 constexpr uint32_t kListEntries = 256;  // entries per row
-constexpr uint32_t kRowHeavy = 32;      // rows longer than this are summed by a warp
+constexpr uint32_t kRowHeavy = 96;      // rows longer than this are summed by a warp
 struct NbrDev {
     uint2* ent;
     uint32_t* cnt;
