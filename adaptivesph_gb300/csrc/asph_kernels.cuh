@@ -30,7 +30,14 @@ struct StepArgs {
 // the warp density kernel too. Both kinds are queued in fheavy for the warp force kernel, which walks their cells.
 // A particle with kRowHeavy < cnt[i] <= maxe entries (many neighbours) is summed over its row by one warp in both
 // passes (row entry e on lane e mod 32): queued in drow by the density pass and in frow by the row density kernel.
+// A box-heavy particle at heavy-queue position w < pool_slots also keeps its accepted blocks for the force pass:
+// lane l of the warp that sums its density stores the blocks of its own sub-cells, in its visiting order, at
+// pool[(w * 32 + l) * kPoolLaneEntries ...] with their number at pool_cnt[w * 32 + l], and cnt[i] = kPooled | w.
+// If a lane has more than kPoolLaneEntries such blocks, cnt[i] = kHeavyMark and the force pass walks the cells.
 constexpr uint32_t kHeavyMark = 0xffffffffu;
+constexpr uint32_t kPooled = 0x80000000u;
+constexpr uint32_t kPoolLaneEntries = 32;
+constexpr uint32_t kPoolSlots = 8192;
 constexpr uint32_t kListEntries = 256;  // entries per row
 constexpr uint32_t kRowHeavy = 96;      // rows longer than this are summed by a warp
 struct NbrDev {
@@ -46,6 +53,9 @@ struct NbrDev {
     uint32_t* drow_n;
     uint32_t* frow;
     uint32_t* frow_n;
+    uint2* pool;
+    uint32_t* pool_cnt;
+    uint32_t pool_slots;
     uint32_t maxe;
 };
 

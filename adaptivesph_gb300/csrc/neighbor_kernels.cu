@@ -54,6 +54,13 @@ __device__ __forceinline__ void decode_entry(const GridDev& g, uint32_t e, uint3
     shz = cz == 0 ? -g.scale[2] : (cz == 2 ? g.scale[2] : 0.0f);
 }
 
+// A row entry: first member (and periodic image offset) and acceptance mask of a block.
+__device__ __forceinline__ void row_entry(const GridDev& g, uint2 en, uint32_t& first, uint32_t& mask, float& shx,
+                                          float& shy, float& shz) {
+    decode_entry(g, en.x, first, shx, shy, shz);
+    mask = en.y;
+}
+
 __device__ __forceinline__ float warp_sum_butterfly(float v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v = v + __shfl_xor_sync(0xffffffffu, v, o);
@@ -82,6 +89,17 @@ __device__ __forceinline__ bool boundary_near(const GridDev& g, const BoundaryDe
                 if (__ldg(b.refflag + cx + g.gs[0] * (cy + g.gs[1] * cz))) return true;
             }
     return false;
+}
+
+// The support test r^2 <= (2 h_j)^2 of neighbour position pj (periodic image offset applied) for p.
+__device__ __forceinline__ bool supported(const GridDev& g, float4 p, float4 pj, float shx, float shy, float shz) {
+    const bool periodic = g.periodic;
+    const float xj = periodic ? pj.x + shx : pj.x;
+    const float yj = periodic ? pj.y + shy : pj.y;
+    const float zj = periodic ? pj.z + shz : pj.z;
+    const float dx = xj - p.x, dy = yj - p.y, dz = zj - p.z;
+    const float twoh = pj.w + pj.w;
+    return dist2(dx, dy, dz) <= twoh * twoh;
 }
 
 // Fluid density term of neighbour j (Algorithm.cu:29-51); false when j fails r^2 <= (2 h_j)^2.
@@ -300,10 +318,7 @@ __global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, Boun
     const float4 pi = in ? a.ph[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const float R = pi.w + pi.w;
     bool active = in;
-    if (in && box_cells(a.grid, pi, R) > kHeavyCells) {  // queued by the reorder kernel for k_density_heavy
-        nl.cnt[i] = kHeavyMark;
-        active = false;
-    }
+    if (in && box_cells(a.grid, pi, R) > kHeavyCells) active = false;  // k_density_heavy (sets cnt[i])
     constexpr bool periodic = kPeriodic;
     uint2* row = nl.ent + (size_t)(in ? i : 0) * nl.maxe;
     uint2* st = stage + threadIdx.x * kStageStride;
@@ -393,20 +408,46 @@ __global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, Boun
 
 // Density of the heavy particles: one warp per particle.
 __global__ void __launch_bounds__(256, 1) k_density_heavy(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl,
-                                                          const uint32_t* queue, const uint32_t* queue_n) {
+                                                          const uint32_t* queue, const uint32_t* queue_n, bool pooled) {
     const int lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     const uint32_t nh = *queue_n;
+    const bool periodic = a.grid.periodic;
     for (uint32_t w = warp; w < nh; w += nwarps) {
         const uint32_t i = queue[w];
         const float4 pi = a.ph[i];
         const float R = pi.w + pi.w;
+        const bool keep = pooled && w < nl.pool_slots;
+        uint2* seg = keep ? nl.pool + ((size_t)w * 32 + lane) * kPoolLaneEntries : nullptr;
+        uint32_t kept = 0;
         float rho = 0.0f;
         for_each_subcell_lane(a.grid, c.start, c.end, c.hmax, c.ex[0], c.ex[1], pi.x, pi.y, pi.z, R, 0.0f, lane,
                               [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
-                                  for (uint32_t j = jb; j < je; ++j) density_term(a, pi, j, shx, shy, shz, rho);
+                                  const uint32_t code = periodic ? (shift_code(shx, shy, shz) << kIdxBits) : 0u;
+                                  for (uint32_t c0 = jb; c0 < je; c0 += 32) {
+                                      const uint32_t cn = je - c0 < 32u ? je - c0 : 32u;
+                                      uint32_t mask = 0;
+                                      for (int k = (int)cn - 1; k >= 0; --k)
+                                          mask = (mask << 1) |
+                                                 (supported(a.grid, pi, __ldg(a.ph + c0 + k), shx, shy, shz) ? 1u : 0u);
+                                      if (mask == 0u) continue;
+                                      if (keep) {
+                                          if (kept < kPoolLaneEntries) seg[kept] = make_uint2(c0 | code, mask);
+                                          kept++;
+                                      }
+                                      while (mask != 0u) {
+                                          const uint32_t k = (uint32_t)(__ffs(mask) - 1);
+                                          mask &= mask - 1u;
+                                          density_term(a, pi, c0 + k, shx, shy, shz, rho);
+                                      }
+                                  }
                               });
+        if (pooled) {
+            const bool fits = keep && !__any_sync(0xffffffffu, kept > kPoolLaneEntries);
+            if (fits) nl.pool_cnt[(size_t)w * 32 + lane] = kept;
+            if (lane == 0) nl.cnt[i] = fits ? (kPooled | w) : kHeavyMark;
+        }
         rho = warp_sum_butterfly(rho);
         float rb = 0.0f;
         if (boundary_near(a.grid, b, pi.x, pi.y, pi.z, R)) rb = warp_sum_butterfly(boundary_density<32>(a, b, i, pi, lane));
@@ -462,13 +503,32 @@ __global__ void __launch_bounds__(256, 1) k_forces_heavy(StepArgs a, CellsDev c,
         const uint32_t i = nl.fheavy[w];
         const ForceCtx x = force_ctx(a, i);
         ForceAcc f = {};
-        for_each_subcell_lane(a.grid, c.start, c.end, c.hmax, c.ex[0], c.ex[1], x.pi.x, x.pi.y, x.pi.z,
-                              x.hi + x.hi, 0.0f, lane, [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
-                                  for (uint32_t j = jb; j < je; ++j) {
-                                      if (j == i) continue;
-                                      force_term<kMorris>(a, x, j, shx, shy, shz, f);
-                                  }
-                              });
+        const uint32_t cnt = nl.cnt[i];
+        if (cnt != kHeavyMark && (cnt & kPooled) != 0u) {
+            // the lane's accepted blocks, kept by k_density_heavy in this lane's visiting order
+            const size_t base = (size_t)(cnt & ~kPooled) * 32 + lane;
+            const uint32_t kept = nl.pool_cnt[base];
+            const uint2* seg = nl.pool + base * kPoolLaneEntries;
+            for (uint32_t e = 0; e < kept; ++e) {
+                uint32_t first, mask;
+                float shx, shy, shz;
+                row_entry(a.grid, seg[e], first, mask, shx, shy, shz);
+                while (mask != 0u) {
+                    const uint32_t j = first + (uint32_t)(__ffs(mask) - 1);
+                    mask &= mask - 1u;
+                    if (j != i) force_term<kMorris>(a, x, j, shx, shy, shz, f);
+                }
+            }
+        } else {
+            for_each_subcell_lane(a.grid, c.start, c.end, c.hmax, c.ex[0], c.ex[1], x.pi.x, x.pi.y, x.pi.z,
+                                  x.hi + x.hi, 0.0f, lane,
+                                  [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
+                                      for (uint32_t j = jb; j < je; ++j) {
+                                          if (j == i) continue;
+                                          force_term<kMorris>(a, x, j, shx, shy, shz, f);
+                                      }
+                                  });
+        }
         if (boundary_near(a.grid, b, x.pi.x, x.pi.y, x.pi.z, x.hi + x.hi)) boundary_forces<32>(a, b, i, x, f, lane);
 #pragma unroll
         for (int q = 0; q < 3; q++) {
@@ -484,11 +544,6 @@ __global__ void __launch_bounds__(256, 1) k_forces_heavy(StepArgs a, CellsDev c,
 
 // Particles with long rows (kRowHeavy < cnt <= maxe): one warp per particle, row entry e on lane e mod 32, each
 // lane expanding its entries' masks in order; lane sums combined by the butterfly.
-__device__ __forceinline__ void row_entry(const GridDev& g, uint2 en, uint32_t& first, uint32_t& mask, float& shx,
-                                          float& shy, float& shz) {
-    decode_entry(g, en.x, first, shx, shy, shz);
-    mask = en.y;
-}
 
 __global__ void __launch_bounds__(256, 2) k_density_row(StepArgs a, BoundaryDev b, NbrDev nl) {
     const int lane = threadIdx.x & 31;
@@ -565,9 +620,9 @@ __global__ void __launch_bounds__(256, 2) k_forces_row(StepArgs a, BoundaryDev b
 cudaError_t launch_density(DensityKernel kind, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c,
                            BoundaryDev b, NbrDev nl) {
     if (kind == kDensityHeavy)
-        k_density_heavy<<<blocks, 256, 0, stream>>>(a, c, b, nl, nl.heavy, nl.heavy_n);
+        k_density_heavy<<<blocks, 256, 0, stream>>>(a, c, b, nl, nl.heavy, nl.heavy_n, true);
     else if (kind == kDensityOverflow)
-        k_density_heavy<<<blocks, 256, 0, stream>>>(a, c, b, nl, nl.dover, nl.dover_n);
+        k_density_heavy<<<blocks, 256, 0, stream>>>(a, c, b, nl, nl.dover, nl.dover_n, false);
     else if (kind == kDensityRow)
         k_density_row<<<blocks, 256, 0, stream>>>(a, b, nl);
     else if (a.grid.periodic)

@@ -151,6 +151,8 @@ struct asph_simulation {
     uint32_t* dover_idx = nullptr;  // [cap] particles whose list row overflowed in the density pass
     uint32_t* drow_idx = nullptr;   // [cap] particles with long rows, density pass
     uint32_t* frow_idx = nullptr;   // [cap] particles with long rows, force pass
+    uint2* pool = nullptr;          // [kPoolSlots * 32 * kPoolLaneEntries] accepted blocks of heavy particles
+    uint32_t* pool_cnt = nullptr;   // [kPoolSlots * 32]
     uint32_t* keys = nullptr;
     uint32_t* vals = nullptr;
     void* sort_mem = nullptr;
@@ -246,8 +248,9 @@ struct asph_simulation {
     CellsDev cells() const { return CellsDev{cell_start, cell_end, cell_hmax, hmax_ref, ex}; }
 
     NbrDev nbrs() const {
-        return NbrDev{nbr_ent,  nbr_cnt,      heavy_idx, heavy_n,  fheavy_idx,   fheavy_n,    dover_idx,
-                      fheavy_n + 1, drow_idx, fheavy_n + 2, frow_idx, fheavy_n + 3, kListEntries};
+        return NbrDev{nbr_ent,      nbr_cnt,  heavy_idx,    heavy_n,  fheavy_idx,   fheavy_n,
+                      dover_idx,    fheavy_n + 1, drow_idx, fheavy_n + 2, frow_idx, fheavy_n + 3,
+                      pool,         pool_cnt, kPoolSlots,   kListEntries};
     }
 
     BoundaryDev boundary() const {
@@ -780,6 +783,8 @@ void destroy(asph_simulation* s) {
     dfree(s->dover_idx);
     dfree(s->drow_idx);
     dfree(s->frow_idx);
+    dfree(s->pool);
+    dfree(s->pool_cnt);
     dfree(s->keys);
     dfree(s->vals);
     dfree(s->sort_mem);
@@ -1041,6 +1046,8 @@ asph_status asph_simulation_create(const asph_parameters* parameters, const floa
     TRY(dalloc(s->dover_idx, C));
     TRY(dalloc(s->drow_idx, C));
     TRY(dalloc(s->frow_idx, C));
+    TRY(dalloc(s->pool, (size_t)kPoolSlots * 32 * kPoolLaneEntries));
+    TRY(dalloc(s->pool_cnt, (size_t)kPoolSlots * 32));
     const uint32_t sort_items = std::max(C, std::max(boundary_count, max_boundary_capacity));
     TRY(dalloc(s->keys, sort_items));
     TRY(dalloc(s->vals, sort_items));
