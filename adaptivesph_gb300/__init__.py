@@ -5,12 +5,13 @@ Python mirror of the reference's simulation interface over that ABI, plus headle
 """
 from .parameters import (BoundaryMode, Criterion, DensityInfo, Domain, Parameters, RefinementParameters,
                          ViscosityModel)
-from .simulation import (BoundaryParticlesDataImportedBuffer, FluidParticlesDataImportedBuffer, ImportedMemory,
+from .simulation import (Batch, BoundaryParticlesDataImportedBuffer, FluidParticlesDataImportedBuffer, ImportedMemory,
                          Simulation, StaticBoundaryDomain, allocate_buffer, create_simulation, import_buffer)
 from ._lib import AsphError, load as load_library
 
 __all__ = [
     "AsphError",
+    "Batch",
     "BoundaryMode",
     "BoundaryParticlesDataImportedBuffer",
     "Criterion",

@@ -85,6 +85,10 @@ SIGNATURES = {
     "asph_simulation_enable_timing": (ctypes.c_int, [_vp, ctypes.c_int]),
     "asph_simulation_kernel_times": (ctypes.c_int, [_vp, P(ctypes.c_double), _up, _u32]),
     "asph_simulation_launch_count": (ctypes.c_int, [_vp, P(ctypes.c_uint64)]),
+    "asph_batch_create": (ctypes.c_int, [P(_vp), _u32, P(_vp)]),
+    "asph_batch_destroy": (None, [_vp]),
+    "asph_batch_step": (ctypes.c_int, [_vp, _fp, _u32]),
+    "asph_batch_stats": (ctypes.c_int, [_vp, P(ctypes.c_uint64), P(ctypes.c_uint64), P(ctypes.c_uint64)]),
     "asph_grid_sort_noalloc": (ctypes.c_int, [P(_p.CParameters), _vp, _u32, _vp, _vp, _vp, _vp, _u32, _vp, _vp]),
     "asph_abi_version": (ctypes.c_uint32, []),
     "asph_status_string": (ctypes.c_char_p, [ctypes.c_int]),

@@ -151,8 +151,9 @@ struct asph_simulation {
     uint32_t* dover_idx = nullptr;  // [cap] particles whose list row overflowed in the density pass
     uint32_t* drow_idx = nullptr;   // [cap] particles with long rows, density pass
     uint32_t* frow_idx = nullptr;   // [cap] particles with long rows, force pass
-    uint2* pool = nullptr;          // [kPoolSlots * 32 * kPoolLaneEntries] accepted blocks of heavy particles
-    uint32_t* pool_cnt = nullptr;   // [kPoolSlots * 32]
+    uint2* pool = nullptr;          // [pool_slots * 32 * kPoolLaneEntries] accepted blocks of heavy particles
+    uint32_t* pool_cnt = nullptr;   // [pool_slots * 32]
+    uint32_t pool_slots = 0;        // capacity / 128, clamped to [64, kPoolSlots]
     uint32_t* keys = nullptr;
     uint32_t* vals = nullptr;
     void* sort_mem = nullptr;
@@ -250,7 +251,7 @@ struct asph_simulation {
     NbrDev nbrs() const {
         return NbrDev{nbr_ent,      nbr_cnt,  heavy_idx,    heavy_n,  fheavy_idx,   fheavy_n,
                       dover_idx,    fheavy_n + 1, drow_idx, fheavy_n + 2, frow_idx, fheavy_n + 3,
-                      pool,         pool_cnt, kPoolSlots,   kListEntries};
+                      pool,         pool_cnt, pool_slots,   kListEntries};
     }
 
     BoundaryDev boundary() const {
@@ -1046,8 +1047,9 @@ asph_status asph_simulation_create(const asph_parameters* parameters, const floa
     TRY(dalloc(s->dover_idx, C));
     TRY(dalloc(s->drow_idx, C));
     TRY(dalloc(s->frow_idx, C));
-    TRY(dalloc(s->pool, (size_t)kPoolSlots * 32 * kPoolLaneEntries));
-    TRY(dalloc(s->pool_cnt, (size_t)kPoolSlots * 32));
+    s->pool_slots = std::min<uint32_t>(kPoolSlots, std::max<uint32_t>(64u, C / 128u));
+    TRY(dalloc(s->pool, (size_t)s->pool_slots * 32 * kPoolLaneEntries));
+    TRY(dalloc(s->pool_cnt, (size_t)s->pool_slots * 32));
     const uint32_t sort_items = std::max(C, std::max(boundary_count, max_boundary_capacity));
     TRY(dalloc(s->keys, sort_items));
     TRY(dalloc(s->vals, sort_items));
@@ -1710,3 +1712,183 @@ extern "C" asph_status asph_grid_sort_noalloc(const asph_parameters* params, con
     }
     return ASPH_OK;
 }
+
+// ------------------------------------------------------------------------------------------------ batches
+// asph_batch: independent simulations advanced together. Each simulation runs on its own streams, so their steps
+// overlap on the device. A plain step (no refinement pass) of a simulation is captured once as a CUDA graph per
+// buffer parity and replayed; the graph is captured again when the particle count, dt or the pending half-kick
+// changes. Steps with a refinement pass read the new particle count back and run eagerly; they are issued after
+// every simulation's plain steps up to its next refinement frame have been queued, so one simulation's read-back
+// does not hold the others' work back.
+namespace {
+
+struct StepKey {
+    uint32_t n = 0;
+    float dt = 0.0f, pending_half = 0.0f;
+    bool has_pending = false;
+    bool operator==(const StepKey& o) const {
+        return n == o.n && std::memcmp(&dt, &o.dt, 4) == 0 && std::memcmp(&pending_half, &o.pending_half, 4) == 0 &&
+               has_pending == o.has_pending;
+    }
+};
+
+struct SceneGraph {
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};  // by buffer parity (asph_simulation::cur) at the step's start
+    StepKey key[2];
+    uint64_t launches[2] = {0, 0};                 // kernels in the captured step
+};
+
+}  // namespace
+
+struct asph_batch {
+    std::vector<asph_simulation*> sims;
+    std::vector<SceneGraph> graphs;
+    uint64_t graph_steps = 0, eager_steps = 0, captures = 0;
+};
+
+namespace {
+
+void drop_graph(SceneGraph& g, int parity) {
+    if (g.exec[parity]) cudaGraphExecDestroy(g.exec[parity]);
+    g.exec[parity] = nullptr;
+}
+
+// Captures one plain step of s as a graph for its current parity; the simulation's host state is left as it was.
+asph_status capture_step(asph_simulation* s, SceneGraph& g, float dt) {
+    const int parity = s->cur;
+    drop_graph(g, parity);
+    const int cur = s->cur;
+    const uint32_t frame = s->frame;
+    const float pending_half = s->pending_half;
+    const bool has_pending = s->has_pending, grid_valid = s->grid_valid, timing = s->timing;
+    const uint64_t launches = s->launches;
+    s->timing = false;
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    const asph_status st = run_step(s, dt, ASPH_STAGE_ALL);
+    const cudaError_t ce = cudaStreamEndCapture(s->stream, &graph);
+    g.launches[parity] = s->launches - launches;
+    s->cur = cur;
+    s->frame = frame;
+    s->pending_half = pending_half;
+    s->has_pending = has_pending;
+    s->grid_valid = grid_valid;
+    s->timing = timing;
+    s->launches = launches;
+    if (st != ASPH_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return st;
+    }
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
+    const cudaError_t ie = cudaGraphInstantiate(&g.exec[parity], graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) {
+        g.exec[parity] = nullptr;
+        return cuda_fail(ie, "cudaGraphInstantiate");
+    }
+    g.key[parity] = StepKey{s->n, dt, s->pending_half, s->has_pending};
+    return ASPH_OK;
+}
+
+// One plain step of s from its graph (captured first if the step's inputs changed).
+asph_status graph_step(asph_batch* b, size_t k, float dt) {
+    asph_simulation* s = b->sims[k];
+    SceneGraph& g = b->graphs[k];
+    const int parity = s->cur;
+    const StepKey key{s->n, dt, s->pending_half, s->has_pending};
+    if (!g.exec[parity] || !(g.key[parity] == key)) {
+        asph_status st = capture_step(s, g, dt);
+        if (st != ASPH_OK) return st;
+        b->captures++;
+    }
+    CK(cudaGraphLaunch(g.exec[parity], s->stream));
+    // the host-side effects of run_step on a plain step
+    s->cur = 1 - s->cur;
+    s->grid_valid = true;
+    s->pending_half = dt / 2.0f;
+    s->has_pending = true;
+    s->frame++;
+    s->launches += g.launches[parity];
+    b->graph_steps++;
+    return ASPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+asph_status asph_batch_create(asph_simulation* const* sims, uint32_t count, asph_batch** out) {
+    API_ENTRY();
+    if (!out || (count > 0 && !sims)) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    for (uint32_t k = 0; k < count; k++) {
+        if (!sims[k]) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation in batch");
+        if (sims[k]->stream == nullptr)
+            return fail(ASPH_ERR_INVALID_ARGUMENT, "a batched simulation needs its own stream, not the default one");
+        for (uint32_t q = 0; q < k; q++)
+            if (sims[q] == sims[k]) return fail(ASPH_ERR_INVALID_ARGUMENT, "simulation listed twice");
+    }
+    asph_batch* b = new (std::nothrow) asph_batch();
+    if (!b) return fail(ASPH_ERR_OUT_OF_MEMORY, "batch");
+    b->sims.assign(sims, sims + count);
+    b->graphs.resize(count);
+    *out = b;
+    return ASPH_OK;
+}
+
+void asph_batch_destroy(asph_batch* b) {
+    if (!b) return;
+    for (auto& g : b->graphs) {
+        drop_graph(g, 0);
+        drop_graph(g, 1);
+    }
+    delete b;
+}
+
+asph_status asph_batch_step(asph_batch* b, const float* dts, uint32_t steps) {
+    API_ENTRY();
+    if (!b || (!b->sims.empty() && !dts)) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
+    const size_t S = b->sims.size();
+    for (size_t k = 0; k < S; k++)
+        if (!std::isfinite(dts[k])) return fail(ASPH_ERR_INVALID_ARGUMENT, "delta time must be finite");
+    std::vector<uint32_t> left(S, steps);
+    asph_status st;
+    for (;;) {
+        bool any = false;
+        // queue every simulation's plain steps up to its next refinement frame
+        for (size_t k = 0; k < S; k++) {
+            asph_simulation* s = b->sims[k];
+            while (left[k] > 0 && !refinement_due(s)) {
+                if (s->n == 0) {
+                    if ((st = run_step(s, dts[k], ASPH_STAGE_ALL)) != ASPH_OK) return st;
+                } else if ((st = graph_step(b, k, dts[k])) != ASPH_OK) {
+                    return st;
+                }
+                left[k]--;
+            }
+        }
+        // then the refinement frames, each with its read-back
+        for (size_t k = 0; k < S; k++) {
+            if (left[k] == 0) continue;
+            if ((st = run_step(b->sims[k], dts[k], ASPH_STAGE_ALL)) != ASPH_OK) return st;
+            b->eager_steps++;
+            left[k]--;
+            any = true;
+        }
+        if (!any) break;
+    }
+    for (size_t k = 0; k < S; k++)
+        if ((st = check_errors(b->sims[k], true)) != ASPH_OK) return st;
+    return ASPH_OK;
+}
+
+asph_status asph_batch_stats(const asph_batch* b, uint64_t* graph_steps, uint64_t* eager_steps, uint64_t* captures) {
+    API_ENTRY();
+    if (!b) return fail(ASPH_ERR_INVALID_ARGUMENT, "null batch");
+    if (graph_steps) *graph_steps = b->graph_steps;
+    if (eager_steps) *eager_steps = b->eager_steps;
+    if (captures) *captures = b->captures;
+    return ASPH_OK;
+}
+
+}  // extern "C"

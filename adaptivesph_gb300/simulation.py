@@ -364,3 +364,38 @@ def create_simulation(parameters: Parameters, positions: np.ndarray,
     sim = Simulation(out.value, parameters, refinement_params)
     sim._keepalive = (fluid_particle_memory, boundary_particle_memory)
     return sim
+
+
+class Batch:
+    """Independent simulations advanced together (asph_batch_*; no reference counterpart): their steps overlap on
+    the device and plain steps replay CUDA graphs. Each simulation's result equals its result when stepped alone.
+    The batch does not own the simulations; keep them alive while the batch exists."""
+
+    def __init__(self, simulations: Sequence[Simulation]):
+        self._lib = _lib.load()
+        self._sims = list(simulations)
+        arr = (_vp * max(len(self._sims), 1))(*[s._h.value for s in self._sims])
+        h = _vp()
+        _lib.check(self._lib.asph_batch_create(arr, len(self._sims), ctypes.byref(h)), "asph_batch_create")
+        self._h = h
+
+    def step(self, delta_times, steps: int = 1) -> None:
+        dts = np.ascontiguousarray(np.broadcast_to(np.asarray(delta_times, np.float32), (len(self._sims),)))
+        _lib.check(self._lib.asph_batch_step(self._h, _fp(dts), int(steps)), "asph_batch_step")
+
+    def stats(self) -> Dict[str, int]:
+        g, e, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        _lib.check(self._lib.asph_batch_stats(self._h, ctypes.byref(g), ctypes.byref(e), ctypes.byref(c)),
+                   "asph_batch_stats")
+        return dict(graph_steps=g.value, eager_steps=e.value, captures=c.value)
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.asph_batch_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -371,6 +371,25 @@ asph_status asph_simulation_kernel_times(asph_simulation* sim, double* ms, uint3
 asph_status asph_simulation_launch_count(const asph_simulation* sim, uint64_t* out);
 
 /* ---------------------------------------------------------------------------------------------
+ * Batches (no reference counterpart): independent simulations advanced together. Each simulation
+ * keeps its own streams, so their steps overlap on the device; plain steps are captured once as
+ * CUDA graphs and replayed. A batch does not own its simulations; while a batch step runs, the
+ * simulations must not be used otherwise. Every simulation's result equals the one it gives when
+ * stepped alone.
+ * ------------------------------------------------------------------------------------------- */
+typedef struct asph_batch asph_batch;
+/* sims[count]: distinct simulations, each on its own stream (the default: set_stream not called with
+ * the legacy default stream). */
+asph_status asph_batch_create(asph_simulation* const* sims, uint32_t count, asph_batch** out);
+void asph_batch_destroy(asph_batch* batch);
+/* Advances simulation k by `steps` steps of dts[k]; returns when all of them have finished, after
+ * checking every simulation's device error word. */
+asph_status asph_batch_step(asph_batch* batch, const float* dts, uint32_t steps);
+/* Steps replayed from graphs, steps run eagerly (refinement frames), graph captures so far. */
+asph_status asph_batch_stats(const asph_batch* batch, uint64_t* graph_steps, uint64_t* eager_steps,
+                             uint64_t* captures);
+
+/* ---------------------------------------------------------------------------------------------
  * Cell sort without allocation. No counterpart in the reference: it is the cell-key computation and
  * stable key sort of NeighborGrid::update (cuda/src/simulation/neighbors/NeighborGrid.cu:123-150)
  * plus the cell tables, offered alone for callers that must not allocate device memory. Such
