@@ -120,3 +120,32 @@ def taylor_green(n: int = 128, seed: int = 3, reynolds: float = 100.0, U: float 
     vel[:, 0] = (U * np.sin(x) * np.cos(y)).astype(np.float32)
     vel[:, 1] = (-U * np.cos(x) * np.sin(y)).astype(np.float32)
     return Scene("taylor_green", p, pos, None, float(0.25 * h / (c0 + U)), velocities=vel)
+
+
+def batched_mix(count: int = 256, seed: int = 4, dx: float = 0.01, min_particles: int = 4096,
+                max_particles: int = 262144):
+    """Independent dam-break scenes of uneven sizes for batched stepping: particle counts log-uniform in
+    [min_particles, max_particles], fill fraction U(0.2, 0.6), Morris viscosity nu log-uniform in [1e-6, 1e-3],
+    refinement (velocity criterion, two split levels) on the even-numbered scenes. Each fluid block is
+    nx x 2nx x nx particles at spacing dx in the corner of a tank 1.25 times the block's height and as deep as the
+    block, whose length makes the fluid fill the requested fraction of the tank."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        n_target = math.exp(rng.uniform(math.log(min_particles), math.log(max_particles)))
+        fill = rng.uniform(0.2, 0.6)
+        nu = math.exp(rng.uniform(math.log(1e-6), math.log(1e-3)))
+        nx = max(4, int(round((n_target / 2.0) ** (1.0 / 3.0))))
+        height = 2 * nx * dx
+        tank = (0.8 * nx * dx / fill, 1.25 * height, nx * dx)
+        refinement = None
+        if k % 2 == 0:
+            refinement = RefinementParameters(enabled=True, min_mass_ratio=0.05, max_mass_ratio=8.0,
+                                              max_particle_count=2 * (2 * nx ** 3), max_batch_ratio=0.2,
+                                              initial_cooldown=10, cooldown=10, criterion=Criterion.VELOCITY)
+        s = dam_break((nx, 2 * nx, nx), dx, seed=seed * 1000 + k, tank=tank, refinement=refinement)
+        s.parameters.viscosity_model = ViscosityModel.MORRIS
+        s.parameters.kinematic_viscosity = float(nu)
+        s.name = f"mix_{k:03d}"
+        out.append(s)
+    return out
