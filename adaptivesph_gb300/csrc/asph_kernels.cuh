@@ -9,7 +9,8 @@ namespace asph {
 struct StepArgs {
     GridDev grid;
     PhysDev phys;
-    uint32_t n;
+    uint32_t n;            // particle count; with np set, only a bound for the grid size
+    const uint32_t* np;    // particle count on the device (steps replayed from a graph), or null
     float4* ph;   // x, y, z, h
     float4* vm;   // vx, vy, vz, m
     float4* acc;  // ax, ay, az, 0
@@ -19,6 +20,10 @@ struct StepArgs {
     uint32_t* id;
     uint32_t* err;
 };
+
+// The step's particle count: from the device when the step is replayed from a graph (the count may have changed
+// since the capture), otherwise the launch argument.
+__device__ __forceinline__ uint32_t count_of(const StepArgs& a) { return a.np ? __ldg(a.np) : a.n; }
 
 // Per-particle neighbour lists of the current step. The candidate cells are scanned in blocks of up to 32
 // consecutive members of a sub-cell; row i holds one entry per block in which particle i accepted a neighbour:

@@ -314,7 +314,7 @@ template <bool kPeriodic>
 __global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
     __shared__ uint2 stage[256 * kStageStride];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool in = i < a.n;
+    const bool in = i < count_of(a);
     const float4 pi = in ? a.ph[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const float R = pi.w + pi.w;
     bool active = in;
@@ -484,7 +484,7 @@ __global__ void __launch_bounds__(256, 1) k_density_heavy(StepArgs a, CellsDev c
 template <bool kMorris>
 __global__ void __launch_bounds__(256, 3) k_forces(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
+    if (i >= count_of(a)) return;
     const uint32_t cnt = nl.cnt[i];
     if (cnt > kRowHeavy) return;  // long row (k_forces_row), overflowed or heavy (k_forces_heavy)
     const ForceCtx x = force_ctx(a, i);

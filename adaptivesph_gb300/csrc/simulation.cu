@@ -217,6 +217,8 @@ struct asph_simulation {
     cudaStream_t own_stream = nullptr;
     cudaStream_t aux = nullptr;  // heavy-particle kernels, forked from and joined back into `stream`
     cudaEvent_t ev_fork = nullptr, ev_main = nullptr, ev_aux = nullptr;
+    cudaEvent_t ev_refine = nullptr;  // end of a refinement pass whose read-back has not been taken yet
+    bool refine_pending = false;
     uint64_t launches = 0;
 
     // timing
@@ -230,11 +232,17 @@ struct asph_simulation {
     double ms[ASPH_KERNEL_COUNT] = {0};
     uint32_t timed[ASPH_KERNEL_COUNT] = {0};
 
+    // set while a step is captured as a graph: kernels read the count from d_count, grids cover grid_n
+    bool graph_mode = false;
+    uint32_t grid_n = 0;
+    uint32_t span() const { return graph_mode ? grid_n : n; }
+
     StepArgs args(int s) const {
         StepArgs a;
         a.grid = grid;
         a.phys = phys;
-        a.n = n;
+        a.n = span();
+        a.np = graph_mode ? d_count : nullptr;
         a.ph = set[s].ph;
         a.vm = set[s].vm;
         a.acc = set[s].acc;
@@ -479,7 +487,7 @@ asph_status upload_count(asph_simulation* s) {
 
 // Sort the current particles by sub-cell, gather into the other buffer set, build the cell tables.
 asph_status build_grid(asph_simulation* s, bool integrate, float dt, bool carry_rho) {
-    const uint32_t n = s->n;
+    const uint32_t n = s->span();
     StepArgs a = s->args(s->cur);
     CK(cudaMemsetAsync(s->q3, 0xff, 2 * sizeof(unsigned long long), s->stream));
     int h = s->tic();
@@ -503,7 +511,7 @@ asph_status build_grid(asph_simulation* s, bool integrate, float dt, bool carry_
     CK(cudaMemsetAsync(s->cell_hmax, 0, sizeof(float) * s->grid.ncells, s->stream));
     CK(cudaMemsetAsync(s->hmax_ref, 0, sizeof(float) * s->refcells_alloc, s->stream));
     CK(cudaMemsetAsync(s->heavy_n, 0, sizeof(uint32_t), s->stream));
-    k_excluded<<<1, 1, 0, s->stream>>>(s->q3, nullptr, n, s->ex, s->grid.periodic);
+    k_excluded<<<1, 1, 0, s->stream>>>(s->q3, s->graph_mode ? s->d_count : nullptr, n, s->ex, s->grid.periodic);
     CK_LAUNCH("k_excluded");
     ReorderArgs r;
     r.keys_sorted = s->keys;
@@ -545,7 +553,7 @@ asph_status run_density(asph_simulation* s) {
     CK(cudaEventRecord(s->ev_fork, s->stream));
     CK(cudaStreamWaitEvent(s->aux, s->ev_fork, 0));
     CK(launch_density(kDensityHeavy, kHeavyBlocks, s->aux, a, s->cells(), s->boundary(), s->nbrs()));
-    CK(launch_density(kDensityOrdinary, blocks_for(s->n), s->stream, a, s->cells(), s->boundary(), s->nbrs()));
+    CK(launch_density(kDensityOrdinary, blocks_for(s->span()), s->stream, a, s->cells(), s->boundary(), s->nbrs()));
     CK(launch_density(kDensityOverflow, kHeavyBlocks, s->stream, a, s->cells(), s->boundary(), s->nbrs()));
     CK(launch_density(kDensityRow, kHeavyBlocks, s->stream, a, s->cells(), s->boundary(), s->nbrs()));
     CK(cudaEventRecord(s->ev_main, s->stream));
@@ -562,7 +570,7 @@ asph_status run_forces(asph_simulation* s) {
     CK(cudaStreamWaitEvent(s->aux, s->ev_main, 0));
     CK(launch_forces(kForcesHeavy, s->phys.morris != 0, kHeavyBlocks, s->aux, a, s->cells(), s->boundary(),
                      s->nbrs()));
-    CK(launch_forces(kForcesOrdinary, s->phys.morris != 0, blocks_for(s->n), s->stream, a, s->cells(), s->boundary(),
+    CK(launch_forces(kForcesOrdinary, s->phys.morris != 0, blocks_for(s->span()), s->stream, a, s->cells(), s->boundary(),
                      s->nbrs()));
     CK(launch_forces(kForcesRow, s->phys.morris != 0, kHeavyBlocks, s->stream, a, s->cells(), s->boundary(),
                      s->nbrs()));
@@ -611,8 +619,9 @@ uint32_t id_bits(uint32_t next_id) {
     return b;
 }
 
-// One refinement pass (performAdaptiveRefinement, AdaptiveSphSimulation.cu:102-252); one read-back at the end.
-asph_status run_refine(asph_simulation* s) {
+// One refinement pass (performAdaptiveRefinement, AdaptiveSphSimulation.cu:102-252), enqueued; its counters are
+// read back into h_ctr at the end and taken by refine_finish.
+asph_status refine_enqueue(asph_simulation* s) {
     const uint32_t n = s->n;
     s->last_report = asph_refinement_report{};
     s->last_report.frame = s->frame;
@@ -684,7 +693,17 @@ asph_status run_refine(asph_simulation* s) {
     CK(cudaMemcpyAsync(s->d_count, s->ctr + kCtrCountOut, sizeof(uint32_t), cudaMemcpyDeviceToDevice, s->stream));
     CK(cudaMemcpyAsync(s->h_ctr, s->ctr, sizeof(uint32_t) * kCtrNum, cudaMemcpyDeviceToHost, s->stream));
     s->toc(h, ASPH_KERNEL_REFINE);
-    CK(cudaStreamSynchronize(s->stream));
+    CK(cudaEventRecord(s->ev_refine, s->stream));
+    s->refine_pending = true;
+    s->grid_valid = false;
+    return ASPH_OK;
+}
+
+// Waits for the enqueued refinement pass and takes its counters (new count, next id, report).
+asph_status refine_finish(asph_simulation* s) {
+    if (!s->refine_pending) return ASPH_OK;
+    s->refine_pending = false;
+    CK(cudaEventSynchronize(s->ev_refine));
     const uint32_t* c2 = s->h_ctr;
     s->n = c2[kCtrCountOut];
     s->next_id = c2[kCtrNextId];
@@ -697,8 +716,20 @@ asph_status run_refine(asph_simulation* s) {
     s->last_report.count_after = s->n;
     s->last_pairs_listed = c2[kCtrPairs];
     s->last_splits_listed = c2[kCtrSplits];
-    s->grid_valid = false;
     return ASPH_OK;
+}
+
+asph_status run_refine(asph_simulation* s) {
+    asph_status st = refine_enqueue(s);
+    if (st != ASPH_OK) return st;
+    return refine_finish(s);
+}
+
+// Upper bound of the particle count after a refinement pass started from n: merges remove, each split adds 12,
+// and splits exceed removed/12 by at most one block's worth (the reference's guard, Q-8); never above capacity.
+uint32_t count_after_refine_bound(const asph_simulation* s) {
+    const uint64_t b = (uint64_t)s->n + 12ull * (s->tpb > 0 ? s->tpb : 256);
+    return (uint32_t)std::min<uint64_t>(b, s->cap);
 }
 
 bool refinement_due(const asph_simulation* s) {
@@ -707,7 +738,9 @@ bool refinement_due(const asph_simulation* s) {
     return f == i0 || (f > i0 && f % cd == 0);
 }
 
-asph_status run_step(asph_simulation* s, float dt, uint32_t last_stage) {
+// One step up to last_stage. With defer_refine a refinement pass is only enqueued (refine_finish takes its
+// read-back later); the host-side count is then stale until refine_finish.
+asph_status run_step(asph_simulation* s, float dt, uint32_t last_stage, bool defer_refine = false) {
     if (!(std::isfinite(dt))) return fail(ASPH_ERR_INVALID_ARGUMENT, "delta time must be finite");
     if (s->n == 0) {
         // nothing to integrate; bookkeeping as the reference (kernels with zero threads)
@@ -738,7 +771,7 @@ asph_status run_step(asph_simulation* s, float dt, uint32_t last_stage) {
     if ((st = run_forces(s)) != ASPH_OK) return st;
     if (last_stage < ASPH_STAGE_ALL) return ASPH_OK;
     if (refinement_due(s)) {
-        if ((st = run_refine(s)) != ASPH_OK) return st;
+        if ((st = defer_refine ? refine_enqueue(s) : run_refine(s)) != ASPH_OK) return st;
     }
     s->pending_half = dt / 2.0f;
     s->has_pending = true;
@@ -823,6 +856,7 @@ void destroy(asph_simulation* s) {
     if (s->ev_fork) cudaEventDestroy(s->ev_fork);
     if (s->ev_main) cudaEventDestroy(s->ev_main);
     if (s->ev_aux) cudaEventDestroy(s->ev_aux);
+    if (s->ev_refine) cudaEventDestroy(s->ev_refine);
     if (s->aux) cudaStreamDestroy(s->aux);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
     delete s;
@@ -1019,6 +1053,7 @@ asph_status asph_simulation_create(const asph_parameters* parameters, const floa
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_main, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_aux, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_refine, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         destroy(s);
         return cuda_fail(e, "aux stream");
@@ -1722,15 +1757,23 @@ extern "C" asph_status asph_grid_sort_noalloc(const asph_parameters* params, con
 // does not hold the others' work back.
 namespace {
 
+// What a captured step depends on besides the device state: the grid bound (the kernels read the particle count
+// from the device, so any count up to the bound replays the same graph), dt and the pending half-kick.
 struct StepKey {
-    uint32_t n = 0;
+    uint32_t bound = 0;
     float dt = 0.0f, pending_half = 0.0f;
     bool has_pending = false;
-    bool operator==(const StepKey& o) const {
-        return n == o.n && std::memcmp(&dt, &o.dt, 4) == 0 && std::memcmp(&pending_half, &o.pending_half, 4) == 0 &&
-               has_pending == o.has_pending;
+    bool replays(const StepKey& o, uint32_t n) const {
+        return n <= bound && bound == o.bound && std::memcmp(&dt, &o.dt, 4) == 0 &&
+               std::memcmp(&pending_half, &o.pending_half, 4) == 0 && has_pending == o.has_pending;
     }
 };
+
+// grid bound of a captured step: room for growth by refinement without a new capture
+uint32_t bound_for(const asph_simulation* s) {
+    const uint64_t b = ((uint64_t)s->n + s->n / 8 + 256 + 255) / 256 * 256;
+    return (uint32_t)std::min<uint64_t>(b, s->cap);
+}
 
 struct SceneGraph {
     cudaGraphExec_t exec[2] = {nullptr, nullptr};  // by buffer parity (asph_simulation::cur) at the step's start
@@ -1762,10 +1805,14 @@ asph_status capture_step(asph_simulation* s, SceneGraph& g, float dt) {
     const float pending_half = s->pending_half;
     const bool has_pending = s->has_pending, grid_valid = s->grid_valid, timing = s->timing;
     const uint64_t launches = s->launches;
+    const uint32_t bound = bound_for(s);
     s->timing = false;
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    s->graph_mode = true;
+    s->grid_n = bound;
     const asph_status st = run_step(s, dt, ASPH_STAGE_ALL);
+    s->graph_mode = false;
     const cudaError_t ce = cudaStreamEndCapture(s->stream, &graph);
     g.launches[parity] = s->launches - launches;
     s->cur = cur;
@@ -1786,20 +1833,26 @@ asph_status capture_step(asph_simulation* s, SceneGraph& g, float dt) {
         g.exec[parity] = nullptr;
         return cuda_fail(ie, "cudaGraphInstantiate");
     }
-    g.key[parity] = StepKey{s->n, dt, s->pending_half, s->has_pending};
+    g.key[parity] = StepKey{bound, dt, s->pending_half, s->has_pending};
     return ASPH_OK;
 }
 
-// One plain step of s from its graph (captured first if the step's inputs changed).
+// One plain step of s from its graph (captured first if the step's inputs changed). A graph replays for any count up
+// to its bound, so a pending refinement read-back only has to be taken when its worst case exceeds the bound.
 asph_status graph_step(asph_batch* b, size_t k, float dt) {
     asph_simulation* s = b->sims[k];
     SceneGraph& g = b->graphs[k];
     const int parity = s->cur;
-    const StepKey key{s->n, dt, s->pending_half, s->has_pending};
-    if (!g.exec[parity] || !(g.key[parity] == key)) {
-        asph_status st = capture_step(s, g, dt);
+    const StepKey key{g.key[parity].bound, dt, s->pending_half, s->has_pending};
+    // while a refinement read-back is outstanding the count is only known to be at most this
+    const uint32_t n_max = s->refine_pending ? count_after_refine_bound(s) : s->n;
+    if (!g.exec[parity] || !g.key[parity].replays(key, n_max)) {
+        asph_status st = refine_finish(s);
         if (st != ASPH_OK) return st;
-        b->captures++;
+        if (!g.exec[parity] || !g.key[parity].replays(key, s->n)) {
+            if ((st = capture_step(s, g, dt)) != ASPH_OK) return st;
+            b->captures++;
+        }
     }
     CK(cudaGraphLaunch(g.exec[parity], s->stream));
     // the host-side effects of run_step on a plain step
@@ -1859,7 +1912,7 @@ asph_status asph_batch_step(asph_batch* b, const float* dts, uint32_t steps) {
         for (size_t k = 0; k < S; k++) {
             asph_simulation* s = b->sims[k];
             while (left[k] > 0 && !refinement_due(s)) {
-                if (s->n == 0) {
+                if (s->n == 0 && !s->refine_pending) {
                     if ((st = run_step(s, dts[k], ASPH_STAGE_ALL)) != ASPH_OK) return st;
                 } else if ((st = graph_step(b, k, dts[k])) != ASPH_OK) {
                     return st;
@@ -1867,16 +1920,20 @@ asph_status asph_batch_step(asph_batch* b, const float* dts, uint32_t steps) {
                 left[k]--;
             }
         }
-        // then the refinement frames, each with its read-back
+        // then the refinement frames, enqueued without waiting for their read-backs
         for (size_t k = 0; k < S; k++) {
             if (left[k] == 0) continue;
-            if ((st = run_step(b->sims[k], dts[k], ASPH_STAGE_ALL)) != ASPH_OK) return st;
+            asph_simulation* s = b->sims[k];
+            if ((st = refine_finish(s)) != ASPH_OK) return st;  // a pass starts from the previous one's count
+            if ((st = run_step(s, dts[k], ASPH_STAGE_ALL, true)) != ASPH_OK) return st;
             b->eager_steps++;
             left[k]--;
             any = true;
         }
         if (!any) break;
     }
+    for (size_t k = 0; k < S; k++)
+        if ((st = refine_finish(b->sims[k])) != ASPH_OK) return st;
     for (size_t k = 0; k < S; k++)
         if ((st = check_errors(b->sims[k], true)) != ASPH_OK) return st;
     return ASPH_OK;

@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(256) k_integrate_keys(StepArgs a, float dt, fl
                                                         uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
                                                         unsigned long long* q3) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t n = a.n;
+    const uint32_t n = count_of(a);
     uint64_t q = ~0ull;
     if (i < n) {
         float4 ph = a.ph[i];
@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(256) k_keys(StepArgs a, uint32_t* __restrict__
                                               unsigned long long* q3) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint64_t q = ~0ull;
-    if (i < a.n) {
+    if (i < count_of(a)) {
         const float4 ph = a.ph[i];
         uint32_t key, refkey;
         cell_of(a.grid, ph.x, ph.y, ph.z, key, refkey);
@@ -146,7 +146,7 @@ __global__ void k_excluded(const unsigned long long* q3, const uint32_t* n_ptr, 
 // tables (start, end, max h) and the global max h.
 __global__ void __launch_bounds__(256) k_reorder_cells(StepArgs a, ReorderArgs r) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t n = a.n;
+    const uint32_t n = count_of(a);
     if (k >= n) return;
     const uint32_t src = r.vals_sorted[k];
     const uint32_t key = r.keys_sorted[k];

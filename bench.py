@@ -27,6 +27,10 @@ import time
 
 import numpy as np
 
+# many simulations step on their own streams in the batched workload: let them use all 32 hardware queues
+# (the default of 8 makes unrelated streams wait on one another); set before CUDA is initialised
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
