@@ -6,7 +6,8 @@ Python mirror of the reference's simulation interface over that ABI, plus headle
 from .parameters import (BoundaryMode, Criterion, DensityInfo, Domain, Parameters, RefinementParameters,
                          ViscosityModel)
 from .simulation import (Batch, BoundaryParticlesDataImportedBuffer, FluidParticlesDataImportedBuffer, ImportedMemory,
-                         Simulation, StaticBoundaryDomain, allocate_buffer, create_simulation, import_buffer)
+                         Server, Simulation, StaticBoundaryDomain, allocate_buffer, create_simulation,
+                         estimate_device_bytes, import_buffer)
 from ._lib import AsphError, load as load_library
 
 __all__ = [
@@ -21,11 +22,13 @@ __all__ = [
     "ImportedMemory",
     "Parameters",
     "RefinementParameters",
+    "Server",
     "Simulation",
     "StaticBoundaryDomain",
     "ViscosityModel",
     "allocate_buffer",
     "create_simulation",
+    "estimate_device_bytes",
     "import_buffer",
     "load_library",
 ]

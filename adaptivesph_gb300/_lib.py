@@ -85,6 +85,17 @@ SIGNATURES = {
     "asph_simulation_enable_timing": (ctypes.c_int, [_vp, ctypes.c_int]),
     "asph_simulation_kernel_times": (ctypes.c_int, [_vp, P(ctypes.c_double), _up, _u32]),
     "asph_simulation_launch_count": (ctypes.c_int, [_vp, P(ctypes.c_uint64)]),
+    "asph_simulation_device_bytes": (ctypes.c_int, [_vp, P(ctypes.c_uint64)]),
+    "asph_estimate_device_bytes": (ctypes.c_int, [P(_p.CParameters), _u32, _u32, P(_p.CRefinementParameters), _u32,
+                                                  _u32, P(ctypes.c_uint64)]),
+    "asph_server_create": (ctypes.c_int, [ctypes.c_uint64, _u32, P(_vp)]),
+    "asph_server_destroy": (None, [_vp]),
+    "asph_server_submit": (ctypes.c_int, [_vp, P(_p.CRequest), P(ctypes.c_uint64)]),
+    "asph_server_poll": (ctypes.c_int, [_vp, _u32, P(_u32)]),
+    "asph_server_status": (ctypes.c_int, [_vp, ctypes.c_uint64, P(_p.CRequestStatus)]),
+    "asph_server_take": (ctypes.c_int, [_vp, ctypes.c_uint64, _fp, _fp, _fp, _fp, _up, _u32]),
+    "asph_server_stats": (ctypes.c_int, [_vp, P(ctypes.c_uint64), P(_u32), P(_u32), P(ctypes.c_uint64),
+                                         P(ctypes.c_uint64)]),
     "asph_batch_create": (ctypes.c_int, [P(_vp), _u32, P(_vp)]),
     "asph_batch_destroy": (None, [_vp]),
     "asph_batch_step": (ctypes.c_int, [_vp, _fp, _u32]),

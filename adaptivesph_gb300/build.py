@@ -20,8 +20,8 @@ LIB = os.path.join(HERE, "libasph_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 CU_SOURCES = ["step_kernels.cu", "neighbor_kernels.cu", "refine_kernels.cu", "radix_sort.cu", "simulation.cu"]
-CPP_SOURCES = ["boundary_domain.cpp"]
-HEADERS = ["asph_device.cuh", "asph_kernels.cuh", "asph_refine.cuh"]
+CPP_SOURCES = ["boundary_domain.cpp", "server.cpp"]
+HEADERS = ["asph_device.cuh", "asph_kernels.cuh", "asph_refine.cuh", "batch_internal.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

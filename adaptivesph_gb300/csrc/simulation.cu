@@ -19,6 +19,7 @@
 #include "../../include/asph.h"
 #include "asph_kernels.cuh"
 #include "asph_refine.cuh"
+#include "batch_internal.h"
 
 using namespace asph;
 
@@ -169,6 +170,7 @@ struct asph_simulation {
     uint32_t* err = nullptr;
     uint32_t* d_count = nullptr;
     uint8_t* red = nullptr;  // [kRedBytes] reduction scratch of totals, CFL and density info
+    uint64_t device_bytes = 0;  // device memory held (device_bytes_for at creation)
 
     // boundary
     float4* bpos = nullptr;
@@ -320,6 +322,26 @@ asph_status dalloc(T*& p, size_t count) {
 
 void dfree(void* p) {
     if (p) cudaFree(p);
+}
+
+// Device memory a simulation holds: the sizes allocated by asph_simulation_create (the export staging buffer,
+// allocated on the first export, and the optional id lists are not included).
+uint64_t device_bytes_for(uint32_t C, uint32_t sort_items, uint32_t ncells, uint32_t refcells, uint32_t nb,
+                          bool adaptive) {
+    const uint64_t c = C;
+    uint64_t b = 0;
+    b += 2 * c * (sizeof(float4) * 3 + sizeof(float2) + sizeof(float) + sizeof(uint32_t));  // two buffer sets
+    b += c * sizeof(float4);                                                                // kernel constants
+    b += c * kListEntries * sizeof(uint2) + c * sizeof(uint32_t);                          // rows and counts
+    b += c * sizeof(uint32_t) * 5 + sizeof(uint32_t) * 5;                                   // queues
+    const uint64_t slots = std::min<uint32_t>(kPoolSlots, std::max<uint32_t>(64u, C / 128u));
+    b += slots * 32 * (kPoolLaneEntries * sizeof(uint2) + sizeof(uint32_t));                // heavy pool
+    b += (uint64_t)sort_items * sizeof(uint32_t) * 2 + sort_scratch_bytes(sort_items);      // sort
+    b += sizeof(uint32_t) * 4 + sizeof(unsigned long long) * 2 + sizeof(uint32_t) * 3 + kRedBytes;
+    b += (uint64_t)refcells * (sizeof(float) + 1) + (uint64_t)ncells * sizeof(uint32_t) * 5;  // cell tables
+    b += (uint64_t)nb * (sizeof(float4) + sizeof(float));                                  // boundary
+    if (adaptive) b += c * sizeof(uint32_t) * 5 + sizeof(uint32_t) * (kCtrNum + 2 + blocks_for(C)) + 8;
+    return b;
 }
 
 asph_status make_grid(const asph_parameters& P, GridDev& g) {
@@ -1086,6 +1108,9 @@ asph_status asph_simulation_create(const asph_parameters* parameters, const floa
     TRY(dalloc(s->pool, (size_t)s->pool_slots * 32 * kPoolLaneEntries));
     TRY(dalloc(s->pool_cnt, (size_t)s->pool_slots * 32));
     const uint32_t sort_items = std::max(C, std::max(boundary_count, max_boundary_capacity));
+    s->device_bytes = device_bytes_for(C, sort_items, s->grid.ncells,
+                                       (uint32_t)(s->grid.gs[0] * s->grid.gs[1] * s->grid.gs[2]), boundary_count,
+                                       adaptive);
     TRY(dalloc(s->keys, sort_items));
     TRY(dalloc(s->vals, sort_items));
     {
@@ -1749,16 +1774,15 @@ extern "C" asph_status asph_grid_sort_noalloc(const asph_parameters* params, con
 }
 
 // ------------------------------------------------------------------------------------------------ batches
-// asph_batch: independent simulations advanced together. Each simulation runs on its own streams, so their steps
-// overlap on the device. A plain step (no refinement pass) of a simulation is captured once as a CUDA graph per
-// buffer parity and replayed; the graph is captured again when the particle count, dt or the pending half-kick
-// changes. Steps with a refinement pass read the new particle count back and run eagerly; they are issued after
-// every simulation's plain steps up to its next refinement frame have been queued, so one simulation's read-back
-// does not hold the others' work back.
+// Independent simulations advanced together (asph_batch, and the serving loop of server.cpp). Each simulation runs
+// on its own streams, so their steps overlap on the device. A plain step (no refinement pass) is captured once as
+// a CUDA graph per buffer parity and replayed; its kernels read the particle count from the device, so a graph
+// replays for any count up to the bound it was captured with. Steps with a refinement pass are enqueued without
+// waiting for their read-back, after every simulation's plain steps up to its next refinement frame; the read-back
+// is taken when the host needs the count (a capture, the next refinement pass, the end of the advance).
 namespace {
 
-// What a captured step depends on besides the device state: the grid bound (the kernels read the particle count
-// from the device, so any count up to the bound replays the same graph), dt and the pending half-kick.
+// What a captured step depends on besides the device state: the grid bound, dt and the pending half-kick.
 struct StepKey {
     uint32_t bound = 0;
     float dt = 0.0f, pending_half = 0.0f;
@@ -1775,19 +1799,26 @@ uint32_t bound_for(const asph_simulation* s) {
     return (uint32_t)std::min<uint64_t>(b, s->cap);
 }
 
+}  // namespace
+
+namespace asph {
+
 struct SceneGraph {
     cudaGraphExec_t exec[2] = {nullptr, nullptr};  // by buffer parity (asph_simulation::cur) at the step's start
     StepKey key[2];
     uint64_t launches[2] = {0, 0};                 // kernels in the captured step
 };
 
-}  // namespace
+SceneGraph* scene_graph_new() { return new (std::nothrow) SceneGraph(); }
 
-struct asph_batch {
-    std::vector<asph_simulation*> sims;
-    std::vector<SceneGraph> graphs;
-    uint64_t graph_steps = 0, eager_steps = 0, captures = 0;
-};
+void scene_graph_free(SceneGraph* g) {
+    if (!g) return;
+    for (int p = 0; p < 2; p++)
+        if (g->exec[p]) cudaGraphExecDestroy(g->exec[p]);
+    delete g;
+}
+
+}  // namespace asph
 
 namespace {
 
@@ -1837,21 +1868,18 @@ asph_status capture_step(asph_simulation* s, SceneGraph& g, float dt) {
     return ASPH_OK;
 }
 
-// One plain step of s from its graph (captured first if the step's inputs changed). A graph replays for any count up
-// to its bound, so a pending refinement read-back only has to be taken when its worst case exceeds the bound.
-asph_status graph_step(asph_batch* b, size_t k, float dt) {
-    asph_simulation* s = b->sims[k];
-    SceneGraph& g = b->graphs[k];
+// One plain step of s from its graph (captured first if the step's inputs changed). A pending refinement
+// read-back is taken only when its worst case exceeds the graph's bound.
+asph_status graph_step(asph_simulation* s, SceneGraph& g, float dt, AdvanceStats& stats) {
     const int parity = s->cur;
     const StepKey key{g.key[parity].bound, dt, s->pending_half, s->has_pending};
-    // while a refinement read-back is outstanding the count is only known to be at most this
     const uint32_t n_max = s->refine_pending ? count_after_refine_bound(s) : s->n;
     if (!g.exec[parity] || !g.key[parity].replays(key, n_max)) {
         asph_status st = refine_finish(s);
         if (st != ASPH_OK) return st;
         if (!g.exec[parity] || !g.key[parity].replays(key, s->n)) {
             if ((st = capture_step(s, g, dt)) != ASPH_OK) return st;
-            b->captures++;
+            stats.captures++;
         }
     }
     CK(cudaGraphLaunch(g.exec[parity], s->stream));
@@ -1862,11 +1890,61 @@ asph_status graph_step(asph_batch* b, size_t k, float dt) {
     s->has_pending = true;
     s->frame++;
     s->launches += g.launches[parity];
-    b->graph_steps++;
+    stats.graph_steps++;
     return ASPH_OK;
 }
 
 }  // namespace
+
+namespace asph {
+
+asph_status advance_scenes(asph_simulation* const* sims, SceneGraph* const* graphs, const float* dts, uint32_t* left,
+                           size_t count, AdvanceStats& stats) {
+    for (size_t k = 0; k < count; k++) {
+        if (!sims[k] || !graphs[k]) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation or graph cache");
+        if (!std::isfinite(dts[k])) return fail(ASPH_ERR_INVALID_ARGUMENT, "delta time must be finite");
+    }
+    asph_status st;
+    for (;;) {
+        bool any = false;
+        // queue every simulation's plain steps up to its next refinement frame
+        for (size_t k = 0; k < count; k++) {
+            asph_simulation* s = sims[k];
+            while (left[k] > 0 && !refinement_due(s)) {
+                if (s->n == 0 && !s->refine_pending) {
+                    if ((st = run_step(s, dts[k], ASPH_STAGE_ALL)) != ASPH_OK) return st;
+                } else if ((st = graph_step(s, *graphs[k], dts[k], stats)) != ASPH_OK) {
+                    return st;
+                }
+                left[k]--;
+            }
+        }
+        // then the refinement frames, enqueued without waiting for their read-backs
+        for (size_t k = 0; k < count; k++) {
+            if (left[k] == 0) continue;
+            asph_simulation* s = sims[k];
+            if ((st = refine_finish(s)) != ASPH_OK) return st;  // a pass starts from the previous one's count
+            if ((st = run_step(s, dts[k], ASPH_STAGE_ALL, true)) != ASPH_OK) return st;
+            stats.eager_steps++;
+            left[k]--;
+            any = true;
+        }
+        if (!any) break;
+    }
+    for (size_t k = 0; k < count; k++)
+        if ((st = refine_finish(sims[k])) != ASPH_OK) return st;
+    for (size_t k = 0; k < count; k++)
+        if ((st = check_errors(sims[k], true)) != ASPH_OK) return st;
+    return ASPH_OK;
+}
+
+}  // namespace asph
+
+struct asph_batch {
+    std::vector<asph_simulation*> sims;
+    std::vector<SceneGraph*> graphs;
+    AdvanceStats stats;
+};
 
 extern "C" {
 
@@ -1884,67 +1962,64 @@ asph_status asph_batch_create(asph_simulation* const* sims, uint32_t count, asph
     asph_batch* b = new (std::nothrow) asph_batch();
     if (!b) return fail(ASPH_ERR_OUT_OF_MEMORY, "batch");
     b->sims.assign(sims, sims + count);
-    b->graphs.resize(count);
+    for (uint32_t k = 0; k < count; k++) {
+        SceneGraph* g = scene_graph_new();
+        if (!g) {
+            asph_batch_destroy(b);
+            return fail(ASPH_ERR_OUT_OF_MEMORY, "batch");
+        }
+        b->graphs.push_back(g);
+    }
     *out = b;
     return ASPH_OK;
 }
 
 void asph_batch_destroy(asph_batch* b) {
     if (!b) return;
-    for (auto& g : b->graphs) {
-        drop_graph(g, 0);
-        drop_graph(g, 1);
-    }
+    for (SceneGraph* g : b->graphs) scene_graph_free(g);
     delete b;
 }
 
 asph_status asph_batch_step(asph_batch* b, const float* dts, uint32_t steps) {
     API_ENTRY();
     if (!b || (!b->sims.empty() && !dts)) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
-    const size_t S = b->sims.size();
-    for (size_t k = 0; k < S; k++)
-        if (!std::isfinite(dts[k])) return fail(ASPH_ERR_INVALID_ARGUMENT, "delta time must be finite");
-    std::vector<uint32_t> left(S, steps);
-    asph_status st;
-    for (;;) {
-        bool any = false;
-        // queue every simulation's plain steps up to its next refinement frame
-        for (size_t k = 0; k < S; k++) {
-            asph_simulation* s = b->sims[k];
-            while (left[k] > 0 && !refinement_due(s)) {
-                if (s->n == 0 && !s->refine_pending) {
-                    if ((st = run_step(s, dts[k], ASPH_STAGE_ALL)) != ASPH_OK) return st;
-                } else if ((st = graph_step(b, k, dts[k])) != ASPH_OK) {
-                    return st;
-                }
-                left[k]--;
-            }
-        }
-        // then the refinement frames, enqueued without waiting for their read-backs
-        for (size_t k = 0; k < S; k++) {
-            if (left[k] == 0) continue;
-            asph_simulation* s = b->sims[k];
-            if ((st = refine_finish(s)) != ASPH_OK) return st;  // a pass starts from the previous one's count
-            if ((st = run_step(s, dts[k], ASPH_STAGE_ALL, true)) != ASPH_OK) return st;
-            b->eager_steps++;
-            left[k]--;
-            any = true;
-        }
-        if (!any) break;
-    }
-    for (size_t k = 0; k < S; k++)
-        if ((st = refine_finish(b->sims[k])) != ASPH_OK) return st;
-    for (size_t k = 0; k < S; k++)
-        if ((st = check_errors(b->sims[k], true)) != ASPH_OK) return st;
-    return ASPH_OK;
+    std::vector<uint32_t> left(b->sims.size(), steps);
+    return advance_scenes(b->sims.data(), b->graphs.data(), dts, left.data(), b->sims.size(), b->stats);
 }
 
 asph_status asph_batch_stats(const asph_batch* b, uint64_t* graph_steps, uint64_t* eager_steps, uint64_t* captures) {
     API_ENTRY();
     if (!b) return fail(ASPH_ERR_INVALID_ARGUMENT, "null batch");
-    if (graph_steps) *graph_steps = b->graph_steps;
-    if (eager_steps) *eager_steps = b->eager_steps;
-    if (captures) *captures = b->captures;
+    if (graph_steps) *graph_steps = b->stats.graph_steps;
+    if (eager_steps) *eager_steps = b->stats.eager_steps;
+    if (captures) *captures = b->stats.captures;
+    return ASPH_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+asph_status asph_simulation_device_bytes(const asph_simulation* sim, uint64_t* out) {
+    API_ENTRY();
+    if (!sim || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
+    *out = sim->device_bytes;
+    return ASPH_OK;
+}
+
+asph_status asph_estimate_device_bytes(const asph_parameters* parameters, uint32_t count, uint32_t boundary_count,
+                                       const asph_refinement_parameters* refinement, uint32_t max_fluid_capacity,
+                                       uint32_t max_boundary_capacity, uint64_t* out) {
+    API_ENTRY();
+    if (!parameters || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
+    GridDev g;
+    asph_status st = make_grid(*parameters, g);
+    if (st != ASPH_OK) return st;
+    const bool adaptive = refinement && refinement->enabled;
+    const uint32_t cap = std::max(adaptive ? refinement->max_particle_count : std::max(max_fluid_capacity, count), 1u);
+    const uint32_t sort_items = std::max(cap, std::max(boundary_count, max_boundary_capacity));
+    *out = device_bytes_for(cap, sort_items, g.ncells, (uint32_t)(g.gs[0] * g.gs[1] * g.gs[2]), boundary_count,
+                            adaptive);
     return ASPH_OK;
 }
 

@@ -235,6 +235,34 @@ class CRefinementReport(ctypes.Structure):
     ]
 
 
+class CRequest(ctypes.Structure):
+    _fields_ = [
+        ("parameters", CParameters),
+        ("positions", ctypes.POINTER(ctypes.c_float)),
+        ("count", ctypes.c_uint32),
+        ("boundary", ctypes.POINTER(CBoundaryParticle)),
+        ("boundary_count", ctypes.c_uint32),
+        ("refinement", ctypes.POINTER(CRefinementParameters)),
+        ("max_fluid_capacity", ctypes.c_uint32),
+        ("delta_time", ctypes.c_float),
+        ("steps", ctypes.c_uint32),
+    ]
+
+
+class CRequestStatus(ctypes.Structure):
+    _fields_ = [
+        ("state", ctypes.c_uint32),
+        ("steps_done", ctypes.c_uint32),
+        ("steps", ctypes.c_uint32),
+        ("count", ctypes.c_uint32),
+        ("error", ctypes.c_int),
+        ("device_bytes", ctypes.c_uint64),
+        ("submit_s", ctypes.c_double),
+        ("admit_s", ctypes.c_double),
+        ("finish_s", ctypes.c_double),
+    ]
+
+
 def to_c_domain(d: Domain) -> CDomain:
     return CDomain((ctypes.c_float * 3)(*d.min), (ctypes.c_float * 3)(*d.max), d.friction)
 

@@ -167,6 +167,11 @@ class Simulation:
         _lib.check(self._lib.asph_simulation_fluid_count(self._h, ctypes.byref(out)), "getFluidParticlesCount")
         return int(out.value)
 
+    def device_bytes(self) -> int:
+        out = ctypes.c_uint64()
+        _lib.check(self._lib.asph_simulation_device_bytes(self._h, ctypes.byref(out)), "device_bytes")
+        return int(out.value)
+
     def get_boundary_particles_count(self) -> int:
         out = ctypes.c_uint32()
         _lib.check(self._lib.asph_simulation_boundary_count(self._h, ctypes.byref(out)), "getBoundaryParticlesCount")
@@ -392,6 +397,88 @@ class Batch:
     def close(self) -> None:
         if self._h:
             self._lib.asph_batch_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def estimate_device_bytes(parameters: Parameters, count: int, boundary_count: int,
+                          refinement: Optional[RefinementParameters], max_fluid_capacity: int) -> int:
+    """Device memory asph_simulation_create would allocate for these arguments."""
+    lib = _lib.load()
+    cp = _p.to_c_parameters(parameters)
+    cr = _p.to_c_refinement(refinement) if refinement is not None and refinement.enabled else None
+    out = ctypes.c_uint64()
+    _lib.check(lib.asph_estimate_device_bytes(ctypes.byref(cp), int(count), int(boundary_count),
+                                              ctypes.byref(cr) if cr is not None else None, int(max_fluid_capacity),
+                                              int(boundary_count), ctypes.byref(out)), "estimate_device_bytes")
+    return int(out.value)
+
+
+REQUEST_STATES = {0: "queued", 1: "active", 2: "done", 3: "failed"}
+
+
+class Server:
+    """The serving loop (asph_server_*; no reference counterpart): requests queue, are admitted first come first
+    served under a device-memory budget, run together, and retire with their particles copied to host memory."""
+
+    def __init__(self, memory_budget_bytes: int, max_active: int = 0):
+        self._lib = _lib.load()
+        h = _vp()
+        _lib.check(self._lib.asph_server_create(int(memory_budget_bytes), int(max_active), ctypes.byref(h)),
+                   "asph_server_create")
+        self._h = h
+
+    def submit(self, parameters: Parameters, positions: np.ndarray, boundary: "StaticBoundaryDomain",
+               refinement: Optional[RefinementParameters], delta_time: float, steps: int,
+               max_fluid_capacity: Optional[int] = None) -> int:
+        pos = np.ascontiguousarray(positions, np.float32).reshape(-1, 4)
+        bp, nb = boundary.to_c()
+        cr = _p.to_c_refinement(refinement) if refinement is not None and refinement.enabled else None
+        cap = max_fluid_capacity if max_fluid_capacity is not None else pos.shape[0]
+        rq = _p.CRequest(_p.to_c_parameters(parameters), _fp(pos), pos.shape[0],
+                         ctypes.cast(bp, ctypes.POINTER(_p.CBoundaryParticle)) if nb else None,
+                         nb, ctypes.pointer(cr) if cr is not None else None, int(cap),
+                         float(delta_time), int(steps))
+        t = ctypes.c_uint64()
+        _lib.check(self._lib.asph_server_submit(self._h, ctypes.byref(rq), ctypes.byref(t)), "asph_server_submit")
+        return int(t.value)
+
+    def poll(self, max_steps: int = 0) -> int:
+        out = ctypes.c_uint32()
+        _lib.check(self._lib.asph_server_poll(self._h, int(max_steps), ctypes.byref(out)), "asph_server_poll")
+        return int(out.value)
+
+    def status(self, ticket: int) -> Dict[str, object]:
+        s = _p.CRequestStatus()
+        _lib.check(self._lib.asph_server_status(self._h, int(ticket), ctypes.byref(s)), "asph_server_status")
+        return dict(state=REQUEST_STATES.get(s.state, "?"), steps_done=s.steps_done, steps=s.steps, count=s.count,
+                    error=s.error, device_bytes=s.device_bytes, submit_s=s.submit_s, admit_s=s.admit_s,
+                    finish_s=s.finish_s)
+
+    def take(self, ticket: int) -> Dict[str, np.ndarray]:
+        n = int(self.status(ticket)["count"])
+        out = dict(positions=np.zeros((n, 4), np.float32), velocities=np.zeros((n, 4), np.float32),
+                   densities=np.zeros(n, np.float32), radii=np.zeros(n, np.float32), ids=np.zeros(n, np.uint32))
+        _lib.check(self._lib.asph_server_take(self._h, int(ticket), _fp(out["positions"]), _fp(out["velocities"]),
+                                              _fp(out["densities"]), _fp(out["radii"]), _up(out["ids"]), n),
+                   "asph_server_take")
+        return out
+
+    def stats(self) -> Dict[str, int]:
+        used, q, a = ctypes.c_uint64(), ctypes.c_uint32(), ctypes.c_uint32()
+        g, e = ctypes.c_uint64(), ctypes.c_uint64()
+        _lib.check(self._lib.asph_server_stats(self._h, ctypes.byref(used), ctypes.byref(q), ctypes.byref(a),
+                                               ctypes.byref(g), ctypes.byref(e)), "asph_server_stats")
+        return dict(used_bytes=used.value, queued=q.value, active=a.value, graph_steps=g.value, eager_steps=e.value)
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.asph_server_destroy(self._h)
             self._h = _vp()
 
     def __del__(self):

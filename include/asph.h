@@ -370,6 +370,17 @@ asph_status asph_simulation_kernel_times(asph_simulation* sim, double* ms, uint3
 /* Number of kernels this library launched on the simulation's stream since create (all classes). */
 asph_status asph_simulation_launch_count(const asph_simulation* sim, uint64_t* out);
 
+/* Device memory a simulation holds, and the same figure for a simulation not yet created (what
+ * asph_simulation_create would allocate for these arguments); no reference counterpart. */
+asph_status asph_simulation_device_bytes(const asph_simulation* sim, uint64_t* out);
+asph_status asph_estimate_device_bytes(const asph_parameters* parameters,
+                                       uint32_t count,
+                                       uint32_t boundary_count,
+                                       const asph_refinement_parameters* refinement,
+                                       uint32_t max_fluid_capacity,
+                                       uint32_t max_boundary_capacity,
+                                       uint64_t* out);
+
 /* ---------------------------------------------------------------------------------------------
  * Batches (no reference counterpart): independent simulations advanced together. Each simulation
  * keeps its own streams, so their steps overlap on the device; plain steps are captured once as
@@ -388,6 +399,62 @@ asph_status asph_batch_step(asph_batch* batch, const float* dts, uint32_t steps)
 /* Steps replayed from graphs, steps run eagerly (refinement frames), graph captures so far. */
 asph_status asph_batch_stats(const asph_batch* batch, uint64_t* graph_steps, uint64_t* eager_steps,
                              uint64_t* captures);
+
+/* ---------------------------------------------------------------------------------------------
+ * Serving loop (no reference counterpart): scene requests are submitted at any time, admitted first
+ * come first served while the device memory they need (asph_estimate_device_bytes, capacity
+ * included, so split headroom is reserved at admission) fits the budget, advanced together with all
+ * other admitted requests (their steps overlap on the device, as in a batch), and retired when their
+ * step count is reached: the particles are copied to host memory and the device memory returns to
+ * the budget. Each request's result equals the one it gives when run alone. Times are seconds since
+ * the server's creation (monotonic clock).
+ * ------------------------------------------------------------------------------------------- */
+typedef struct asph_server asph_server;
+
+typedef struct asph_request {
+    asph_parameters parameters;
+    const float* positions; /* host, 4 floats per particle; copied at submission */
+    uint32_t count;
+    const asph_boundary_particle* boundary; /* host; copied at submission */
+    uint32_t boundary_count;
+    const asph_refinement_parameters* refinement; /* NULL or disabled: plain */
+    uint32_t max_fluid_capacity;                  /* plain: at least count (adaptive: refinement->max_particle_count) */
+    float delta_time;
+    uint32_t steps;
+} asph_request;
+
+#define ASPH_REQUEST_QUEUED 0u
+#define ASPH_REQUEST_ACTIVE 1u
+#define ASPH_REQUEST_DONE 2u
+#define ASPH_REQUEST_FAILED 3u
+
+typedef struct asph_request_status {
+    uint32_t state; /* ASPH_REQUEST_* */
+    uint32_t steps_done;
+    uint32_t steps;
+    uint32_t count;      /* particles of the result (done) */
+    asph_status error;   /* failed: why */
+    uint64_t device_bytes;
+    double submit_s, admit_s, finish_s;
+} asph_request_status;
+
+/* max_active: most requests running at once (0: 1024). */
+asph_status asph_server_create(uint64_t memory_budget_bytes, uint32_t max_active, asph_server** out);
+/* Releases every request, finished or not. */
+void asph_server_destroy(asph_server* server);
+/* Queues a request; ASPH_ERR_CAPACITY if it could never fit the budget. May be called from another
+ * thread than the one polling. */
+asph_status asph_server_submit(asph_server* server, const asph_request* request, uint64_t* ticket);
+/* Admits what fits, advances every running request by up to max_steps steps (0: to its end), retires
+ * the finished ones; returns when those steps are done. *outstanding: requests queued or running. */
+asph_status asph_server_poll(asph_server* server, uint32_t max_steps, uint32_t* outstanding);
+asph_status asph_server_status(asph_server* server, uint64_t ticket, asph_request_status* out);
+/* Copies a finished request's particles (as asph_simulation_export_host) and forgets the request; a
+ * failed request returns its error and is forgotten. */
+asph_status asph_server_take(asph_server* server, uint64_t ticket, float* positions, float* velocities,
+                             float* densities, float* radii, uint32_t* ids, uint32_t capacity);
+asph_status asph_server_stats(const asph_server* server, uint64_t* used_bytes, uint32_t* queued, uint32_t* active,
+                              uint64_t* graph_steps, uint64_t* eager_steps);
 
 /* ---------------------------------------------------------------------------------------------
  * Cell sort without allocation. No counterpart in the reference: it is the cell-key computation and

@@ -59,6 +59,8 @@ STRUCTS = {
     "asph_state_info": P.CStateInfo,
     "asph_grid_info": P.CGridInfo,
     "asph_refinement_report": P.CRefinementReport,
+    "asph_request": P.CRequest,
+    "asph_request_status": P.CRequestStatus,
 }
 
 

@@ -1,0 +1,105 @@
+"""The serving loop: requests admitted under a device-memory budget, run together, retired; each result equals the
+request run alone, bit for bit, and the budget is never exceeded."""
+import numpy as np
+import pytest
+
+from adaptivesph_gb300 import Server, create_simulation, estimate_device_bytes
+from helpers import adaptive_refinement, assert_bitexact, boundary_of, small_dam_break
+
+
+
+def _requests():
+    return [
+        (small_dam_break(), 30),
+        (small_dam_break(counts=(8, 12, 8), seed=3), 45),
+        (small_dam_break(refinement=adaptive_refinement()), 25),
+        (small_dam_break(counts=(12, 16, 8), seed=5, refinement=adaptive_refinement(cooldown=4)), 40),
+        (small_dam_break(counts=(6, 10, 6), seed=8), 12),
+    ]
+
+
+def _alone(sc, steps):
+    bd = boundary_of(sc)
+    cap = sc.refinement.max_particle_count if sc.refinement else sc.positions.shape[0]
+    sim = create_simulation(sc.parameters, sc.positions, None, None, bd, sc.refinement, cap,
+                            max(bd.get_particle_count(), 1))
+    for _ in range(steps):
+        sim.update(sc.dt)
+    out = sim.export_host()
+    sim.close()
+    return out
+
+
+def _bytes(sc):
+    bd = boundary_of(sc)
+    cap = sc.refinement.max_particle_count if sc.refinement else sc.positions.shape[0]
+    return estimate_device_bytes(sc.parameters, sc.positions.shape[0], bd.get_particle_count(), sc.refinement, cap)
+
+
+@pytest.mark.gpu
+def test_server_results_equal_alone_under_a_budget():
+    reqs = _requests()
+    sizes = [_bytes(sc) for sc, _ in reqs]
+    budget = int(sum(sorted(sizes)[-2:]) * 1.01)  # room for about two requests at a time: admission must wait
+    server = Server(budget)
+    tickets = []
+    for sc, steps in reqs:
+        tickets.append(server.submit(sc.parameters, sc.positions, boundary_of(sc), sc.refinement, sc.dt, steps,
+                                     sc.refinement.max_particle_count if sc.refinement else None))
+    seen_queue = False
+    while True:
+        left = server.poll(7)
+        st = server.stats()
+        assert st["used_bytes"] <= budget
+        seen_queue |= st["queued"] > 0
+        if left == 0:
+            break
+    assert seen_queue, "the budget must make requests wait"
+    for (sc, steps), t in zip(reqs, tickets):
+        s = server.status(t)
+        assert s["state"] == "done" and s["steps_done"] == steps
+        assert s["submit_s"] <= s["admit_s"] <= s["finish_s"]
+        got = server.take(t)
+        want = _alone(sc, steps)
+        for k in ("ids", "positions", "velocities", "densities", "radii"):
+            assert_bitexact(k, got[k], want[k])
+    server.close()
+
+
+def test_server_queue_and_budget_on_the_host():
+    """Host-only part of the server (no GPU): requests that could never fit are refused, the others queue in order
+    with their memory estimate."""
+    from adaptivesph_gb300 import AsphError
+
+    sc = small_dam_break()
+    need = _bytes(sc)
+    server = Server(need // 2)
+    with pytest.raises(AsphError):
+        server.submit(sc.parameters, sc.positions, boundary_of(sc), None, sc.dt, 5)
+    server.close()
+    server = Server(3 * need)
+    t1 = server.submit(sc.parameters, sc.positions, boundary_of(sc), None, sc.dt, 5)
+    t2 = server.submit(sc.parameters, sc.positions, boundary_of(sc), None, sc.dt, 7)
+    for t, steps in ((t1, 5), (t2, 7)):
+        s = server.status(t)
+        assert s["state"] == "queued" and s["steps"] == steps and s["device_bytes"] == need
+    assert server.stats()["queued"] == 2
+    server.close()
+
+
+@pytest.mark.gpu
+def test_estimate_matches_device_memory():
+    torch = pytest.importorskip("torch")
+    sc = small_dam_break(counts=(40, 40, 40), refinement=adaptive_refinement(capacity=300000))
+    bd = boundary_of(sc)
+    est = _bytes(sc)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    sim = create_simulation(sc.parameters, sc.positions, None, None, bd, sc.refinement, 300000,
+                            bd.get_particle_count())
+    torch.cuda.synchronize()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert sim.device_bytes() == est
+    used = free0 - free1
+    assert abs(used - est) <= 0.05 * est + (64 << 20), (used, est)
+    sim.close()
