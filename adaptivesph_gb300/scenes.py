@@ -149,3 +149,28 @@ def batched_mix(count: int = 256, seed: int = 4, dx: float = 0.01, min_particles
         s.name = f"mix_{k:03d}"
         out.append(s)
     return out
+
+
+def served_requests(count: int = 24, seed: int = 5, min_particles: int = 8192, max_particles: int = 1_000_000,
+                    refinement_probability: float = 0.5, min_steps: int = 200, max_steps: int = 2000):
+    """Scene requests for the serving loop: dam breaks whose spacing gives a particle count log-uniform in
+    [min_particles, max_particles] (nx x 2nx x nx lattice in a 1.6 x 1.0 x 0.67 m tank, the column 0.8 m high),
+    refinement (velocity criterion, two split levels) with the given probability, a step count uniform in
+    [min_steps, max_steps]. Returns (scene, steps) pairs in arrival order."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        n_target = math.exp(rng.uniform(math.log(min_particles), math.log(max_particles)))
+        nx = max(8, int(round((n_target / 2.0) ** (1.0 / 3.0))))
+        dx = 0.4 / nx  # the column is 0.4 m wide and 0.8 m high, whatever the resolution
+        refine = rng.uniform() < refinement_probability
+        steps = int(rng.integers(min_steps, max_steps + 1))
+        refinement = None
+        if refine:
+            refinement = RefinementParameters(enabled=True, min_mass_ratio=0.05, max_mass_ratio=8.0,
+                                              max_particle_count=2 * (2 * nx ** 3), max_batch_ratio=0.2,
+                                              initial_cooldown=10, cooldown=10, criterion=Criterion.VELOCITY)
+        s = dam_break((nx, 2 * nx, nx), dx, seed=seed * 1000 + k, refinement=refinement, column_height=0.8)
+        s.name = f"request_{k:03d}"
+        out.append((s, steps))
+    return out

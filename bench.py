@@ -444,6 +444,108 @@ def run_batched(args, rank: int, world: int, dist):
     }
 
 
+# ------------------------------------------------------------------------------------------------ served
+def _pct(v, q):
+    return float(np.percentile(np.asarray(v, np.float64), q)) if len(v) else None
+
+
+def run_served(args, rank: int, world: int, dist):
+    """Scene requests (scenes.served_requests) arriving as a Poisson stream at each rate of --rates, served by
+    asph_server (continuous batching under a device-memory budget), against the same requests run one at a time in
+    arrival order (first come first served, each alone through asph_simulation_update); latency = finish - arrival."""
+    import torch
+
+    from adaptivesph_gb300 import Server, StaticBoundaryDomain, create_simulation, scenes
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    reqs = scenes.served_requests(count=args.requests)
+    bds = [StaticBoundaryDomain.generate(sc.parameters.domain, sc.boundary_spacing, sc.parameters.rest_density,
+                                         sc.parameters.base_smoothing_radius) for sc, _ in reqs]
+    work = float(sum(sc.positions.shape[0] * steps for sc, steps in reqs))
+    budget = int(args.budget_gb * 1e9)
+    # sequential: every request alone, its service time measured; queueing follows from the arrival times
+    service = []
+    for (sc, steps), bd in zip(reqs, bds):
+        cap = sc.refinement.max_particle_count if sc.refinement else sc.positions.shape[0]
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        sim = create_simulation(sc.parameters, sc.positions, None, None, bd, sc.refinement, cap,
+                                bd.get_particle_count())
+        for _ in range(steps):
+            sim.update(sc.dt)
+        sim.export_host()
+        service.append(time.perf_counter() - t)
+        sim.close()
+    rng = np.random.default_rng(5)
+    results = []
+    for rate in args.rates:
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, size=len(reqs)))
+        # sequential first come first served
+        t_free, seq_lat = 0.0, []
+        for a, s in zip(arrivals, service):
+            start = max(a, t_free)
+            t_free = start + s
+            seq_lat.append(t_free - a)
+        seq_makespan = t_free
+        # served
+        server = Server(budget)
+        t0 = time.perf_counter()  # the server's clock starts with it: arrival times are on the same clock
+        tickets, nxt = [], 0
+        while True:
+            now = time.perf_counter() - t0
+            while nxt < len(reqs) and arrivals[nxt] <= now:
+                sc, steps = reqs[nxt]
+                tickets.append(server.submit(sc.parameters, sc.positions, bds[nxt], sc.refinement, sc.dt, steps,
+                                             sc.refinement.max_particle_count if sc.refinement else None))
+                nxt += 1
+            left = server.poll(args.poll_steps)
+            if left == 0:
+                if nxt == len(reqs):
+                    break
+                time.sleep(max(0.0, min(0.01, arrivals[nxt] - (time.perf_counter() - t0))))
+        lat, finish = [], []
+        for k, t in enumerate(tickets):
+            st = server.status(t)
+            assert st["state"] == "done", st
+            lat.append(st["finish_s"] - arrivals[k])
+            finish.append(st["finish_s"])
+            server.take(t)
+        stats = server.stats()
+        server.close()
+        makespan = max(finish)
+        results.append({
+            "rate_per_s": rate,
+            "served": {"scenes_per_s": len(reqs) / makespan, "particle_steps_per_s": work / makespan,
+                       "latency_s": {"p50": _pct(lat, 50), "p95": _pct(lat, 95), "p99": _pct(lat, 99)},
+                       "graph_steps": stats["graph_steps"], "eager_steps": stats["eager_steps"]},
+            "sequential": {"scenes_per_s": len(reqs) / seq_makespan, "particle_steps_per_s": work / seq_makespan,
+                           "latency_s": {"p50": _pct(seq_lat, 50), "p95": _pct(seq_lat, 95),
+                                         "p99": _pct(seq_lat, 99)}},
+        })
+    if rank != 0:
+        return None
+    best = max(r["served"]["particle_steps_per_s"] for r in results)
+    seq_best = max(r["sequential"]["particle_steps_per_s"] for r in results)
+    return {
+        "metric": "particle-steps/s, served scene requests",
+        "value": best,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": int(sum(s for _, s in reqs)),
+        "warmup": 0,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded requests and Poisson arrivals; no dataset involved)",
+        "config": {"workload": f"{len(reqs)} dam-break requests, 8k-1M particles (log-uniform), refinement p=0.5, "
+                               f"200-2000 steps, Poisson arrivals", "budget_bytes": budget,
+                   "poll_steps": args.poll_steps, "parallelism": f"replicas x{world}"},
+        "speedup_vs_sequential": best / seq_best,
+        "rates": results,
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -453,8 +555,13 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=10)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
-    ap.add_argument("--workload", choices=["adaptive1m", "batched"], default="adaptive1m",
-                    help="adaptive1m: the headline 1M adaptive dam break; batched: the scene mix through asph_batch")
+    ap.add_argument("--workload", choices=["adaptive1m", "batched", "served"], default="adaptive1m",
+                    help="adaptive1m: the headline 1M adaptive dam break; batched: the scene mix through asph_batch; "
+                         "served: Poisson scene requests through asph_server")
+    ap.add_argument("--requests", type=int, default=24, help="requests of the served workload")
+    ap.add_argument("--rates", type=float, nargs="+", default=[5.0, 50.0, 200.0], help="arrival rates (1/s)")
+    ap.add_argument("--budget-gb", type=float, default=150.0, help="device-memory budget of the server")
+    ap.add_argument("--poll-steps", type=int, default=50, help="steps per server poll")
     ap.add_argument("--scenes", type=int, default=256, help="scenes of the batched mix")
     ap.add_argument("--capacity", type=int, default=0,
                     help="particle capacity (default: the workload's 4M); a smaller one keeps profiling runs small")
@@ -477,7 +584,8 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         tdist.init_process_group("nccl")
         dist = tdist
-    line = run_batched(args, rank, world, dist) if args.workload == "batched" else run_ours(args, rank, world, dist)
+    runners = {"batched": run_batched, "served": run_served, "adaptive1m": run_ours}
+    line = runners[args.workload](args, rank, world, dist)
     if line is not None:
         print(json.dumps(line), flush=True)
     if dist is not None:
