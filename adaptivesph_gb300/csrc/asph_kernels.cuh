@@ -132,5 +132,7 @@ void sort_scratch_bind(SortScratch& s, void* base, uint32_t max_items);
 // ping-pong buffers are swapped back if the number of passes is odd). Returns the number of kernels launched.
 int radix_sort_pairs(uint32_t*& keys, uint32_t*& vals, const uint32_t* d_n, uint32_t n_max, uint32_t key_bits,
                      SortScratch& s, uint32_t* err, cudaStream_t stream);
+// A digit pass whose look-back wait runs out on purpose (failure-detection test); see radix_sort.cu.
+cudaError_t radix_sort_wait_probe(uint32_t* err, cudaStream_t stream);
 
 }  // namespace asph

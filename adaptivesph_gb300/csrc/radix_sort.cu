@@ -202,4 +202,46 @@ int radix_sort_pairs(uint32_t*& keys, uint32_t*& vals, const uint32_t* d_n, uint
     return launches;
 }
 
+// The bounded wait, made to run out: one digit pass of two tiles in which only the second tile's block runs (the
+// tile counter starts at 1), so its look-back waits on a predecessor that never publishes. The block gives up after
+// kSpinLimit polls, records ASPH_DEVERR_SPIN_LIMIT in err and finishes its tile (with an incomplete prefix; every
+// position stays inside the arrays). Used by the failure-detection test; returns the first CUDA error.
+cudaError_t radix_sort_wait_probe(uint32_t* err, cudaStream_t stream) {
+    constexpr uint32_t n = 2 * kSortTile;
+    uint32_t *keys = nullptr, *vals = nullptr, *keys_out = nullptr, *vals_out = nullptr, *scratch = nullptr;
+    // scratch: count, digit counts of the pass, offsets, tile counter, look-back words of both tiles
+    const size_t words = 1 + 4 * 256 + 1 + 2 * 256;
+    cudaError_t e = cudaMalloc(&keys, sizeof(uint32_t) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&vals, sizeof(uint32_t) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&keys_out, sizeof(uint32_t) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&vals_out, sizeof(uint32_t) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&scratch, sizeof(uint32_t) * words);
+    if (e == cudaSuccess) {
+        uint32_t* d_n = scratch;
+        uint32_t* hist = scratch + 1;
+        uint32_t* counter = hist + 4 * 256;
+        uint32_t* lookback = counter + 1;
+        e = cudaMemsetAsync(keys, 0, sizeof(uint32_t) * n, stream);  // every key in digit 0
+        if (e == cudaSuccess) e = cudaMemsetAsync(vals, 0, sizeof(uint32_t) * n, stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(scratch, 0, sizeof(uint32_t) * words, stream);
+        const uint32_t host[2] = {n, 1u};
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d_n, &host[0], sizeof(uint32_t), cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(counter, &host[1], sizeof(uint32_t), cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) {
+            k_sort_hist<<<1, 256, 0, stream>>>(keys, d_n, 1, hist);
+            k_sort_scan<<<1, 256, 0, stream>>>(hist, 1);
+            k_sort_onesweep<<<1, kSortThreads, 0, stream>>>(keys, vals, keys_out, vals_out, d_n, 0, hist, lookback,
+                                                            counter, err);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    }
+    cudaFree(keys);
+    cudaFree(vals);
+    cudaFree(keys_out);
+    cudaFree(vals_out);
+    cudaFree(scratch);
+    return e;
+}
+
 }  // namespace asph

@@ -2024,3 +2024,18 @@ asph_status asph_estimate_device_bytes(const asph_parameters* parameters, uint32
 }
 
 }  // extern "C"
+
+// Failure detection without a fault (test hook, not in asph.h): runs a sort pass whose bounded look-back wait runs
+// out, and returns the error word it left (ASPH_DEVERR_SPIN_LIMIT expected); the context stays usable.
+extern "C" asph_status asph_debug_wait_limit_probe(uint32_t* error_word) {
+    API_ENTRY();
+    if (!error_word) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
+    uint32_t* err = nullptr;
+    CK(cudaMalloc(&err, sizeof(uint32_t)));
+    cudaError_t e = cudaMemset(err, 0, sizeof(uint32_t));
+    if (e == cudaSuccess) e = radix_sort_wait_probe(err, nullptr);
+    if (e == cudaSuccess) e = cudaMemcpy(error_word, err, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    cudaFree(err);
+    if (e != cudaSuccess) return cuda_fail(e, "wait-limit probe");
+    return ASPH_OK;
+}
