@@ -97,11 +97,13 @@ __global__ void k_boundary_reorder(GridDev g, const float4* pos_in, const float*
 // density and force passes (neighbour_kernels.cu): the ordinary kernel (one thread per particle) or the heavy
 // kernel (one warp per queued particle; for the density pass, over the box-heavy queue or the overflow queue)
 enum DensityKernel { kDensityOrdinary, kDensityHeavy, kDensityOverflow, kDensityRow };
-cudaError_t launch_density(DensityKernel kind, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c,
-                           BoundaryDev b, NbrDev nl);
+// `priority` (a stream priority value) is given to the heavy kernels' launches themselves, so that it holds when
+// the step is replayed from a CUDA graph too.
+cudaError_t launch_density(DensityKernel kind, uint32_t blocks, cudaStream_t stream, int priority, StepArgs a,
+                           CellsDev c, BoundaryDev b, NbrDev nl);
 enum ForceKernel { kForcesOrdinary, kForcesHeavy, kForcesRow };
-cudaError_t launch_forces(ForceKernel kind, bool morris, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c,
-                          BoundaryDev b, NbrDev nl);
+cudaError_t launch_forces(ForceKernel kind, bool morris, uint32_t blocks, cudaStream_t stream, int priority, StepArgs a,
+                          CellsDev c, BoundaryDev b, NbrDev nl);
 // number of reference cells of the query box [x - R, x + R] above which a particle is heavy
 constexpr int kHeavyCells = 27;
 __global__ void k_neighbor_counts(StepArgs a, CellsDev c, uint32_t* counts, unsigned long long* total);

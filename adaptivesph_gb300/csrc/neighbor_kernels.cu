@@ -17,6 +17,8 @@
 // canonical index (for_each_subcell_lane), each lane sums its sub-cells' members in order, and the lane sums are
 // combined by a fixed butterfly. They are queued for separate warp kernels, so a few large boxes do not stall
 // whole blocks.
+#include <utility>
+
 #include "asph_device.cuh"
 #include "asph_kernels.cuh"
 
@@ -636,11 +638,28 @@ __global__ void __launch_bounds__(256, 2) k_forces_row(StepArgs a, BoundaryDev b
 // The ordinary and the box-heavy kernels of a pass are independent of each other (the heavy queue is filled by the
 // reorder kernel), so the host runs them on two streams; the overflow queue is filled by k_density and summed
 // after it on its stream.
-cudaError_t launch_density(DensityKernel kind, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c,
-                           BoundaryDev b, NbrDev nl) {
+// A launch of 256-thread blocks with a launch priority (kept by graph capture, unlike the stream's).
+template <class... Exp, class... Act>
+cudaError_t launch_with_priority(void (*kernel)(Exp...), uint32_t blocks, cudaStream_t stream, int priority,
+                                 Act&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(256);
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributePriority;
+    attr[0].val.priority = priority;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Act>(args)...);
+}
+
+cudaError_t launch_density(DensityKernel kind, uint32_t blocks, cudaStream_t stream, int priority, StepArgs a,
+                           CellsDev c, BoundaryDev b, NbrDev nl) {
     if (kind == kDensityHeavy)
-        k_density_heavy<<<blocks, 256, 0, stream>>>(a, c, b, nl, nl.heavy, nl.heavy_n, true);
-    else if (kind == kDensityOverflow)
+        return launch_with_priority(k_density_heavy, blocks, stream, priority, a, c, b, nl, (const uint32_t*)nl.heavy,
+                                    (const uint32_t*)nl.heavy_n, true);
+    if (kind == kDensityOverflow)
         k_density_heavy<<<blocks, 256, 0, stream>>>(a, c, b, nl, nl.dover, nl.dover_n, false);
     else if (kind == kDensityRow)
         k_density_row<<<blocks, 256, 0, stream>>>(a, b, nl);
@@ -651,14 +670,13 @@ cudaError_t launch_density(DensityKernel kind, uint32_t blocks, cudaStream_t str
     return cudaGetLastError();
 }
 
-cudaError_t launch_forces(ForceKernel kind, bool morris, uint32_t blocks, cudaStream_t stream, StepArgs a, CellsDev c,
-                          BoundaryDev b, NbrDev nl) {
+cudaError_t launch_forces(ForceKernel kind, bool morris, uint32_t blocks, cudaStream_t stream, int priority, StepArgs a,
+                          CellsDev c, BoundaryDev b, NbrDev nl) {
     if (kind == kForcesHeavy) {
-        if (morris)
-            k_forces_heavy<true><<<blocks, 256, 0, stream>>>(a, c, b, nl);
-        else
-            k_forces_heavy<false><<<blocks, 256, 0, stream>>>(a, c, b, nl);
-    } else if (kind == kForcesRow) {
+        if (morris) return launch_with_priority(k_forces_heavy<true>, blocks, stream, priority, a, c, b, nl);
+        return launch_with_priority(k_forces_heavy<false>, blocks, stream, priority, a, c, b, nl);
+    }
+    if (kind == kForcesRow) {
         if (morris)
             k_forces_row<true><<<blocks, 256, 0, stream>>>(a, b, nl);
         else

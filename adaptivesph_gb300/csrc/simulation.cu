@@ -218,6 +218,7 @@ struct asph_simulation {
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;
     cudaStream_t aux = nullptr;  // heavy-particle kernels, forked from and joined back into `stream`
+    int heavy_priority = 0;      // the device's highest stream priority, given to the heavy kernels
     cudaEvent_t ev_fork = nullptr, ev_main = nullptr, ev_aux = nullptr;
     cudaEvent_t ev_refine = nullptr;  // end of a refinement pass whose read-back has not been taken yet
     bool refine_pending = false;
@@ -574,10 +575,10 @@ asph_status run_density(asph_simulation* s) {
     CK(cudaMemsetAsync(s->fheavy_n, 0, 4 * sizeof(uint32_t), s->stream));
     CK(cudaEventRecord(s->ev_fork, s->stream));
     CK(cudaStreamWaitEvent(s->aux, s->ev_fork, 0));
-    CK(launch_density(kDensityHeavy, kHeavyBlocks, s->aux, a, s->cells(), s->boundary(), s->nbrs()));
-    CK(launch_density(kDensityOrdinary, blocks_for(s->span()), s->stream, a, s->cells(), s->boundary(), s->nbrs()));
-    CK(launch_density(kDensityOverflow, kHeavyBlocks, s->stream, a, s->cells(), s->boundary(), s->nbrs()));
-    CK(launch_density(kDensityRow, kHeavyBlocks, s->stream, a, s->cells(), s->boundary(), s->nbrs()));
+    CK(launch_density(kDensityHeavy, kHeavyBlocks, s->aux, s->heavy_priority, a, s->cells(), s->boundary(), s->nbrs()));
+    CK(launch_density(kDensityOrdinary, blocks_for(s->span()), s->stream, 0, a, s->cells(), s->boundary(), s->nbrs()));
+    CK(launch_density(kDensityOverflow, kHeavyBlocks, s->stream, 0, a, s->cells(), s->boundary(), s->nbrs()));
+    CK(launch_density(kDensityRow, kHeavyBlocks, s->stream, 0, a, s->cells(), s->boundary(), s->nbrs()));
     CK(cudaEventRecord(s->ev_main, s->stream));
     CK(cudaEventRecord(s->ev_aux, s->aux));
     CK(cudaStreamWaitEvent(s->stream, s->ev_aux, 0));
@@ -590,11 +591,11 @@ asph_status run_forces(asph_simulation* s) {
     StepArgs a = s->args(s->cur);
     int h = s->tic();
     CK(cudaStreamWaitEvent(s->aux, s->ev_main, 0));
-    CK(launch_forces(kForcesHeavy, s->phys.morris != 0, kHeavyBlocks, s->aux, a, s->cells(), s->boundary(),
+    CK(launch_forces(kForcesHeavy, s->phys.morris != 0, kHeavyBlocks, s->aux, s->heavy_priority, a, s->cells(), s->boundary(),
                      s->nbrs()));
-    CK(launch_forces(kForcesOrdinary, s->phys.morris != 0, blocks_for(s->span()), s->stream, a, s->cells(), s->boundary(),
+    CK(launch_forces(kForcesOrdinary, s->phys.morris != 0, blocks_for(s->span()), s->stream, 0, a, s->cells(), s->boundary(),
                      s->nbrs()));
-    CK(launch_forces(kForcesRow, s->phys.morris != 0, kHeavyBlocks, s->stream, a, s->cells(), s->boundary(),
+    CK(launch_forces(kForcesRow, s->phys.morris != 0, kHeavyBlocks, s->stream, 0, a, s->cells(), s->boundary(),
                      s->nbrs()));
     CK(cudaEventRecord(s->ev_aux, s->aux));
     CK(cudaStreamWaitEvent(s->stream, s->ev_aux, 0));
@@ -1072,6 +1073,7 @@ asph_status asph_simulation_create(const asph_parameters* parameters, const floa
     int prio_least = 0, prio_greatest = 0;
     e = cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s->aux, cudaStreamNonBlocking, prio_greatest);
+    s->heavy_priority = prio_greatest;
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_main, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_aux, cudaEventDisableTiming);
@@ -1858,7 +1860,8 @@ asph_status capture_step(asph_simulation* s, SceneGraph& g, float dt) {
         return st;
     }
     if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
-    const cudaError_t ie = cudaGraphInstantiate(&g.exec[parity], graph, 0);
+    // per-node priorities: the heavy kernels keep the priority they were launched with (launch_with_priority)
+    const cudaError_t ie = cudaGraphInstantiateWithFlags(&g.exec[parity], graph, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(graph);
     if (ie != cudaSuccess) {
         g.exec[parity] = nullptr;
