@@ -122,6 +122,38 @@ __device__ __forceinline__ bool density_term(const StepArgs& a, float4 pi, uint3
     return true;
 }
 
+// density_term for two neighbours, in packed FP32x2 arithmetic (each half rounds as the scalar operation), added in
+// order: j1 then j2.
+template <bool kPeriodic>
+__device__ __forceinline__ void density_pair(const StepArgs& a, float4 pi, uint32_t j1, float s1x, float s1y,
+                                             float s1z, uint32_t j2, float s2x, float s2y, float s2z, float& rho) {
+    const float4 p1 = __ldg(a.ph + j1), p2 = __ldg(a.ph + j2);
+    const float4 k1 = __ldg(a.kc + j1), k2 = __ldg(a.kc + j2);
+    float2 x = make_float2(p1.x, p2.x), y = make_float2(p1.y, p2.y), z = make_float2(p1.z, p2.z);
+    if (kPeriodic) {
+        x = __fadd2_rn(x, make_float2(s1x, s2x));
+        y = __fadd2_rn(y, make_float2(s1y, s2y));
+        z = __fadd2_rn(z, make_float2(s1z, s2z));
+    }
+    const float2 dx = __fadd2_rn(x, make_float2(-pi.x, -pi.x));
+    const float2 dy = __fadd2_rn(y, make_float2(-pi.y, -pi.y));
+    const float2 dz = __fadd2_rn(z, make_float2(-pi.z, -pi.z));
+    const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+    const float2 h = make_float2(p1.w, p2.w);
+    const float2 twoh = __fadd2_rn(h, h);
+    const float2 t2h = __fmul2_rn(twoh, twoh);
+    const float2 r = make_float2(sqrtf(r2.x), sqrtf(r2.y));
+    // kernel_w(r, 1/h, coef/h^3) for both
+    const float2 q = __fmul2_rn(r, make_float2(k1.x, k2.x));
+    const float2 t = __ffma2_rn(make_float2(-0.5f, -0.5f), q, make_float2(1.0f, 1.0f));
+    const float2 tt = __fmul2_rn(t, t);
+    const float2 t4 = __fmul2_rn(tt, tt);
+    const float2 w = __fmul2_rn(__fmul2_rn(make_float2(k1.y, k2.y), t4),
+                                __ffma2_rn(make_float2(2.0f, 2.0f), q, make_float2(1.0f, 1.0f)));
+    if (r2.x <= t2h.x) rho = fmaf(k1.w, q.x > 2.0f ? 0.0f : w.x, rho);
+    if (r2.y <= t2h.y) rho = fmaf(k2.w, q.y > 2.0f ? 0.0f : w.y, rho);
+}
+
 // Boundary density of particle i over the cells of lane `lane` (BoundaryAlgorithm.cu:15-51).
 template <int kLanes>
 __device__ __forceinline__ float boundary_density(const StepArgs& a, const BoundaryDev& b, uint32_t i, float4 pi,
@@ -402,22 +434,36 @@ __global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, Boun
         nl.drow[atomicAdd(nl.drow_n, 1u)] = i;
         return;
     }
-    // the fluid sum over the row in canonical order (plain loads: the row was written by this thread)
+    // the fluid sum over the row in canonical order (plain loads: the row was written by this thread), two
+    // neighbours per iteration in packed FP32x2 arithmetic, added to rho one after the other
     {
         uint2 next = cnt > 0u ? row[0] : make_uint2(0u, 0u);
         uint32_t k = 1, first = 0, mask = 0;
         float shx = 0.0f, shy = 0.0f, shz = 0.0f;
-        for (;;) {
+        auto pull = [&](uint32_t& j, float& sx, float& sy, float& sz) -> bool {
             if (mask == 0u) {
-                if (k > cnt) break;
+                if (k > cnt) return false;
                 decode_entry(a.grid, next.x, first, shx, shy, shz);
                 mask = next.y;
                 if (k < cnt) next = row[k];
                 k++;
             }
-            const uint32_t j = first + (uint32_t)(__ffs(mask) - 1);
+            j = first + (uint32_t)(__ffs(mask) - 1);
             mask &= mask - 1u;
-            density_term(a, pi, j, shx, shy, shz, rho);
+            sx = shx;
+            sy = shy;
+            sz = shz;
+            return true;
+        };
+        for (;;) {
+            uint32_t j1, j2;
+            float s1x, s1y, s1z, s2x, s2y, s2z;
+            if (!pull(j1, s1x, s1y, s1z)) break;
+            if (!pull(j2, s2x, s2y, s2z)) {
+                density_term(a, pi, j1, s1x, s1y, s1z, rho);
+                break;
+            }
+            density_pair<periodic>(a, pi, j1, s1x, s1y, s1z, j2, s2x, s2y, s2z, rho);
         }
     }
     float rb = 0.0f;
