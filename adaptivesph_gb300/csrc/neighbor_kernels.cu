@@ -268,6 +268,126 @@ __device__ __forceinline__ void force_term(const StepArgs& a, const ForceCtx& c,
     }
 }
 
+// force_term for two neighbours: the per-pair quantities in packed FP32x2 arithmetic (each half rounds as the
+// scalar operation; divisions and square roots stay scalar), each accumulator updated for j1, then j2.
+template <bool kMorris, bool kPeriodic>
+__device__ __forceinline__ void force_pair(const StepArgs& a, const ForceCtx& c, uint32_t j1, float s1x, float s1y,
+                                           float s1z, uint32_t j2, float s2x, float s2y, float s2z, ForceAcc& f) {
+    const float4 p1 = __ldg(a.ph + j1), p2 = __ldg(a.ph + j2);
+    const float4 k1 = __ldg(a.kc + j1), k2 = __ldg(a.kc + j2);
+    const float2 rp1 = __ldg(a.rp + j1), rp2 = __ldg(a.rp + j2);
+    float4 v1 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), v2 = v1;
+    if (c.visc_on) {
+        v1 = __ldg(a.vm + j1);
+        v2 = __ldg(a.vm + j2);
+    }
+    float2 x = make_float2(p1.x, p2.x), y = make_float2(p1.y, p2.y), z = make_float2(p1.z, p2.z);
+    if (kPeriodic) {
+        x = __fadd2_rn(x, make_float2(s1x, s2x));
+        y = __fadd2_rn(y, make_float2(s1y, s2y));
+        z = __fadd2_rn(z, make_float2(s1z, s2z));
+    }
+    // d = p_i - p_j
+    const float2 dx = __fadd2_rn(make_float2(c.pi.x, c.pi.x), make_float2(-x.x, -x.y));
+    const float2 dy = __fadd2_rn(make_float2(c.pi.y, c.pi.y), make_float2(-y.x, -y.y));
+    const float2 dz = __fadd2_rn(make_float2(c.pi.z, c.pi.z), make_float2(-z.x, -z.y));
+    const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+    const float2 h = make_float2(p1.w, p2.w);
+    const float2 twoh = __fadd2_rn(h, h);
+    const float2 t2h = __fmul2_rn(twoh, twoh);
+    const bool ok1 = r2.x <= t2h.x, ok2 = r2.y <= t2h.y;
+    const float2 r = make_float2(sqrtf(r2.x), sqrtf(r2.y));
+    const float2 ir = make_float2(r.x > 0.0f ? 1.0f / r.x : 0.0f, r.y > 0.0f ? 1.0f / r.y : 0.0f);
+    float2 ux = __fmul2_rn(dx, ir), uy = __fmul2_rn(dy, ir), uz = __fmul2_rn(dz, ir);
+    if (!(r.x > 0.0f)) {
+        ux.x = 0.0f;
+        uy.x = 1.0f;
+        uz.x = 0.0f;
+    }
+    if (!(r.y > 0.0f)) {
+        ux.y = 0.0f;
+        uy.y = 1.0f;
+        uz.y = 0.0f;
+    }
+    // kernel_dw(r, 1/h, dcoef/h^4)
+    const float2 q = __fmul2_rn(r, make_float2(k1.x, k2.x));
+    const float2 t = __ffma2_rn(make_float2(-0.5f, -0.5f), q, make_float2(1.0f, 1.0f));
+    const float2 t3 = __fmul2_rn(__fmul2_rn(t, t), t);
+    float2 dw = __fmul2_rn(__fmul2_rn(make_float2(k1.z, k2.z), q), t3);
+    if (q.x > 2.0f) dw.x = 0.0f;
+    if (q.y > 2.0f) dw.y = 0.0f;
+    const float2 m = make_float2(k1.w, k2.w);
+    const float2 sp = __fmul2_rn(__fmul2_rn(m, dw), __fadd2_rn(make_float2(c.pti, c.pti), make_float2(rp1.y, rp2.y)));
+    if (ok1) {
+        f.ap[0] = fmaf(-sp.x, ux.x, f.ap[0]);
+        f.ap[1] = fmaf(-sp.x, uy.x, f.ap[1]);
+        f.ap[2] = fmaf(-sp.x, uz.x, f.ap[2]);
+    }
+    if (ok2) {
+        f.ap[0] = fmaf(-sp.y, ux.y, f.ap[0]);
+        f.ap[1] = fmaf(-sp.y, uy.y, f.ap[1]);
+        f.ap[2] = fmaf(-sp.y, uz.y, f.ap[2]);
+    }
+    if (c.visc_on) {
+        const float2 vdx = __fadd2_rn(make_float2(c.vi.x, c.vi.x), make_float2(-v1.x, -v2.x));
+        const float2 vdy = __fadd2_rn(make_float2(c.vi.y, c.vi.y), make_float2(-v1.y, -v2.y));
+        const float2 vdz = __fadd2_rn(make_float2(c.vi.z, c.vi.z), make_float2(-v1.z, -v2.z));
+        const float2 rhoj = make_float2(rp1.x, rp2.x);
+        const float2 den = __fadd2_rn(r2, make_float2(c.ei, c.ei));
+        if (!kMorris) {
+            const float2 comp = __ffma2_rn(vdz, dz, __ffma2_rn(vdy, dy, __fmul2_rn(vdx, dx)));
+            const float2 rsum = __fadd2_rn(make_float2(c.rhoi, c.rhoi), rhoj);
+            if (ok1 && comp.x < 0.0f) {
+                const float nuij = c.Ki / rsum.x;
+                const float piv = (-nuij * comp.x) / den.x;
+                const float sv = (m.x * piv) * dw.x;
+                f.av[0] = fmaf(-sv, ux.x, f.av[0]);
+                f.av[1] = fmaf(-sv, uy.x, f.av[1]);
+                f.av[2] = fmaf(-sv, uz.x, f.av[2]);
+            }
+            if (ok2 && comp.y < 0.0f) {
+                const float nuij = c.Ki / rsum.y;
+                const float piv = (-nuij * comp.y) / den.y;
+                const float sv = (m.y * piv) * dw.y;
+                f.av[0] = fmaf(-sv, ux.y, f.av[0]);
+                f.av[1] = fmaf(-sv, uy.y, f.av[1]);
+                f.av[2] = fmaf(-sv, uz.y, f.av[2]);
+            }
+        } else {
+            const float2 mnu = __fmul2_rn(m, make_float2(a.phys.nu, a.phys.nu));
+            const float2 num = __fmul2_rn(mnu, __fadd2_rn(make_float2(c.rhoi, c.rhoi), rhoj));
+            const float2 prod = __fmul2_rn(make_float2(c.rhoi, c.rhoi), rhoj);
+            const float2 rdw = __fmul2_rn(r, dw);
+            if (ok1) {
+                const float sv = (num.x / prod.x) * (rdw.x / den.x);
+                f.av[0] = fmaf(sv, vdx.x, f.av[0]);
+                f.av[1] = fmaf(sv, vdy.x, f.av[1]);
+                f.av[2] = fmaf(sv, vdz.x, f.av[2]);
+            }
+            if (ok2) {
+                const float sv = (num.y / prod.y) * (rdw.y / den.y);
+                f.av[0] = fmaf(sv, vdx.y, f.av[0]);
+                f.av[1] = fmaf(sv, vdy.y, f.av[1]);
+                f.av[2] = fmaf(sv, vdz.y, f.av[2]);
+            }
+        }
+    }
+    if (c.sigma_on) {
+        if (ok1) {
+            const float ss = m.x * kernel_w(r.x, k1.x, k1.y);
+            f.as[0] = fmaf(ss, ux.x, f.as[0]);
+            f.as[1] = fmaf(ss, uy.x, f.as[1]);
+            f.as[2] = fmaf(ss, uz.x, f.as[2]);
+        }
+        if (ok2) {
+            const float ss = m.y * kernel_w(r.y, k2.x, k2.y);
+            f.as[0] = fmaf(ss, ux.y, f.as[0]);
+            f.as[1] = fmaf(ss, uy.y, f.as[1]);
+            f.as[2] = fmaf(ss, uz.y, f.as[2]);
+        }
+    }
+}
+
 // Boundary pressure and friction (BoundaryAlgorithm.cu:53-162) over the cells of lane `lane`.
 template <int kLanes>
 __device__ __forceinline__ void boundary_forces(const StepArgs& a, const BoundaryDev& b, uint32_t i,
@@ -537,23 +657,43 @@ __global__ void __launch_bounds__(256, 3) k_forces(StepArgs a, CellsDev c, Bound
     if (cnt > kRowHeavy) return;  // long row (k_forces_row), overflowed or heavy (k_forces_heavy)
     const ForceCtx x = force_ctx(a, i);
     ForceAcc f = {};
-    // One neighbour per iteration (the row's masks expanded in order), so a warp runs as many iterations as its
-    // lane with the most neighbours; the next entry is fetched as soon as the current one is decoded.
+    // Two neighbours per iteration (the row's masks expanded in order, the particle itself skipped), so a warp runs
+    // half as many iterations as its lane with the most neighbours; the next entry is fetched as soon as the
+    // current one is decoded.
     const uint2* row = nl.ent + (size_t)i * nl.maxe;
     uint2 next = cnt > 0u ? __ldg(row) : make_uint2(0u, 0u);
     uint32_t k = 1, first = 0, mask = 0;
     float shx = 0.0f, shy = 0.0f, shz = 0.0f;
-    for (;;) {
-        if (mask == 0u) {
-            if (k > cnt) break;
-            decode_entry(a.grid, next.x, first, shx, shy, shz);
-            mask = next.y;
-            if (k < cnt) next = __ldg(row + k);
-            k++;
+    auto pull = [&](uint32_t& j, float& sx, float& sy, float& sz) -> bool {
+        for (;;) {
+            if (mask == 0u) {
+                if (k > cnt) return false;
+                decode_entry(a.grid, next.x, first, shx, shy, shz);
+                mask = next.y;
+                if (k < cnt) next = __ldg(row + k);
+                k++;
+            }
+            j = first + (uint32_t)(__ffs(mask) - 1);
+            mask &= mask - 1u;
+            sx = shx;
+            sy = shy;
+            sz = shz;
+            if (j != i) return true;
         }
-        const uint32_t j = first + (uint32_t)(__ffs(mask) - 1);
-        mask &= mask - 1u;
-        if (j != i) force_term<kMorris>(a, x, j, shx, shy, shz, f);
+    };
+    const bool periodic = a.grid.periodic;
+    for (;;) {
+        uint32_t j1, j2;
+        float s1x, s1y, s1z, s2x, s2y, s2z;
+        if (!pull(j1, s1x, s1y, s1z)) break;
+        if (!pull(j2, s2x, s2y, s2z)) {
+            force_term<kMorris>(a, x, j1, s1x, s1y, s1z, f);
+            break;
+        }
+        if (periodic)
+            force_pair<kMorris, true>(a, x, j1, s1x, s1y, s1z, j2, s2x, s2y, s2z, f);
+        else
+            force_pair<kMorris, false>(a, x, j1, s1x, s1y, s1z, j2, s2x, s2y, s2z, f);
     }
     if (boundary_near(a.grid, b, x.pi.x, x.pi.y, x.pi.z, x.hi + x.hi)) boundary_forces<1>(a, b, i, x, f, 0);
     finish_force(a, i, x, f);
