@@ -36,15 +36,20 @@ __device__ __forceinline__ uint64_t warp_min_u64(uint64_t v) {
 }
 
 // Two smallest values of the warp (a < b; ~0 when absent), merged into the global pair (S, T):
-// old = atomicMin(S, a); T <- min(T, max(old, a), b). Every value but the global minimum is offered to T.
+// old = atomicMin(S, a); T <- min(T, max(old, a), b). Every value but the global minimum is offered to T. T only
+// decreases and the values are distinct, so a value not below the T the warp reads can be neither of the final
+// two: such warps skip the atomics (most of them, once the first warps have run).
 __device__ __forceinline__ void top2_merge(uint64_t v, unsigned long long* S, unsigned long long* T) {
     const uint64_t a = warp_min_u64(v);
     const uint64_t second = warp_min_u64(v == a ? ~0ull : v);
     if ((threadIdx.x & 31) == 0 && a != ~0ull) {
-        const uint64_t old = atomicMin(S, (unsigned long long)a);
-        const uint64_t lost = old > a ? old : a;
-        atomicMin(T, (unsigned long long)lost);
-        if (second != ~0ull) atomicMin(T, (unsigned long long)second);
+        const uint64_t t_now = *reinterpret_cast<volatile unsigned long long*>(T);
+        if (a < t_now) {
+            const uint64_t old = atomicMin(S, (unsigned long long)a);
+            const uint64_t lost = old > a ? old : a;
+            atomicMin(T, (unsigned long long)lost);
+            if (second < t_now) atomicMin(T, (unsigned long long)second);
+        }
     }
 }
 
