@@ -19,6 +19,7 @@ struct StepArgs {
     float* rad;
     uint32_t* id;
     uint32_t* err;
+    float4* pq;   // x, y, z, (2h)^2: the support test's operands, written by the reorder kernel for the density scan
 };
 
 // The step's particle count: from the device when the step is replayed from a graph (the count may have changed

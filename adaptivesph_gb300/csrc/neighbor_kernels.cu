@@ -502,19 +502,18 @@ __global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, Boun
         uint32_t mask = 0;
         int k = (int)cn - 1;
         if ((cn & 1u) != 0u) {
-            const float4 pj = __ldg(a.ph + c0 + k);
+            const float4 pj = __ldg(a.pq + c0 + k);
             const float xj = periodic ? pj.x + shx : pj.x;
             const float yj = periodic ? pj.y + shy : pj.y;
             const float zj = periodic ? pj.z + shz : pj.z;
             const float dx = xj - pi.x, dy = yj - pi.y, dz = zj - pi.z;
             const float r2 = dist2(dx, dy, dz);
-            const float twoh = pj.w + pj.w;
-            mask = r2 <= twoh * twoh ? 1u : 0u;
+            mask = r2 <= pj.w ? 1u : 0u;
             --k;
         }
 #pragma unroll 2
         for (; k >= 1; k -= 2) {
-            const float4 p1 = __ldg(a.ph + c0 + k), p0 = __ldg(a.ph + c0 + k - 1);
+            const float4 p1 = __ldg(a.pq + c0 + k), p0 = __ldg(a.pq + c0 + k - 1);
             float2 x = make_float2(p1.x, p0.x), y = make_float2(p1.y, p0.y), z = make_float2(p1.z, p0.z);
             if (periodic) {
                 x = __fadd2_rn(x, make_float2(shx, shx));
@@ -523,10 +522,7 @@ __global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, Boun
             }
             const float2 dx = __fadd2_rn(x, nx), dy = __fadd2_rn(y, ny), dz = __fadd2_rn(z, nz);
             const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
-            const float2 h = make_float2(p1.w, p0.w);
-            const float2 twoh = __fadd2_rn(h, h);
-            const float2 t2 = __fmul2_rn(twoh, twoh);
-            mask = (mask << 2) | (r2.x <= t2.x ? 2u : 0u) | (r2.y <= t2.y ? 1u : 0u);
+            mask = (mask << 2) | (r2.x <= p1.w ? 2u : 0u) | (r2.y <= p0.w ? 1u : 0u);
         }
         if (mask != 0u) append(c0 | code, mask);
     };

@@ -143,6 +143,7 @@ struct asph_simulation {
     BufferSet set[2];
     int cur = 0;
     float4* kc = nullptr;
+    float4* pq = nullptr;  // [cap] x, y, z, (2h)^2 of the current step (StepArgs::pq)
     uint2* nbr_ent = nullptr;     // [kListEntries * cap] neighbour lists, one row per particle
     uint32_t* nbr_cnt = nullptr;  // [cap]
     uint32_t* heavy_idx = nullptr;  // [cap] queue of heavy particles of the current step
@@ -254,6 +255,7 @@ struct asph_simulation {
         a.id = set[s].id;
         a.kc = kc;
         a.err = err;
+        a.pq = pq;
         return a;
     }
 
@@ -332,7 +334,7 @@ uint64_t device_bytes_for(uint32_t C, uint32_t sort_items, uint32_t ncells, uint
     const uint64_t c = C;
     uint64_t b = 0;
     b += 2 * c * (sizeof(float4) * 3 + sizeof(float2) + sizeof(float) + sizeof(uint32_t));  // two buffer sets
-    b += c * sizeof(float4);                                                                // kernel constants
+    b += c * sizeof(float4) * 2;                                           // kernel constants, support operands
     b += c * kListEntries * sizeof(uint2) + c * sizeof(uint32_t);                          // rows and counts
     b += c * sizeof(uint32_t) * 5 + sizeof(uint32_t) * 5;                                   // queues
     const uint64_t slots = std::min<uint32_t>(kPoolSlots, std::max<uint32_t>(64u, C / 128u));
@@ -831,6 +833,7 @@ void destroy(asph_simulation* s) {
         dfree(s->set[k].id);
     }
     dfree(s->kc);
+    dfree(s->pq);
     dfree(s->nbr_ent);
     dfree(s->nbr_cnt);
     dfree(s->heavy_idx);
@@ -1097,6 +1100,7 @@ asph_status asph_simulation_create(const asph_parameters* parameters, const floa
         TRY(dalloc(s->set[k].id, C));
     }
     TRY(dalloc(s->kc, C));
+    TRY(dalloc(s->pq, C));
     TRY(dalloc(s->nbr_ent, (size_t)kListEntries * C));
     TRY(dalloc(s->nbr_cnt, C));
     TRY(dalloc(s->heavy_idx, C));

@@ -166,6 +166,8 @@ __global__ void __launch_bounds__(256) k_reorder_cells(StepArgs a, ReorderArgs r
     float invh, wc, dwc;
     kernel_consts(ph.w, invh, wc, dwc);
     a.kc[k] = make_float4(invh, wc, dwc, vm.w);
+    const float twoh = ph.w + ph.w;
+    a.pq[k] = make_float4(ph.x, ph.y, ph.z, twoh * twoh);
     if (r.heavy != nullptr && box_cells(a.grid, ph, ph.w + ph.w) > kHeavyCells) r.heavy[atomicAdd(r.heavy_n, 1u)] = k;
     const uint32_t lin = lin_of_key(a.grid, key);
     if (k == 0 || r.keys_sorted[k - 1] != key) r.start[lin] = k;
