@@ -2,7 +2,7 @@
  * asph.h — C ABI of the GB300-native AdaptiveSph per-step particle pipeline.
  *
  * Every entry point replaces one call of the reference's C++ simulation interface
- * (cuda/include/cuda/** in a-soltysik/AdaptiveSph). The reference interface each one
+ * (the headers under cuda/include/cuda in a-soltysik/AdaptiveSph). The reference interface each one
  * stands in for is cited beside it as path:line. Plain C types only: pointers, sizes,
  * POD structs. Every call returns an asph_status; asph_last_error() gives the message of
  * the last failing call on the calling thread.

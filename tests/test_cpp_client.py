@@ -1,6 +1,7 @@
-"""The C ABI from a C++ caller (tests/cpp/abi_client.cpp, compiled here with g++ against include/asph.h): generate
-walls, create, step, export. The compile and link run on the CPU; the run needs a GPU and is compared bit for bit
-with the oracle."""
+"""The C ABI from C++ callers, compiled here with g++: tests/cpp/abi_client.cpp against include/asph.h and
+tests/cpp/hpp_client.cpp against the reference-shaped classes of include/asph.hpp. Each generates walls, creates,
+steps and exports. The compile and link run on the CPU; the runs need a GPU and are compared bit for bit with the
+oracle."""
 import os
 import subprocess
 
@@ -15,15 +16,15 @@ from helpers import assert_bitexact, small_dam_break
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-@pytest.fixture(scope="module")
-def client(tmp_path_factory):
+@pytest.fixture(scope="module", params=["abi_client", "hpp_client"])
+def client(request, tmp_path_factory):
     _lib.load()
     lib = _lib.library_path()
-    exe = str(tmp_path_factory.mktemp("cpp") / "abi_client")
+    exe = str(tmp_path_factory.mktemp("cpp") / request.param)
     libdir = os.path.dirname(lib)
-    subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
-                    os.path.join(ROOT, "tests", "cpp", "abi_client.cpp"), "-o", exe, "-L", libdir, "-lasph_gb300",
-                    f"-Wl,-rpath,{libdir}"], check=True)
+    subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", request.param + ".cpp"), "-o", exe, "-L", libdir,
+                    "-lasph_gb300", f"-Wl,-rpath,{libdir}"], check=True)
     return exe
 
 
