@@ -290,10 +290,15 @@ __device__ __forceinline__ void for_each_cell(const GridDev& g, const uint32_t* 
 // visits those with t mod 32 == l, in increasing t. Excluded, empty and culled sub-cells are skipped (culling as in
 // for_each_cell<true>: reach = Rfix when Rfix > 0, else 2 * max h of the sub-cell); so the 32 lanes walk a large
 // box in 1/32 of the sequential walk, and each lane's visiting order is fixed by the box alone.
+// The walk is two-level: 32 reference cells at a time are tested against their max h (one cell per lane), and
+// only the surviving cells are opened. Lane l owns sub-cell (l mod 8) of the cells whose index in the box is
+// congruent to l / 8 modulo 4, so the four groups of 8 lanes open their own survivors side by side, each in
+// increasing cell order. The query (px, py, pz, R) must be the same on every lane.
 template <class Body>
 __device__ __forceinline__ void for_each_subcell_lane(const GridDev& g, const uint32_t* __restrict__ start,
                                                       const uint32_t* __restrict__ end,
-                                                      const float* __restrict__ hmax, uint32_t ex0, uint32_t ex1,
+                                                      const float* __restrict__ hmax,
+                                                      const float* __restrict__ hmax_ref, uint32_t ex0, uint32_t ex1,
                                                       float px, float py, float pz, float R, float Rfix, int lane,
                                                       Body&& body) {
     int32_t lo[3], hi[3];
@@ -304,34 +309,158 @@ __device__ __forceinline__ void for_each_subcell_lane(const GridDev& g, const ui
     if (!ok) return;
     const uint32_t nx = (uint32_t)(hi[0] - lo[0] + 1), ny = (uint32_t)(hi[1] - lo[1] + 1);
     const uint32_t nz = (uint32_t)(hi[2] - lo[2] + 1);
-    const uint32_t total = nx * ny * nz * 8u;
+    const uint32_t ncell = nx * ny * nz;
     const bool periodic = g.periodic;
     const float m = g.cull_margin;
-    for (uint32_t t = (uint32_t)lane; t < total; t += 32u) {
-        const uint32_t q = t & 7u, cell = t >> 3;
-        const uint32_t cxy = cell % (nx * ny);
-        float shx, shy, shz;
-        const int32_t cz = wrap_cell(lo[2] + (int32_t)(cell / (nx * ny)), g.gs[2], g.scale[2], periodic, shz);
-        const int32_t cy = wrap_cell(lo[1] + (int32_t)(cxy / nx), g.gs[1], g.scale[1], periodic, shy);
-        const int32_t cx = wrap_cell(lo[0] + (int32_t)(cxy % nx), g.gs[0], g.scale[0], periodic, shx);
-        if (cz < 0 || cz >= g.gs[2] || cy < 0 || cy >= g.gs[1] || cx < 0 || cx >= g.gs[0]) continue;
-        if (!periodic) {
-            const uint32_t rk =
-                (uint32_t)cx + (uint32_t)g.gs[0] * ((uint32_t)cy + (uint32_t)g.gs[1] * (uint32_t)cz);
-            if (rk == ex0 || rk == ex1) continue;
+    const uint32_t grp = (uint32_t)lane >> 3, q = (uint32_t)lane & 7u;
+    const int32_t qx = (int32_t)(q & 1u), qy = (int32_t)((q >> 1) & 1u), qz = (int32_t)(q >> 2);
+    for (uint32_t base = 0; base < ncell; base += 32u) {
+        // level 1: reference cell base + lane
+        const uint32_t cell = base + (uint32_t)lane;
+        float shx = 0.0f, shy = 0.0f, shz = 0.0f;
+        int32_t cx = 0, cy = 0, cz = 0;
+        bool live = false;
+        if (cell < ncell) {
+            const uint32_t cxy = cell % (nx * ny);
+            cz = wrap_cell(lo[2] + (int32_t)(cell / (nx * ny)), g.gs[2], g.scale[2], periodic, shz);
+            cy = wrap_cell(lo[1] + (int32_t)(cxy / nx), g.gs[1], g.scale[1], periodic, shy);
+            cx = wrap_cell(lo[0] + (int32_t)(cxy % nx), g.gs[0], g.scale[0], periodic, shx);
+            if (cz >= 0 && cz < g.gs[2] && cy >= 0 && cy < g.gs[1] && cx >= 0 && cx < g.gs[0]) {
+                const uint32_t rk =
+                    (uint32_t)cx + (uint32_t)g.gs[0] * ((uint32_t)cy + (uint32_t)g.gs[1] * (uint32_t)cz);
+                const float hr = __ldg(hmax_ref + rk);
+                if (hr > 0.0f && (periodic || (rk != ex0 && rk != ex1))) {
+                    const float reach = (Rfix > 0.0f ? Rfix : 2.0f * hr) * 1.00005f;
+                    const float dx = gap1(px, g.dmin[0] + (float)cx * g.cs[0] + shx, g.cs[0], m);
+                    const float dy = gap1(py, g.dmin[1] + (float)cy * g.cs[1] + shy, g.cs[1], m);
+                    const float dz = gap1(pz, g.dmin[2] + (float)cz * g.cs[2] + shz, g.cs[2], m);
+                    live = dx * dx + dy * dy + dz * dz <= reach * reach;
+                }
+            }
         }
-        const int32_t sx = 2 * cx + (int32_t)(q & 1u), sy = 2 * cy + (int32_t)((q >> 1) & 1u),
-                      sz = 2 * cz + (int32_t)(q >> 2);
+        // level 2: each group of 8 lanes opens its survivors (cells congruent to the group modulo 4) in order
+        uint32_t mine = __ballot_sync(0xffffffffu, live) & (0x11111111u << grp);
+        while (__any_sync(0xffffffffu, mine != 0u)) {
+            const bool has = mine != 0u;
+            const int src = has ? __ffs(mine) - 1 : lane;
+            mine &= mine - 1u;
+            const int32_t ox = __shfl_sync(0xffffffffu, cx, src), oy = __shfl_sync(0xffffffffu, cy, src),
+                          oz = __shfl_sync(0xffffffffu, cz, src);
+            const float sx_ = __shfl_sync(0xffffffffu, shx, src), sy_ = __shfl_sync(0xffffffffu, shy, src),
+                        sz_ = __shfl_sync(0xffffffffu, shz, src);
+            if (!has) continue;  // this group has no survivor left
+            const int32_t sx = 2 * ox + qx, sy = 2 * oy + qy, sz = 2 * oz + qz;
+            const uint32_t lin =
+                (uint32_t)sx + (uint32_t)g.sgs[0] * ((uint32_t)sy + (uint32_t)g.sgs[1] * (uint32_t)sz);
+            const uint32_t b = __ldg(start + lin);
+            if (b == kEmpty) continue;
+            const float hs = __ldg(hmax + lin);
+            const float reach = (Rfix > 0.0f ? Rfix : 2.0f * hs) * 1.00005f;
+            const float dx = gap1(px, g.dmin[0] + (float)sx * g.w[0] + sx_, g.w[0], m);
+            const float dy = gap1(py, g.dmin[1] + (float)sy * g.w[1] + sy_, g.w[1], m);
+            const float dz = gap1(pz, g.dmin[2] + (float)sz * g.w[2] + sz_, g.w[2], m);
+            if (dx * dx + dy * dy + dz * dz > reach * reach) continue;
+            body(b, __ldg(end + lin), sx_, sy_, sz_);
+        }
+    }
+}
+
+// Boundary cells of the query box [x-R, x+R] in the canonical order (reference cells z, y, x; their sub-cells z, y, x),
+// skipping excluded reference cells, reference cells without boundary particles and cells or sub-cells farther than
+// R from p (R is the support radius of the boundary sums, so a skipped sub-cell holds no member with r <= R).
+// body(begin, end, shx, shy, shz) gets each remaining sub-cell's member range.
+// kLanes == 1: one lane walks alone. kLanes == 32: the whole warp walks one query (the same on every lane) and
+// calls body warp-uniformly; 32 reference cells are tested at a time, one per lane.
+template <int kLanes, class Body>
+__device__ __forceinline__ void for_each_boundary_cell(const GridDev& g, const BoundaryDev& b, float px, float py,
+                                                       float pz, float R, int lane, Body&& body) {
+    if (b.n == 0) return;
+    int32_t lo[3], hi[3];
+    const float p[3] = {px, py, pz};
+    bool ok = true;
+#pragma unroll
+    for (int a = 0; a < 3; a++) ok &= box_axis(g, a, p[a], R, lo[a], hi[a]);
+    if (!ok) return;
+    const bool periodic = g.periodic;
+    const float m = g.cull_margin;
+    const float reach = R * 1.00005f;
+    const float reach2 = reach * reach;
+    // reference cell (rx, ry, rz) of the box: wrapped coordinates, image offsets, and whether it can contribute
+    auto ref_live = [&](int32_t rx, int32_t ry, int32_t rz, int32_t& cx, int32_t& cy, int32_t& cz, float& shx,
+                        float& shy, float& shz) -> bool {
+        cz = wrap_cell(rz, g.gs[2], g.scale[2], periodic, shz);
+        cy = wrap_cell(ry, g.gs[1], g.scale[1], periodic, shy);
+        cx = wrap_cell(rx, g.gs[0], g.scale[0], periodic, shx);
+        if (cz < 0 || cz >= g.gs[2] || cy < 0 || cy >= g.gs[1] || cx < 0 || cx >= g.gs[0]) return false;
+        const uint32_t rk = (uint32_t)cx + (uint32_t)g.gs[0] * ((uint32_t)cy + (uint32_t)g.gs[1] * (uint32_t)cz);
+        if (!periodic && (rk == b.ex0 || rk == b.ex1)) return false;
+        if (!__ldg(b.refflag + rk)) return false;
+        const float dx = gap1(px, g.dmin[0] + (float)cx * g.cs[0] + shx, g.cs[0], m);
+        const float dy = gap1(py, g.dmin[1] + (float)cy * g.cs[1] + shy, g.cs[1], m);
+        const float dz = gap1(pz, g.dmin[2] + (float)cz * g.cs[2] + shz, g.cs[2], m);
+        return dx * dx + dy * dy + dz * dz <= reach2;
+    };
+    // sub-cell (sx, sy, sz): its member range when it is non-empty and within reach
+    auto sub_live = [&](int32_t sx, int32_t sy, int32_t sz, float shx, float shy, float shz, uint32_t& kb,
+                        uint32_t& ke) -> bool {
         const uint32_t lin = (uint32_t)sx + (uint32_t)g.sgs[0] * ((uint32_t)sy + (uint32_t)g.sgs[1] * (uint32_t)sz);
-        const uint32_t b = __ldg(start + lin);
-        const float hs = __ldg(hmax + lin);
-        if (b == kEmpty) continue;
-        const float reach = (Rfix > 0.0f ? Rfix : 2.0f * hs) * 1.00005f;
+        kb = __ldg(b.start + lin);
+        if (kb == kEmpty) return false;
         const float dx = gap1(px, g.dmin[0] + (float)sx * g.w[0] + shx, g.w[0], m);
         const float dy = gap1(py, g.dmin[1] + (float)sy * g.w[1] + shy, g.w[1], m);
         const float dz = gap1(pz, g.dmin[2] + (float)sz * g.w[2] + shz, g.w[2], m);
-        if (dx * dx + dy * dy + dz * dz > reach * reach) continue;
-        body(b, __ldg(end + lin), shx, shy, shz);
+        if (dx * dx + dy * dy + dz * dz > reach2) return false;
+        ke = __ldg(b.end + lin);
+        return true;
+    };
+    if (kLanes == 1) {
+        for (int32_t rz = lo[2]; rz <= hi[2]; ++rz)
+            for (int32_t ry = lo[1]; ry <= hi[1]; ++ry)
+                for (int32_t rx = lo[0]; rx <= hi[0]; ++rx) {
+                    int32_t cx, cy, cz;
+                    float shx, shy, shz;
+                    if (!ref_live(rx, ry, rz, cx, cy, cz, shx, shy, shz)) continue;
+#pragma unroll 1
+                    for (int q = 0; q < 8; ++q) {
+                        uint32_t kb, ke;
+                        if (sub_live(2 * cx + (q & 1), 2 * cy + ((q >> 1) & 1), 2 * cz + (q >> 2), shx, shy, shz, kb,
+                                     ke))
+                            body(kb, ke, shx, shy, shz);
+                    }
+                }
+        return;
+    }
+    const uint32_t nx = (uint32_t)(hi[0] - lo[0] + 1), ny = (uint32_t)(hi[1] - lo[1] + 1);
+    const uint32_t ncell = nx * ny * (uint32_t)(hi[2] - lo[2] + 1);
+    for (uint32_t base = 0; base < ncell; base += 32u) {
+        const uint32_t cell = base + (uint32_t)lane;
+        int32_t cx = 0, cy = 0, cz = 0;
+        float shx = 0.0f, shy = 0.0f, shz = 0.0f;
+        bool live = false;
+        if (cell < ncell) {
+            const uint32_t cxy = cell % (nx * ny);
+            live = ref_live(lo[0] + (int32_t)(cxy % nx), lo[1] + (int32_t)(cxy / nx), lo[2] + (int32_t)(cell / (nx * ny)),
+                            cx, cy, cz, shx, shy, shz);
+        }
+        uint32_t cells = __ballot_sync(0xffffffffu, live);
+        while (cells != 0u) {
+            const int src = __ffs(cells) - 1;
+            cells &= cells - 1u;
+            const int32_t ox = __shfl_sync(0xffffffffu, cx, src), oy = __shfl_sync(0xffffffffu, cy, src),
+                          oz = __shfl_sync(0xffffffffu, cz, src);
+            const float sx_ = __shfl_sync(0xffffffffu, shx, src), sy_ = __shfl_sync(0xffffffffu, shy, src),
+                        sz_ = __shfl_sync(0xffffffffu, shz, src);
+            // lanes 0-7 look at the eight sub-cells, then the warp visits the live ones in order
+            uint32_t kb = 0, ke = 0;
+            const bool sl = lane < 8 && sub_live(2 * ox + (lane & 1), 2 * oy + ((lane >> 1) & 1), 2 * oz + (lane >> 2),
+                                                 sx_, sy_, sz_, kb, ke);
+            uint32_t subs = __ballot_sync(0xffffffffu, sl);
+            while (subs != 0u) {
+                const int q = __ffs(subs) - 1;
+                subs &= subs - 1u;
+                body(__shfl_sync(0xffffffffu, kb, q), __shfl_sync(0xffffffffu, ke, q), sx_, sy_, sz_);
+            }
+        }
     }
 }
 

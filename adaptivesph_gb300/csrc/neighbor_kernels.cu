@@ -69,30 +69,6 @@ __device__ __forceinline__ float warp_sum_butterfly(float v) {
     return v;
 }
 
-// True when any reference cell of the query box of p holds boundary particles.
-__device__ __forceinline__ bool boundary_near(const GridDev& g, const BoundaryDev& b, float px, float py, float pz,
-                                              float R) {
-    if (b.n == 0) return false;
-    int32_t lo[3], hi[3];
-    const float p[3] = {px, py, pz};
-    bool ok = true;
-#pragma unroll
-    for (int a = 0; a < 3; a++) ok &= box_axis(g, a, p[a], R, lo[a], hi[a]);
-    if (!ok) return false;
-    for (int32_t z = lo[2]; z <= hi[2]; z++)
-        for (int32_t y = lo[1]; y <= hi[1]; y++)
-            for (int32_t x = lo[0]; x <= hi[0]; x++) {
-                int32_t cx = x, cy = y, cz = z;
-                if (g.periodic) {
-                    cx = (cx % g.gs[0] + g.gs[0]) % g.gs[0];
-                    cy = (cy % g.gs[1] + g.gs[1]) % g.gs[1];
-                    cz = (cz % g.gs[2] + g.gs[2]) % g.gs[2];
-                }
-                if (__ldg(b.refflag + cx + g.gs[0] * (cy + g.gs[1] * cz))) return true;
-            }
-    return false;
-}
-
 // The support test r^2 <= (2 h_j)^2 of neighbour position pj (periodic image offset applied) for p.
 __device__ __forceinline__ bool supported(const GridDev& g, float4 p, float4 pj, float shx, float shy, float shz) {
     const bool periodic = g.periodic;
@@ -163,8 +139,8 @@ __device__ __forceinline__ float boundary_density(const StepArgs& a, const Bound
     const float cut = R * R;
     const bool periodic = a.grid.periodic;
     float rb = 0.0f;
-    for_each_cell<false>(
-        a.grid, b.start, b.end, nullptr, nullptr, b.ex0, b.ex1, pi.x, pi.y, pi.z, R, 0.0f,
+    for_each_boundary_cell<kLanes>(
+        a.grid, b, pi.x, pi.y, pi.z, R, lane,
         [&](uint32_t kb, uint32_t ke, float shx, float shy, float shz) {
             for (uint32_t k = kb + lane; k < ke; k += kLanes) {
                 const float4 pb = __ldg(b.pos + k);
@@ -397,8 +373,8 @@ __device__ __forceinline__ void boundary_forces(const StepArgs& a, const Boundar
     const float cut = R * R;
     const bool periodic = a.grid.periodic;
     const float c0 = a.phys.c0;
-    for_each_cell<false>(
-        a.grid, b.start, b.end, nullptr, nullptr, b.ex0, b.ex1, c.pi.x, c.pi.y, c.pi.z, R, 0.0f,
+    for_each_boundary_cell<kLanes>(
+        a.grid, b, c.pi.x, c.pi.y, c.pi.z, R, lane,
         [&](uint32_t kb, uint32_t ke, float shx, float shy, float shz) {
             for (uint32_t k = kb + lane; k < ke; k += kLanes) {
                 const float4 pb = __ldg(b.pos + k);
@@ -583,7 +559,7 @@ __global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, Boun
         }
     }
     float rb = 0.0f;
-    if (boundary_near(a.grid, b, pi.x, pi.y, pi.z, R)) rb = boundary_density<1>(a, b, i, pi, 0);
+    if (b.n != 0) rb = boundary_density<1>(a, b, i, pi, 0);
     const float rh = rho + rb;
     if (!isfinite(rh)) atomicOr(a.err, 0x2u);
     a.rp[i] = make_float2(rh, pressure_term(rh, a.phys.rho0, a.phys.B));
@@ -605,7 +581,7 @@ __global__ void __launch_bounds__(256, 1) k_density_heavy(StepArgs a, CellsDev c
         uint2* seg = keep ? nl.pool + ((size_t)w * 32 + lane) * kPoolLaneEntries : nullptr;
         uint32_t kept = 0;
         float rho = 0.0f;
-        for_each_subcell_lane(a.grid, c.start, c.end, c.hmax, c.ex[0], c.ex[1], pi.x, pi.y, pi.z, R, 0.0f, lane,
+        for_each_subcell_lane(a.grid, c.start, c.end, c.hmax, c.hmax_ref, c.ex[0], c.ex[1], pi.x, pi.y, pi.z, R, 0.0f, lane,
                               [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
                                   const uint32_t code = periodic ? (shift_code(shx, shy, shz) << kIdxBits) : 0u;
                                   for (uint32_t c0 = jb; c0 < je; c0 += 32) {
@@ -633,7 +609,7 @@ __global__ void __launch_bounds__(256, 1) k_density_heavy(StepArgs a, CellsDev c
         }
         rho = warp_sum_butterfly(rho);
         float rb = 0.0f;
-        if (boundary_near(a.grid, b, pi.x, pi.y, pi.z, R)) rb = warp_sum_butterfly(boundary_density<32>(a, b, i, pi, lane));
+        if (b.n != 0) rb = warp_sum_butterfly(boundary_density<32>(a, b, i, pi, lane));
         if (lane == 0) {
             const float rh = rho + rb;
             if (!isfinite(rh)) atomicOr(a.err, 0x2u);
@@ -691,7 +667,7 @@ __global__ void __launch_bounds__(256, 3) k_forces(StepArgs a, CellsDev c, Bound
         else
             force_pair<kMorris, false>(a, x, j1, s1x, s1y, s1z, j2, s2x, s2y, s2z, f);
     }
-    if (boundary_near(a.grid, b, x.pi.x, x.pi.y, x.pi.z, x.hi + x.hi)) boundary_forces<1>(a, b, i, x, f, 0);
+    if (b.n != 0) boundary_forces<1>(a, b, i, x, f, 0);
     finish_force(a, i, x, f);
 }
 
@@ -723,7 +699,7 @@ __global__ void __launch_bounds__(256, 1) k_forces_heavy(StepArgs a, CellsDev c,
                 }
             }
         } else {
-            for_each_subcell_lane(a.grid, c.start, c.end, c.hmax, c.ex[0], c.ex[1], x.pi.x, x.pi.y, x.pi.z,
+            for_each_subcell_lane(a.grid, c.start, c.end, c.hmax, c.hmax_ref, c.ex[0], c.ex[1], x.pi.x, x.pi.y, x.pi.z,
                                   x.hi + x.hi, 0.0f, lane,
                                   [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
                                       for (uint32_t j = jb; j < je; ++j) {
@@ -732,7 +708,7 @@ __global__ void __launch_bounds__(256, 1) k_forces_heavy(StepArgs a, CellsDev c,
                                       }
                                   });
         }
-        if (boundary_near(a.grid, b, x.pi.x, x.pi.y, x.pi.z, x.hi + x.hi)) boundary_forces<32>(a, b, i, x, f, lane);
+        if (b.n != 0) boundary_forces<32>(a, b, i, x, f, lane);
 #pragma unroll
         for (int q = 0; q < 3; q++) {
             f.ap[q] = warp_sum_butterfly(f.ap[q]);
@@ -772,7 +748,7 @@ __global__ void __launch_bounds__(256, 2) k_density_row(StepArgs a, BoundaryDev 
         rho = warp_sum_butterfly(rho);
         const float R = pi.w + pi.w;
         float rb = 0.0f;
-        if (boundary_near(a.grid, b, pi.x, pi.y, pi.z, R)) rb = warp_sum_butterfly(boundary_density<32>(a, b, i, pi, lane));
+        if (b.n != 0) rb = warp_sum_butterfly(boundary_density<32>(a, b, i, pi, lane));
         if (lane == 0) {
             const float rh = rho + rb;
             if (!isfinite(rh)) atomicOr(a.err, 0x2u);
@@ -804,7 +780,7 @@ __global__ void __launch_bounds__(256, 2) k_forces_row(StepArgs a, BoundaryDev b
                 if (j != i) force_term<kMorris>(a, x, j, shx, shy, shz, f);
             }
         }
-        if (boundary_near(a.grid, b, x.pi.x, x.pi.y, x.pi.z, x.hi + x.hi)) boundary_forces<32>(a, b, i, x, f, lane);
+        if (b.n != 0) boundary_forces<32>(a, b, i, x, f, lane);
 #pragma unroll
         for (int q = 0; q < 3; q++) {
             f.ap[q] = warp_sum_butterfly(f.ap[q]);

@@ -265,7 +265,7 @@ __global__ void __launch_bounds__(256, 4) k_merge_candidates_heavy(StepArgs a, C
         const float he = pe.w;
         float best = 3.402823466e38f;
         uint32_t bj = kNone, bid = 0xffffffffu;
-        for_each_subcell_lane(a.grid, c.start, c.end, c.hmax, c.ex[0], c.ex[1], pe.x, pe.y, pe.z, he, he, lane,
+        for_each_subcell_lane(a.grid, c.start, c.end, c.hmax, c.hmax_ref, c.ex[0], c.ex[1], pe.x, pe.y, pe.z, he, he, lane,
                               [&](uint32_t jb, uint32_t je, float, float, float) {
                                 for (uint32_t j = jb; j < je; ++j) {
                                     if (j == e) continue;
