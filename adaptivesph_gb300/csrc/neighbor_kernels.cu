@@ -441,7 +441,7 @@ __device__ __forceinline__ void fluid_candidates(const StepArgs& a, const CellsD
 
 // Density pass, ordinary particles; heavy particles are queued for k_density_heavy.
 template <bool kPeriodic>
-__global__ void __launch_bounds__(256, 3) k_density(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
+__global__ void __launch_bounds__(256, 4) k_density(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
     __shared__ uint2 stage[256 * kStageStride];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool in = i < count_of(a);
