@@ -17,6 +17,7 @@ namespace asph {
 
 constexpr uint32_t kEmpty = 0xffffffffu;
 constexpr uint32_t kNone = 0xffffffffu;
+constexpr uint32_t kEligible = 0xfffffffeu;  // cand[] mark of a selected merge candidate before its search
 constexpr float kPi = 3.141592653589793f;
 
 // Grid geometry: the reference grid (cell 4 h0, NeighborGrid.cu:108-121) and its 2x2x2 sub-cells.

@@ -52,7 +52,8 @@ __global__ void k_select_scores(const float* score, const uint32_t* n_ptr, int d
 __global__ void k_merge_limits(RefineArgs r, uint32_t n);
 __global__ void k_cand_init(RefineArgs r, uint32_t n);
 __global__ void k_merge_candidates_heavy(StepArgs a, CellsDev c, RefineArgs r);
-__global__ void k_merge_candidates(StepArgs a, CellsDev c, RefineArgs r, const uint32_t* sel);
+__global__ void k_mark_eligible(RefineArgs r, const uint32_t* sel);
+__global__ void k_merge_candidates(StepArgs a, CellsDev c, RefineArgs r);
 __global__ void k_merge_pairs(StepArgs a, RefineArgs r);
 __global__ void k_compact_count(const uint32_t* flag, uint32_t n, uint32_t* block_counts);
 __global__ void k_compact_scan(uint32_t* block_counts, uint32_t nblocks, uint32_t n, RefineArgs r);

@@ -216,12 +216,18 @@ __global__ void __launch_bounds__(256) k_cand_init(RefineArgs r, uint32_t n) {
     }
 }
 
-// identifyMergeCandidates (AdaptiveAlgorithm.cu:159-206)
-__global__ void __launch_bounds__(256, 4) k_merge_candidates(StepArgs a, CellsDev c, RefineArgs r,
-                                                          const uint32_t* sel) {
+// Marks the selected merge candidates (the first `eligible` slots of the score-sorted ids) in cand[].
+__global__ void __launch_bounds__(256) k_mark_eligible(RefineArgs r, const uint32_t* sel) {
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= r.ctr[kCtrEligible]) return;
-    const uint32_t e = sel[q];
+    if (q < r.ctr[kCtrEligible]) r.cand[sel[q]] = kEligible;
+}
+
+// identifyMergeCandidates (AdaptiveAlgorithm.cu:159-206) for the marked particles, taken in the cell order of the
+// particle array rather than in score order, so that a warp's searches are neighbours and share their loads. Each
+// particle's result depends on that particle alone.
+__global__ void __launch_bounds__(256, 4) k_merge_candidates(StepArgs a, CellsDev c, RefineArgs r) {
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= a.n || r.cand[e] != kEligible) return;
     const float4 pe = a.ph[e];
     const float he = pe.w;
     if (box_cells(a.grid, pe, he) > kHeavyCells) {  // large box: one warp (k_merge_candidates_heavy)

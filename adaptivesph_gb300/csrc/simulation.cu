@@ -677,7 +677,8 @@ asph_status refine_enqueue(asph_simulation* s) {
     s->launches += 1 + radix_sort_pairs(s->keys, s->vals, s->ctr + kCtrSortN, n, 32, s->ss, s->err, s->stream);
     // candidates, pairs + merges
     k_cand_init<<<nbk, 256, 0, s->stream>>>(r, n);
-    k_merge_candidates<<<nbk, 256, 0, s->stream>>>(a, s->cells(), r, s->vals);
+    k_mark_eligible<<<nbk, 256, 0, s->stream>>>(r, s->vals);
+    k_merge_candidates<<<nbk, 256, 0, s->stream>>>(a, s->cells(), r);
     k_merge_candidates_heavy<<<kHeavyBlocks, 256, 0, s->stream>>>(a, s->cells(), r);
     k_merge_pairs<<<nbk, 256, 0, s->stream>>>(a, r);
     CK_LAUNCH("merge");
@@ -691,7 +692,7 @@ asph_status refine_enqueue(asph_simulation* s) {
     k_compact_scatter<<<nbk, 256, 0, s->stream>>>(a, b, s->flag, s->block_counts, vort ? s->rkeys : nullptr,
                                                    keys_c);
     CK_LAUNCH("compaction");
-    s->launches += 7;
+    s->launches += 8;
     s->cur = nxt;
     StepArgs c = s->args(s->cur);
     if (vort) {
