@@ -1,0 +1,93 @@
+"""Parity at the benchmark sizes, through the C ABI, bit for bit against the oracle.
+
+* The plain 3D dam break (40x80x40 = 128,000 particles at dx = 0.01 m, walls from StaticBoundaryDomain::generate):
+  the whole trajectory of 20 frames from the initial lattice.
+* The adaptive dam break of the headline measurement (100x200x50 = 1,000,000 particles at dx = 0.004 m, 503,100
+  wall particles, velocity criterion, capacity 4M): the GPU runs it alone to frame 155, where merged particles have
+  grown to several h0 and every summation kind occurs (heavy boxes, long rows, ordinary rows); its state then goes
+  to the oracle, and both take 6 more frames, one of them a refinement frame. A second simulation built from the
+  same input reaches frame 155 with the same state bit for bit (run-to-run determinism at full size).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from adaptivesph_gb300 import StaticBoundaryDomain, create_simulation, scenes
+from helpers import assert_state_bitexact
+
+pytestmark = pytest.mark.gpu
+
+
+def _scene_pair(sc, capacity):
+    bd = StaticBoundaryDomain.generate(sc.parameters.domain, sc.boundary_spacing, sc.parameters.rest_density,
+                                       sc.parameters.base_smoothing_radius)
+    sim = create_simulation(sc.parameters, sc.positions, None, None, bd, sc.refinement, capacity,
+                            bd.get_particle_count())
+    orc = oracle.OracleSim(sc.parameters, sc.positions, bd.positions, bd.psi, sc.refinement, capacity=capacity)
+    return sim, orc, bd
+
+
+def test_plain_dam_break_128k_trajectory_bitexact():
+    sc = scenes.c1_plain()
+    sim, orc, _ = _scene_pair(sc, sc.positions.shape[0])
+    for k in range(20):
+        sim.step_async(sc.dt)
+        orc.step(sc.dt)
+        if k % 5 == 4:
+            sim.synchronize()
+            assert_state_bitexact(sim.read_state(), orc.arrays())
+    assert sim.device_errors() == 0
+
+
+def _transfer(sim, orc):
+    st = sim.read_state()
+    info = sim.state_info()
+    orc.load(st, frame=int(info["frame"]), next_id=int(info["next_id"]),
+             pending_half=info["pending_half_dt"] if info["has_pending"] else None)
+    return st, info
+
+
+def test_adaptive_dam_break_1m_late_frames_bitexact():
+    sc = scenes.c2_adaptive()
+    cap = sc.refinement.max_particle_count
+    sim, orc, bd = _scene_pair(sc, cap)
+    for _ in range(155):
+        sim.step_async(sc.dt)
+    sim.synchronize()
+    st, info = _transfer(sim, orc)
+    h0 = np.float32(sc.parameters.base_smoothing_radius)
+    assert st["h"].max() > 3 * h0, "merged particles must have grown"
+
+    # every summation kind occurs in the next step (a separate oracle instance: its grid build reorders)
+    probe = oracle.OracleSim(sc.parameters, sc.positions, bd.positions, bd.psi, sc.refinement, capacity=cap)
+    probe.load(st, frame=int(info["frame"]), next_id=int(info["next_id"]),
+               pending_half=info["pending_half_dt"] if info["has_pending"] else None)
+    probe.integrate(sc.dt)
+    probe.grid_build()
+    kinds = np.bincount(probe.sum_kinds(), minlength=3)
+    assert kinds.min() > 0, kinds
+    del probe
+
+    # run-to-run determinism at full size
+    bd2 = StaticBoundaryDomain.generate(sc.parameters.domain, sc.boundary_spacing, sc.parameters.rest_density,
+                                        sc.parameters.base_smoothing_radius)
+    sim2 = create_simulation(sc.parameters, sc.positions, None, None, bd2, sc.refinement, cap,
+                             bd2.get_particle_count())
+    for _ in range(155):
+        sim2.step_async(sc.dt)
+    sim2.synchronize()
+    assert_state_bitexact(sim2.read_state(), st)
+    sim2.close()
+
+    refined = False
+    for _ in range(6):
+        sim.step_async(sc.dt)
+        sim.synchronize()
+        if orc.step(sc.dt):
+            refined = True
+            rep, o = sim.last_refinement(), orc.last_report()
+            for key in ("merge_eligible", "merge_pairs", "split_candidates", "splits", "count_after"):
+                assert rep[key] == o[key], (key, rep[key], o[key])
+        assert_state_bitexact(sim.read_state(), orc.arrays())
+    assert refined, "the frames must include a refinement pass"
+    assert sim.device_errors() == 0
