@@ -494,6 +494,7 @@ __device__ __forceinline__ bool for_each_cell_warp(const GridDev& g, const uint3
     if (span > max_union) return false;
     const bool periodic = g.periodic;
     const float m = g.cull_margin;
+    const int lane = (int)(threadIdx.x & 31u);
     for (int32_t rz = ulo[2]; rz <= uhi[2]; ++rz) {
         for (int32_t ry = ulo[1]; ry <= uhi[1]; ++ry) {
             for (int32_t rx = ulo[0]; rx <= uhi[0]; ++rx) {
@@ -511,37 +512,47 @@ __device__ __forceinline__ bool for_each_cell_warp(const GridDev& g, const uint3
                 const float reach = 2.0f * hr * 1.00005f;
                 const float sh[3] = {shx, shy, shz};
                 const int32_t c3[3] = {cx, cy, cz};
-                bool k0[3], k1[3];
+                // squared distances to the lower and upper sub-cell slab on each axis
+                float q0[3], q1[3];
                 float d2 = 0.0f;
 #pragma unroll
                 for (int a = 0; a < 3; a++) {
                     const float base = g.dmin[a] + (float)c3[a] * g.cs[a] + sh[a];
                     const float d = gap1(p[a], base, g.cs[a], m);
                     d2 += d * d;
-                    k0[a] = gap1(p[a], base, g.w[a], m) <= reach;
-                    k1[a] = gap1(p[a], base + g.w[a], g.w[a], m) <= reach;
-                    need &= (k0[a] || k1[a]);
+                    const float e0 = gap1(p[a], base, g.w[a], m), e1 = gap1(p[a], base + g.w[a], g.w[a], m);
+                    q0[a] = e0 * e0;
+                    q1[a] = e1 * e1;
                 }
                 need &= d2 <= reach * reach;
                 if (!__any_sync(0xffffffffu, need)) continue;
-#pragma unroll 1
-                for (int q = 0; q < 8; ++q) {
-                    const int dx = q & 1, dy = (q >> 1) & 1, dz = q >> 2;
-                    const int32_t sx = 2 * cx + dx, sy = 2 * cy + dy, sz = 2 * cz + dz;
+                // the eight sub-cells' member ranges and max h, fetched by lanes 0-7 at once
+                uint32_t sb = kEmpty, se = 0u;
+                float shm = 0.0f;
+                if (lane < 8) {
+                    const int32_t sx = 2 * cx + (lane & 1), sy = 2 * cy + ((lane >> 1) & 1), sz = 2 * cz + (lane >> 2);
                     const uint32_t lin =
                         (uint32_t)sx + (uint32_t)g.sgs[0] * ((uint32_t)sy + (uint32_t)g.sgs[1] * (uint32_t)sz);
-                    const uint32_t b = __ldg(start + lin);
-                    if (b == kEmpty) continue;
-                    bool ns = need && (dx ? k1[0] : k0[0]) && (dy ? k1[1] : k0[1]) && (dz ? k1[2] : k0[2]);
+                    sb = __ldg(start + lin);
+                    if (sb != kEmpty) {
+                        se = __ldg(end + lin);
+                        shm = __ldg(hmax + lin);
+                    }
+                }
+                uint32_t live = __ballot_sync(0xffffffffu, sb != kEmpty) & 0xffu;
+                while (live != 0u) {
+                    const int q = __ffs(live) - 1;
+                    live &= live - 1u;
+                    const uint32_t b = __shfl_sync(0xffffffffu, sb, q), e = __shfl_sync(0xffffffffu, se, q);
+                    const float hs = __shfl_sync(0xffffffffu, shm, q);
+                    bool ns = need;
                     if (ns) {
-                        const float rs = 2.0f * __ldg(hmax + lin) * 1.00005f;
-                        const float ex = gap1(px, g.dmin[0] + (float)sx * g.w[0] + shx, g.w[0], m);
-                        const float ey = gap1(py, g.dmin[1] + (float)sy * g.w[1] + shy, g.w[1], m);
-                        const float ez = gap1(pz, g.dmin[2] + (float)sz * g.w[2] + shz, g.w[2], m);
-                        ns = ex * ex + ey * ey + ez * ez <= rs * rs;
+                        const float rs = 2.0f * hs * 1.00005f;
+                        const float e2 = ((q & 1) ? q1[0] : q0[0]) + ((q & 2) ? q1[1] : q0[1]) + ((q & 4) ? q1[2] : q0[2]);
+                        ns = e2 <= rs * rs;
                     }
                     if (!__any_sync(0xffffffffu, ns)) continue;
-                    body(b, __ldg(end + lin), shx, shy, shz, ns);
+                    body(b, e, shx, shy, shz, ns);
                 }
             }
         }

@@ -28,8 +28,6 @@ namespace {
 
 constexpr uint32_t kIdxBits = 27;
 constexpr uint32_t kIdxMask = (1u << kIdxBits) - 1u;
-constexpr int kStage = 8;          // list entries (8 bytes each) staged per thread before a 64-byte flush
-constexpr int kStageStride = 9;    // padded staging row
 constexpr int32_t kMaxUnion = 64;  // a warp walks its lanes' boxes together when their union is at most this big
 
 // Periodic image of a listed neighbour: the index keeps 27 bits, the cell's image offset (-1, 0, +1 per axis)
@@ -442,7 +440,6 @@ __device__ __forceinline__ void fluid_candidates(const StepArgs& a, const CellsD
 // Density pass, ordinary particles; heavy particles are queued for k_density_heavy.
 template <bool kPeriodic>
 __global__ void __launch_bounds__(256, 4) k_density(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
-    __shared__ uint2 stage[256 * kStageStride];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool in = i < count_of(a);
     const float4 pi = in ? a.ph[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -451,20 +448,17 @@ __global__ void __launch_bounds__(256, 4) k_density(StepArgs a, CellsDev c, Boun
     if (in && box_cells(a.grid, pi, R) > kHeavyCells) active = false;  // k_density_heavy (sets cnt[i])
     constexpr bool periodic = kPeriodic;
     uint2* row = nl.ent + (size_t)(in ? i : 0) * nl.maxe;
-    uint2* st = stage + threadIdx.x * kStageStride;
     const uint32_t maxe = nl.maxe;
-    uint32_t cnt = 0, staged = 0;
+    uint32_t cnt = 0;
+    // entries are written in 16-byte pairs: an even entry waits in registers for its odd partner
+    uint2 held = make_uint2(0u, 0u);
     float rho = 0.0f;
     auto append = [&](uint32_t first, uint32_t mask) {
         if (cnt < maxe) {
-            st[staged++] = make_uint2(first, mask);
-            if (staged == kStage) {
-                uint4* dst = reinterpret_cast<uint4*>(row + (cnt + 1 - kStage));
-#pragma unroll
-                for (int q = 0; q < kStage / 2; q++)
-                    dst[q] = make_uint4(st[2 * q].x, st[2 * q].y, st[2 * q + 1].x, st[2 * q + 1].y);
-                staged = 0;
-            }
+            if (cnt & 1u)
+                *reinterpret_cast<uint4*>(row + (cnt - 1u)) = make_uint4(held.x, held.y, first, mask);
+            else
+                held = make_uint2(first, mask);
         }
         cnt++;
     };
@@ -520,8 +514,7 @@ __global__ void __launch_bounds__(256, 4) k_density(StepArgs a, CellsDev c, Boun
         nl.dover[atomicAdd(nl.dover_n, 1u)] = i;
         return;
     }
-    // remaining staged entries (fewer than a full segment)
-    for (uint32_t q = 0; q < staged; ++q) row[cnt - staged + q] = st[q];
+    if (cnt & 1u) row[cnt - 1u] = held;  // the unpaired last entry
     if (cnt > kRowHeavy) {  // many neighbours: summed over the row by a warp (k_density_row)
         nl.drow[atomicAdd(nl.drow_n, 1u)] = i;
         return;
