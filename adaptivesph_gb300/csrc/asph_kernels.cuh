@@ -42,6 +42,7 @@ __device__ __forceinline__ uint32_t count_of(const StepArgs& a) { return a.np ? 
 // If a lane has more than kPoolLaneEntries such blocks, cnt[i] = kHeavyMark and the force pass walks the cells.
 constexpr uint32_t kHeavyMark = 0xffffffffu;
 constexpr uint32_t kPooled = 0x80000000u;
+constexpr uint32_t kBoundaryWalk = 0xffffffffu;
 constexpr uint32_t kPoolLaneEntries = 32;
 constexpr uint32_t kPoolSlots = 8192;
 constexpr uint32_t kListEntries = 256;  // entries per row
@@ -59,6 +60,7 @@ struct NbrDev {
     uint32_t* drow_n;
     uint32_t* frow;
     uint32_t* frow_n;
+    uint32_t* bcnt;  // wall entries recorded after the fluid entries of an ordinary row (kBoundaryWalk: none fit)
     uint2* pool;
     uint32_t* pool_cnt;
     uint32_t pool_slots;

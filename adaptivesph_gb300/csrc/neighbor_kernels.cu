@@ -160,6 +160,45 @@ struct ForceAcc {
     float ap[3], av[3], as[3], bp[3], bf[3];
 };
 
+// boundary_density<1> that also records, after the fluid entries of the particle's row, one entry per block of up
+// to 32 wall members with an accepted member: (first member | image code << 27, acceptance mask). `space` entries
+// fit; *entries is their number, or kBoundaryWalk when they did not fit (the force pass then walks the cells).
+__device__ __forceinline__ float boundary_density_rows(const StepArgs& a, const BoundaryDev& b, uint32_t i, float4 pi,
+                                                       uint2* out, uint32_t space, uint32_t* entries) {
+    const float R = pi.w + pi.w;
+    const float4 ki = a.kc[i];
+    const float cut = R * R;
+    const bool periodic = a.grid.periodic;
+    float rb = 0.0f;
+    uint32_t n = 0;
+    for_each_boundary_cell<1>(
+        a.grid, b, pi.x, pi.y, pi.z, R, 0, [&](uint32_t kb, uint32_t ke, float shx, float shy, float shz) {
+            const uint32_t code = periodic ? (shift_code(shx, shy, shz) << kIdxBits) : 0u;
+            for (uint32_t c0 = kb; c0 < ke; c0 += 32u) {
+                const uint32_t cn = ke - c0 < 32u ? ke - c0 : 32u;
+                uint32_t mask = 0;
+                for (uint32_t k = 0; k < cn; ++k) {
+                    const float4 pb = __ldg(b.pos + c0 + k);
+                    const float xb = periodic ? pb.x + shx : pb.x;
+                    const float yb = periodic ? pb.y + shy : pb.y;
+                    const float zb = periodic ? pb.z + shz : pb.z;
+                    const float dx = xb - pi.x, dy = yb - pi.y, dz = zb - pi.z;
+                    const float r2 = dist2(dx, dy, dz);
+                    if (r2 > cut) continue;
+                    const float w = kernel_w(sqrtf(r2), ki.x, ki.y);
+                    rb = fmaf(pb.w, w, rb);
+                    mask |= 1u << k;
+                }
+                if (mask != 0u) {
+                    if (n < space) out[n] = make_uint2(c0 | code, mask);
+                    n++;
+                }
+            }
+        });
+    *entries = n <= space ? n : kBoundaryWalk;
+    return rb;
+}
+
 struct ForceCtx {
     float4 pi, vi;
     float rhoi, pti, Ki, ei, hi;
@@ -437,6 +476,139 @@ __device__ __forceinline__ void fluid_candidates(const StepArgs& a, const CellsD
 
 }  // namespace
 
+// Boundary pressure and friction term of wall member k (Algorithm.cu:118-221), the member known to be within the
+// support: the arithmetic of boundary_forces.
+__device__ __forceinline__ void boundary_term(const StepArgs& a, const BoundaryDev& b, const ForceCtx& c, float4 ki,
+                                              uint32_t k, float shx, float shy, float shz, ForceAcc& f) {
+    const bool periodic = a.grid.periodic;
+    const float4 pb = __ldg(b.pos + k);
+    const float xb = periodic ? pb.x + shx : pb.x;
+    const float yb = periodic ? pb.y + shy : pb.y;
+    const float zb = periodic ? pb.z + shz : pb.z;
+    const float dx = c.pi.x - xb, dy = c.pi.y - yb, dz = c.pi.z - zb;
+    const float r2 = dist2(dx, dy, dz);
+    const float r = sqrtf(r2);
+    float u[3];
+    if (r > 0.0f) {
+        const float ir = 1.0f / r;
+        u[0] = dx * ir;
+        u[1] = dy * ir;
+        u[2] = dz * ir;
+    } else {
+        u[0] = 0.0f;
+        u[1] = 1.0f;
+        u[2] = 0.0f;
+    }
+    const float dw = kernel_dw(r, ki.x, ki.z);
+    const float psi = pb.w;
+    const float sp = (psi * c.pti) * dw;
+#pragma unroll
+    for (int q = 0; q < 3; q++) f.bp[q] = fmaf(-sp, u[q], f.bp[q]);
+    const float comp = fmaf(c.vi.z, dz, fmaf(c.vi.y, dy, c.vi.x * dx));
+    if (comp < 0.0f) {
+        const float nub = ((__ldg(b.fric + k) * c.hi) * a.phys.c0) / (2.0f * c.rhoi);
+        const float pib = (-nub * comp) / (r2 + c.ei);
+        const float sf = (psi * pib) * dw;
+#pragma unroll
+        for (int q = 0; q < 3; q++) f.bf[q] = fmaf(-sf, u[q], f.bf[q]);
+    }
+}
+
+// boundary_term for two wall members in packed FP32x2 arithmetic (each half rounds as the scalar operation; divisions
+// and square roots stay scalar); each accumulator is updated for k1, then k2.
+__device__ __forceinline__ void boundary_pair(const StepArgs& a, const BoundaryDev& b, const ForceCtx& c, float4 ki,
+                                              uint32_t k1, float s1x, float s1y, float s1z, uint32_t k2, float s2x,
+                                              float s2y, float s2z, ForceAcc& f) {
+    const float4 p1 = __ldg(b.pos + k1), p2 = __ldg(b.pos + k2);
+    float2 x = make_float2(p1.x, p2.x), y = make_float2(p1.y, p2.y), z = make_float2(p1.z, p2.z);
+    if (a.grid.periodic) {
+        x = __fadd2_rn(x, make_float2(s1x, s2x));
+        y = __fadd2_rn(y, make_float2(s1y, s2y));
+        z = __fadd2_rn(z, make_float2(s1z, s2z));
+    }
+    const float2 dx = __fadd2_rn(make_float2(c.pi.x, c.pi.x), make_float2(-x.x, -x.y));
+    const float2 dy = __fadd2_rn(make_float2(c.pi.y, c.pi.y), make_float2(-y.x, -y.y));
+    const float2 dz = __fadd2_rn(make_float2(c.pi.z, c.pi.z), make_float2(-z.x, -z.y));
+    const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+    const float2 r = make_float2(sqrtf(r2.x), sqrtf(r2.y));
+    const float2 ir = make_float2(r.x > 0.0f ? 1.0f / r.x : 0.0f, r.y > 0.0f ? 1.0f / r.y : 0.0f);
+    float2 ux = __fmul2_rn(dx, ir), uy = __fmul2_rn(dy, ir), uz = __fmul2_rn(dz, ir);
+    if (!(r.x > 0.0f)) {
+        ux.x = 0.0f;
+        uy.x = 1.0f;
+        uz.x = 0.0f;
+    }
+    if (!(r.y > 0.0f)) {
+        ux.y = 0.0f;
+        uy.y = 1.0f;
+        uz.y = 0.0f;
+    }
+    // kernel_dw(r, 1/h_i, dcoef/h_i^4)
+    const float2 q = __fmul2_rn(r, make_float2(ki.x, ki.x));
+    const float2 t = __ffma2_rn(make_float2(-0.5f, -0.5f), q, make_float2(1.0f, 1.0f));
+    const float2 t3 = __fmul2_rn(__fmul2_rn(t, t), t);
+    float2 dw = __fmul2_rn(__fmul2_rn(make_float2(ki.z, ki.z), q), t3);
+    if (q.x > 2.0f) dw.x = 0.0f;
+    if (q.y > 2.0f) dw.y = 0.0f;
+    const float2 psi = make_float2(p1.w, p2.w);
+    const float2 sp = __fmul2_rn(__fmul2_rn(psi, make_float2(c.pti, c.pti)), dw);
+    f.bp[0] = fmaf(-sp.x, ux.x, f.bp[0]);
+    f.bp[1] = fmaf(-sp.x, uy.x, f.bp[1]);
+    f.bp[2] = fmaf(-sp.x, uz.x, f.bp[2]);
+    f.bp[0] = fmaf(-sp.y, ux.y, f.bp[0]);
+    f.bp[1] = fmaf(-sp.y, uy.y, f.bp[1]);
+    f.bp[2] = fmaf(-sp.y, uz.y, f.bp[2]);
+    const float2 comp = __ffma2_rn(make_float2(c.vi.z, c.vi.z), dz,
+                                   __ffma2_rn(make_float2(c.vi.y, c.vi.y), dy, __fmul2_rn(make_float2(c.vi.x, c.vi.x), dx)));
+    if (comp.x < 0.0f) {
+        const float nub = ((__ldg(b.fric + k1) * c.hi) * a.phys.c0) / (2.0f * c.rhoi);
+        const float pib = (-nub * comp.x) / (r2.x + c.ei);
+        const float sf = (psi.x * pib) * dw.x;
+        f.bf[0] = fmaf(-sf, ux.x, f.bf[0]);
+        f.bf[1] = fmaf(-sf, uy.x, f.bf[1]);
+        f.bf[2] = fmaf(-sf, uz.x, f.bf[2]);
+    }
+    if (comp.y < 0.0f) {
+        const float nub = ((__ldg(b.fric + k2) * c.hi) * a.phys.c0) / (2.0f * c.rhoi);
+        const float pib = (-nub * comp.y) / (r2.y + c.ei);
+        const float sf = (psi.y * pib) * dw.y;
+        f.bf[0] = fmaf(-sf, ux.y, f.bf[0]);
+        f.bf[1] = fmaf(-sf, uy.y, f.bf[1]);
+        f.bf[2] = fmaf(-sf, uz.y, f.bf[2]);
+    }
+}
+
+// Boundary forces of particle i from its recorded wall entries, in the recorded (canonical) order.
+__device__ __forceinline__ void boundary_forces_rows(const StepArgs& a, const BoundaryDev& b, uint32_t i,
+                                                     const ForceCtx& c, ForceAcc& f, const uint2* ent, uint32_t n) {
+    const float4 ki = a.kc[i];
+    uint32_t e = 0, first = 0, mask = 0;
+    float shx = 0.0f, shy = 0.0f, shz = 0.0f;
+    auto pull = [&](uint32_t& k, float& sx, float& sy, float& sz) -> bool {
+        if (mask == 0u) {
+            if (e >= n) return false;
+            row_entry(a.grid, __ldg(ent + e), first, mask, shx, shy, shz);
+            e++;
+        }
+        k = first + (uint32_t)(__ffs(mask) - 1);
+        mask &= mask - 1u;
+        sx = shx;
+        sy = shy;
+        sz = shz;
+        return true;
+    };
+    for (;;) {
+        uint32_t k1, k2;
+        float s1x, s1y, s1z, s2x, s2y, s2z;
+        if (!pull(k1, s1x, s1y, s1z)) break;
+        if (!pull(k2, s2x, s2y, s2z)) {
+            boundary_term(a, b, c, ki, k1, s1x, s1y, s1z, f);
+            break;
+        }
+        boundary_pair(a, b, c, ki, k1, s1x, s1y, s1z, k2, s2x, s2y, s2z, f);
+    }
+}
+
 // Density pass, ordinary particles; heavy particles are queued for k_density_heavy.
 template <bool kPeriodic>
 __global__ void __launch_bounds__(256, 4) k_density(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
@@ -552,7 +724,9 @@ __global__ void __launch_bounds__(256, 4) k_density(StepArgs a, CellsDev c, Boun
         }
     }
     float rb = 0.0f;
-    if (b.n != 0) rb = boundary_density<1>(a, b, i, pi, 0);
+    uint32_t bn = 0;
+    if (b.n != 0) rb = boundary_density_rows(a, b, i, pi, row + cnt, maxe - cnt, &bn);
+    nl.bcnt[i] = bn;
     const float rh = rho + rb;
     if (!isfinite(rh)) atomicOr(a.err, 0x2u);
     a.rp[i] = make_float2(rh, pressure_term(rh, a.phys.rho0, a.phys.B));
@@ -660,7 +834,11 @@ __global__ void __launch_bounds__(256, 3) k_forces(StepArgs a, CellsDev c, Bound
         else
             force_pair<kMorris, false>(a, x, j1, s1x, s1y, s1z, j2, s2x, s2y, s2z, f);
     }
-    if (b.n != 0) boundary_forces<1>(a, b, i, x, f, 0);
+    const uint32_t bn = nl.bcnt[i];
+    if (bn == kBoundaryWalk)
+        boundary_forces<1>(a, b, i, x, f, 0);
+    else if (bn != 0u)
+        boundary_forces_rows(a, b, i, x, f, row + cnt, bn);
     finish_force(a, i, x, f);
 }
 

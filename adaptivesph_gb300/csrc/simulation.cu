@@ -146,6 +146,7 @@ struct asph_simulation {
     float4* pq = nullptr;  // [cap] x, y, z, (2h)^2 of the current step (StepArgs::pq)
     uint2* nbr_ent = nullptr;     // [kListEntries * cap] neighbour lists, one row per particle
     uint32_t* nbr_cnt = nullptr;  // [cap]
+    uint32_t* nbr_bcnt = nullptr;  // [cap] wall entries of ordinary rows
     uint32_t* heavy_idx = nullptr;  // [cap] queue of heavy particles of the current step
     uint32_t* heavy_n = nullptr;
     uint32_t* fheavy_idx = nullptr;  // [cap] queue of the force pass's warp kernel
@@ -264,7 +265,7 @@ struct asph_simulation {
     NbrDev nbrs() const {
         return NbrDev{nbr_ent,      nbr_cnt,  heavy_idx,    heavy_n,  fheavy_idx,   fheavy_n,
                       dover_idx,    fheavy_n + 1, drow_idx, fheavy_n + 2, frow_idx, fheavy_n + 3,
-                      pool,         pool_cnt, pool_slots,   kListEntries};
+                      nbr_bcnt,     pool,     pool_cnt,     pool_slots,   kListEntries};
     }
 
     BoundaryDev boundary() const {
@@ -335,7 +336,7 @@ uint64_t device_bytes_for(uint32_t C, uint32_t sort_items, uint32_t ncells, uint
     uint64_t b = 0;
     b += 2 * c * (sizeof(float4) * 3 + sizeof(float2) + sizeof(float) + sizeof(uint32_t));  // two buffer sets
     b += c * sizeof(float4) * 2;                                           // kernel constants, support operands
-    b += c * kListEntries * sizeof(uint2) + c * sizeof(uint32_t);                          // rows and counts
+    b += c * kListEntries * sizeof(uint2) + c * sizeof(uint32_t) * 2;                      // rows and counts
     b += c * sizeof(uint32_t) * 5 + sizeof(uint32_t) * 5;                                   // queues
     const uint64_t slots = std::min<uint32_t>(kPoolSlots, std::max<uint32_t>(64u, C / 128u));
     b += slots * 32 * (kPoolLaneEntries * sizeof(uint2) + sizeof(uint32_t));                // heavy pool
@@ -837,6 +838,7 @@ void destroy(asph_simulation* s) {
     dfree(s->pq);
     dfree(s->nbr_ent);
     dfree(s->nbr_cnt);
+    dfree(s->nbr_bcnt);
     dfree(s->heavy_idx);
     dfree(s->heavy_n);
     dfree(s->fheavy_idx);
@@ -1104,6 +1106,7 @@ asph_status asph_simulation_create(const asph_parameters* parameters, const floa
     TRY(dalloc(s->pq, C));
     TRY(dalloc(s->nbr_ent, (size_t)kListEntries * C));
     TRY(dalloc(s->nbr_cnt, C));
+    TRY(dalloc(s->nbr_bcnt, C));
     TRY(dalloc(s->heavy_idx, C));
     TRY(dalloc(s->heavy_n, 1));
     TRY(dalloc(s->fheavy_idx, C));
