@@ -28,7 +28,7 @@ namespace {
 
 constexpr uint32_t kIdxBits = 27;
 constexpr uint32_t kIdxMask = (1u << kIdxBits) - 1u;
-constexpr int32_t kMaxUnion = 64;  // a warp walks its lanes' boxes together when their union is at most this big
+constexpr int32_t kMaxUnion = 40;  // a warp walks its lanes' boxes together when their union is at most this big
 
 // Periodic image of a listed neighbour: the index keeps 27 bits, the cell's image offset (-1, 0, +1 per axis)
 // is packed into the top 5 bits.
