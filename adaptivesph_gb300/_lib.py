@@ -71,6 +71,8 @@ SIGNATURES = {
     "asph_simulation_enable_adaptive_refinement": (ctypes.c_int, [_vp]),
     "asph_simulation_export": (ctypes.c_int, [_vp]),
     "asph_simulation_export_host": (ctypes.c_int, [_vp, _fp, _fp, _fp, _fp, _up, _u32]),
+    "asph_simulation_export_host_async": (ctypes.c_int, [_vp, _fp, _fp, _fp, _fp, _up, _u32]),
+    "asph_simulation_export_wait": (ctypes.c_int, [_vp]),
     "asph_simulation_totals": (ctypes.c_int, [_vp, P(_p.CTotals)]),
     "asph_simulation_device_errors": (ctypes.c_int, [_vp, _up, ctypes.c_int]),
     "asph_simulation_set_stream": (ctypes.c_int, [_vp, _vp]),

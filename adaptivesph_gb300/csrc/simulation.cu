@@ -222,6 +222,9 @@ struct asph_simulation {
     cudaStream_t aux = nullptr;  // heavy-particle kernels, forked from and joined back into `stream`
     int heavy_priority = 0;      // the device's highest stream priority, given to the heavy kernels
     cudaEvent_t ev_fork = nullptr, ev_main = nullptr, ev_aux = nullptr;
+    cudaStream_t copy = nullptr;  // device-to-host copies of asynchronous exports (created on first use)
+    cudaEvent_t ev_export_ready = nullptr, ev_export_done = nullptr;
+    bool export_inflight = false;
     cudaEvent_t ev_refine = nullptr;  // end of a refinement pass whose read-back has not been taken yet
     bool refine_pending = false;
     uint64_t launches = 0;
@@ -823,6 +826,67 @@ asph_status ensure_grid(asph_simulation* s) {
     return build_grid(s, false, 0.0f, true);
 }
 
+// Waits for the copies of an asynchronous export still in flight.
+asph_status export_settle(asph_simulation* s) {
+    if (!s->export_inflight) return ASPH_OK;
+    CK(cudaEventSynchronize(s->ev_export_done));
+    s->export_inflight = false;
+    return ASPH_OK;
+}
+
+// Device staging of one export: positions, velocities (pending half-kick applied), densities, radii, ids.
+struct ExportStage {
+    float4* pos;
+    float4* vel;
+    float* rho;
+    float* rad;
+    uint32_t* ids;
+    size_t n;
+};
+
+// Writes the requested export arrays of the current particles into the staging buffer (kept across calls, grown on
+// demand, so that a per-frame export allocates nothing), on the simulation's stream.
+asph_status export_stage(asph_simulation* s, const void* positions, const void* velocities, const void* densities,
+                         const void* radii, const void* ids, ExportStage& x) {
+    const size_t n = s->n;
+    const size_t bytes = n * (16 + 16 + 4 + 4 + 4);
+    if (bytes > s->stage_bytes) {
+        asph_status st = export_settle(s);
+        if (st != ASPH_OK) return st;
+        CK(cudaStreamSynchronize(s->stream));
+        dfree(s->stage);
+        s->stage = nullptr;
+        s->stage_bytes = 0;
+        if ((st = dalloc(s->stage, bytes)) != ASPH_OK) return st;
+        s->stage_bytes = bytes;
+    }
+    x.n = n;
+    x.pos = reinterpret_cast<float4*>(s->stage);
+    x.vel = x.pos + n;
+    x.rho = reinterpret_cast<float*>(x.vel + n);
+    x.rad = x.rho + n;
+    x.ids = reinterpret_cast<uint32_t*>(x.rad + n);
+    k_export<<<blocks_for((uint32_t)n), 256, 0, s->stream>>>(s->args(s->cur), s->pending_half, s->has_pending ? 1 : 0,
+                                                            positions ? x.pos : nullptr, velocities ? x.vel : nullptr,
+                                                            densities ? x.rho : nullptr, radii ? x.rad : nullptr,
+                                                            ids ? x.ids : nullptr);
+    CK_LAUNCH("k_export");
+    s->launches++;
+    return ASPH_OK;
+}
+
+// Device-to-host copies of a staged export on `stream`.
+asph_status export_copies(asph_simulation* s, cudaStream_t stream, const ExportStage& x, float* positions,
+                          float* velocities, float* densities, float* radii, uint32_t* ids) {
+    (void)s;
+    if (positions) CK(cudaMemcpyAsync(positions, x.pos, 16 * x.n, cudaMemcpyDeviceToHost, stream));
+    if (velocities) CK(cudaMemcpyAsync(velocities, x.vel, 16 * x.n, cudaMemcpyDeviceToHost, stream));
+    if (densities) CK(cudaMemcpyAsync(densities, x.rho, 4 * x.n, cudaMemcpyDeviceToHost, stream));
+    if (radii) CK(cudaMemcpyAsync(radii, x.rad, 4 * x.n, cudaMemcpyDeviceToHost, stream));
+    if (ids) CK(cudaMemcpyAsync(ids, x.ids, 4 * x.n, cudaMemcpyDeviceToHost, stream));
+    return ASPH_OK;
+}
+
 void destroy(asph_simulation* s) {
     if (!s) return;
     if (s->stream) cudaStreamSynchronize(s->stream);
@@ -882,6 +946,10 @@ void destroy(asph_simulation* s) {
     }
     for (auto e : s->event_pool) cudaEventDestroy(e);
     if (s->aux) cudaStreamSynchronize(s->aux);
+    if (s->copy) cudaStreamSynchronize(s->copy);
+    if (s->ev_export_ready) cudaEventDestroy(s->ev_export_ready);
+    if (s->ev_export_done) cudaEventDestroy(s->ev_export_done);
+    if (s->copy) cudaStreamDestroy(s->copy);
     if (s->ev_fork) cudaEventDestroy(s->ev_fork);
     if (s->ev_main) cudaEventDestroy(s->ev_main);
     if (s->ev_aux) cudaEventDestroy(s->ev_aux);
@@ -1213,6 +1281,8 @@ asph_status asph_simulation_run_stages(asph_simulation* sim, float delta_time, u
 asph_status asph_simulation_synchronize(asph_simulation* sim) {
     API_ENTRY();
     if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
+    asph_status st = export_settle(sim);
+    if (st != ASPH_OK) return st;
     return check_errors(sim, true);
 }
 
@@ -1425,35 +1495,47 @@ asph_status asph_simulation_export_host(asph_simulation* sim, float* positions, 
     if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
     const uint32_t n = sim->n;
     if (capacity < n) return fail(ASPH_ERR_CAPACITY, "host arrays too small");
+    asph_status st = export_settle(sim);
+    if (st != ASPH_OK) return st;
     if (n == 0) return ASPH_OK;
-    // staging buffer kept across calls (grown on demand) so that a per-frame export allocates nothing
-    const size_t bytes = (size_t)n * (16 + 16 + 4 + 4 + 4);
-    if (bytes > sim->stage_bytes) {
-        dfree(sim->stage);
-        sim->stage = nullptr;
-        sim->stage_bytes = 0;
-        asph_status st;
-        if ((st = dalloc(sim->stage, bytes)) != ASPH_OK) return st;
-        sim->stage_bytes = bytes;
-    }
-    uint8_t* stage = sim->stage;
-    float4* dp = reinterpret_cast<float4*>(stage);
-    float4* dv = dp + n;
-    float* dr = reinterpret_cast<float*>(dv + n);
-    float* dd = dr + n;
-    uint32_t* di = reinterpret_cast<uint32_t*>(dd + n);
-    k_export<<<blocks_for(n), 256, 0, sim->stream>>>(sim->args(sim->cur), sim->pending_half, sim->has_pending ? 1 : 0,
-                                                      positions ? dp : nullptr, velocities ? dv : nullptr,
-                                                      densities ? dr : nullptr, radii ? dd : nullptr,
-                                                      ids ? di : nullptr);
-    CK_LAUNCH("k_export");
-    sim->launches++;
-    if (positions) CK(cudaMemcpyAsync(positions, dp, 16 * (size_t)n, cudaMemcpyDeviceToHost, sim->stream));
-    if (velocities) CK(cudaMemcpyAsync(velocities, dv, 16 * (size_t)n, cudaMemcpyDeviceToHost, sim->stream));
-    if (densities) CK(cudaMemcpyAsync(densities, dr, 4 * (size_t)n, cudaMemcpyDeviceToHost, sim->stream));
-    if (radii) CK(cudaMemcpyAsync(radii, dd, 4 * (size_t)n, cudaMemcpyDeviceToHost, sim->stream));
-    if (ids) CK(cudaMemcpyAsync(ids, di, 4 * (size_t)n, cudaMemcpyDeviceToHost, sim->stream));
+    ExportStage x;
+    if ((st = export_stage(sim, positions, velocities, densities, radii, ids, x)) != ASPH_OK) return st;
+    if ((st = export_copies(sim, sim->stream, x, positions, velocities, densities, radii, ids)) != ASPH_OK) return st;
     CK(cudaStreamSynchronize(sim->stream));
+    return check_errors(sim, false);
+}
+
+asph_status asph_simulation_export_host_async(asph_simulation* sim, float* positions, float* velocities,
+                                              float* densities, float* radii, uint32_t* ids, uint32_t capacity) {
+    API_ENTRY();
+    if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
+    const uint32_t n = sim->n;
+    if (capacity < n) return fail(ASPH_ERR_CAPACITY, "host arrays too small");
+    if (!sim->copy) {
+        cudaError_t e = cudaStreamCreateWithFlags(&sim->copy, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sim->ev_export_ready, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sim->ev_export_done, cudaEventDisableTiming);
+        if (e != cudaSuccess) return cuda_fail(e, "export stream");
+    }
+    if (n == 0) return ASPH_OK;
+    // the staging buffer is reused: the export kernel waits (on the device) for the previous copies
+    if (sim->export_inflight) CK(cudaStreamWaitEvent(sim->stream, sim->ev_export_done, 0));
+    ExportStage x;
+    asph_status st = export_stage(sim, positions, velocities, densities, radii, ids, x);
+    if (st != ASPH_OK) return st;
+    CK(cudaEventRecord(sim->ev_export_ready, sim->stream));
+    CK(cudaStreamWaitEvent(sim->copy, sim->ev_export_ready, 0));
+    if ((st = export_copies(sim, sim->copy, x, positions, velocities, densities, radii, ids)) != ASPH_OK) return st;
+    CK(cudaEventRecord(sim->ev_export_done, sim->copy));
+    sim->export_inflight = true;
+    return ASPH_OK;
+}
+
+asph_status asph_simulation_export_wait(asph_simulation* sim) {
+    API_ENTRY();
+    if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
+    asph_status st = export_settle(sim);
+    if (st != ASPH_OK) return st;
     return check_errors(sim, false);
 }
 

@@ -223,6 +223,19 @@ class Simulation:
                    "export_host")
         return out
 
+    def export_host_async(self, out: Dict[str, np.ndarray]) -> Dict[str, np.ndarray]:
+        """Enqueues the export into `out` (pinned arrays for asynchronous copies) and returns at once; the arrays
+        hold the particles of this point of the stream after export_wait()."""
+        cap = min(v.shape[0] for v in out.values()) if out else 0
+        _lib.check(self._lib.asph_simulation_export_host_async(self._h, _fp(out.get("positions")),
+                                                               _fp(out.get("velocities")), _fp(out.get("densities")),
+                                                               _fp(out.get("radii")), _up(out.get("ids")), cap),
+                   "export_host_async")
+        return out
+
+    def export_wait(self) -> None:
+        _lib.check(self._lib.asph_simulation_export_wait(self._h), "export_wait")
+
     def totals(self) -> Dict[str, float]:
         t = _p.CTotals()
         _lib.check(self._lib.asph_simulation_totals(self._h, ctypes.byref(t)), "totals")

@@ -221,7 +221,7 @@ asph_status asph_simulation_step_async(asph_simulation* sim, float delta_time);
  * written to *dt_used (no reference counterpart: the reference takes dt from its caller, app/App.cpp:230). */
 asph_status asph_simulation_step_cfl(asph_simulation* sim, float cfl, float dt_max, float* dt_used);
 
-/* Drains the simulation's stream and checks the device error word. */
+/* Drains the simulation's stream (and the copies of an asynchronous export) and checks the device error word. */
 asph_status asph_simulation_synchronize(asph_simulation* sim);
 
 /* Simulation::updateDomain (Simulation.cuh:125-126; SphSimulation.cu:122-134). */
@@ -258,6 +258,21 @@ asph_status asph_simulation_export_host(asph_simulation* sim,
                                         float* radii,
                                         uint32_t* ids,
                                         uint32_t capacity);
+
+/* The same export without waiting (no reference counterpart): the export kernel is enqueued behind the steps
+ * already enqueued and the device-to-host copies run on a copy stream of the simulation, so later steps overlap
+ * them. The host arrays (pinned for the copies to be asynchronous) must stay valid and must not be read until
+ * asph_simulation_export_wait returns. At most one such export is in flight: the next one reuses the staging
+ * buffer after the previous copies (a device-side wait, not a host one). */
+asph_status asph_simulation_export_host_async(asph_simulation* sim,
+                                              float* positions,
+                                              float* velocities,
+                                              float* densities,
+                                              float* radii,
+                                              uint32_t* ids,
+                                              uint32_t capacity);
+/* Waits for the copies of the last asph_simulation_export_host_async and checks the device error word. */
+asph_status asph_simulation_export_wait(asph_simulation* sim);
 
 /* FP64 totals (no reference counterpart). */
 asph_status asph_simulation_totals(asph_simulation* sim, asph_totals* out);

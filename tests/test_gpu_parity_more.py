@@ -157,3 +157,42 @@ def test_split_capacity_limit_bitexact():
         assert_state_bitexact(sim.read_state(), orc.arrays())
     assert hit, "the scene must reach the capacity"
     assert sim.get_fluid_particles_count() <= n + 60
+
+
+def test_async_export_overlapping_steps_bitexact():
+    """asph_simulation_export_host_async: frame k's copies run while frame k + 1 is enqueued and computed; each
+    frame's exported arrays equal the oracle's state of that frame."""
+    sc = small_dam_break()
+    sim, orc = make_pair(sc)
+    n = sc.positions.shape[0]
+
+    def host_set():
+        return dict(positions=np.zeros((n, 4), np.float32), velocities=np.zeros((n, 4), np.float32),
+                    densities=np.zeros(n, np.float32), radii=np.zeros(n, np.float32), ids=np.zeros(n, np.uint32))
+
+    sets = [host_set(), host_set()]
+    want = []
+
+    def check(k):
+        got, (pos, vel, rho, rad, ids) = sets[k % 2], want[k]
+        assert_bitexact("positions", got["positions"], pos)
+        assert_bitexact("velocities", got["velocities"], vel)
+        assert_bitexact("densities", got["densities"], rho)
+        assert_bitexact("radii", got["radii"], rad)
+        assert_bitexact("ids", got["ids"], ids)
+
+    for k in range(8):
+        sim.step_async(sc.dt)
+        orc.step(sc.dt)
+        if k > 0:
+            sim.export_wait()
+            check(k - 1)
+        sim.export_host_async(sets[k % 2])
+        o = orc.arrays()
+        want.append((o["pos"].copy(), orc.export_velocities().copy(), o["rho"].copy(), o["rad"].copy(),
+                     o["id"].copy()))
+    sim.export_wait()
+    check(7)
+    # a synchronous export after asynchronous ones sees the same state
+    sync = sim.export_host()
+    assert_bitexact("positions", sync["positions"], want[7][0])
