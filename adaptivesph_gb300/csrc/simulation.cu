@@ -57,7 +57,15 @@ static asph_status cuda_fail(cudaError_t e, const char* what) {
 static inline uint32_t blocks_for(uint32_t n, uint32_t t = 256) { return n == 0 ? 1u : (n + t - 1) / t; }
 
 // blocks of 8 warps for the heavy-particle kernels (one warp per heavy particle, grid-stride over the queue)
-static constexpr uint32_t kHeavyBlocks = 304;
+static constexpr uint32_t kHeavyBlocks = 304;  // grid of the one-warp-per-particle kernels at 600k particles and more
+
+// The grid of the one-warp-per-particle kernels (heavy boxes, overflowed and long rows): they stride over a queue
+// whose length is known only on the device, usually a small fraction of the particles, so small simulations get a
+// small grid (an empty queue still costs every block of the launch).
+uint32_t heavy_blocks(uint32_t n) {
+    const uint32_t b = n / 2048u;
+    return b < 16u ? 16u : (b > kHeavyBlocks ? kHeavyBlocks : b);
+}
 
 // bytes of the per-simulation reduction scratch (totals, CFL minimum, density info)
 static constexpr size_t kRedBytes = 256;
@@ -581,10 +589,10 @@ asph_status run_density(asph_simulation* s) {
     CK(cudaMemsetAsync(s->fheavy_n, 0, 4 * sizeof(uint32_t), s->stream));
     CK(cudaEventRecord(s->ev_fork, s->stream));
     CK(cudaStreamWaitEvent(s->aux, s->ev_fork, 0));
-    CK(launch_density(kDensityHeavy, kHeavyBlocks, s->aux, s->heavy_priority, a, s->cells(), s->boundary(), s->nbrs()));
+    CK(launch_density(kDensityHeavy, heavy_blocks(s->span()), s->aux, s->heavy_priority, a, s->cells(), s->boundary(), s->nbrs()));
     CK(launch_density(kDensityOrdinary, blocks_for(s->span()), s->stream, 0, a, s->cells(), s->boundary(), s->nbrs()));
-    CK(launch_density(kDensityOverflow, kHeavyBlocks, s->stream, 0, a, s->cells(), s->boundary(), s->nbrs()));
-    CK(launch_density(kDensityRow, kHeavyBlocks, s->stream, 0, a, s->cells(), s->boundary(), s->nbrs()));
+    CK(launch_density(kDensityOverflow, heavy_blocks(s->span()), s->stream, 0, a, s->cells(), s->boundary(), s->nbrs()));
+    CK(launch_density(kDensityRow, heavy_blocks(s->span()), s->stream, 0, a, s->cells(), s->boundary(), s->nbrs()));
     CK(cudaEventRecord(s->ev_main, s->stream));
     CK(cudaEventRecord(s->ev_aux, s->aux));
     CK(cudaStreamWaitEvent(s->stream, s->ev_aux, 0));
@@ -597,11 +605,11 @@ asph_status run_forces(asph_simulation* s) {
     StepArgs a = s->args(s->cur);
     int h = s->tic();
     CK(cudaStreamWaitEvent(s->aux, s->ev_main, 0));
-    CK(launch_forces(kForcesHeavy, s->phys.morris != 0, kHeavyBlocks, s->aux, s->heavy_priority, a, s->cells(), s->boundary(),
+    CK(launch_forces(kForcesHeavy, s->phys.morris != 0, heavy_blocks(s->span()), s->aux, s->heavy_priority, a, s->cells(), s->boundary(),
                      s->nbrs()));
     CK(launch_forces(kForcesOrdinary, s->phys.morris != 0, blocks_for(s->span()), s->stream, 0, a, s->cells(), s->boundary(),
                      s->nbrs()));
-    CK(launch_forces(kForcesRow, s->phys.morris != 0, kHeavyBlocks, s->stream, 0, a, s->cells(), s->boundary(),
+    CK(launch_forces(kForcesRow, s->phys.morris != 0, heavy_blocks(s->span()), s->stream, 0, a, s->cells(), s->boundary(),
                      s->nbrs()));
     CK(cudaEventRecord(s->ev_aux, s->aux));
     CK(cudaStreamWaitEvent(s->stream, s->ev_aux, 0));
@@ -683,7 +691,7 @@ asph_status refine_enqueue(asph_simulation* s) {
     k_cand_init<<<nbk, 256, 0, s->stream>>>(r, n);
     k_mark_eligible<<<nbk, 256, 0, s->stream>>>(r, s->vals);
     k_merge_candidates<<<nbk, 256, 0, s->stream>>>(a, s->cells(), r);
-    k_merge_candidates_heavy<<<kHeavyBlocks, 256, 0, s->stream>>>(a, s->cells(), r);
+    k_merge_candidates_heavy<<<heavy_blocks(n), 256, 0, s->stream>>>(a, s->cells(), r);
     k_merge_pairs<<<nbk, 256, 0, s->stream>>>(a, r);
     CK_LAUNCH("merge");
     // stable compaction into the other buffer set (also carries the cell keys for the vorticity split pass)
