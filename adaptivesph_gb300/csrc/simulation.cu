@@ -1999,6 +1999,9 @@ asph_status graph_step(asph_simulation* s, SceneGraph& g, float dt, AdvanceStats
 
 namespace asph {
 
+// plain steps a simulation may run ahead per round of advance_scenes (the reference's default refinement cooldown)
+constexpr uint32_t kRoundSteps = 10;
+
 asph_status advance_scenes(asph_simulation* const* sims, SceneGraph* const* graphs, const float* dts, uint32_t* left,
                            size_t count, AdvanceStats& stats) {
     for (size_t k = 0; k < count; k++) {
@@ -2008,21 +2011,25 @@ asph_status advance_scenes(asph_simulation* const* sims, SceneGraph* const* grap
     asph_status st;
     for (;;) {
         bool any = false;
-        // queue every simulation's plain steps up to its next refinement frame
+        // queue every simulation's plain steps up to its next refinement frame, at most kRoundSteps of them, so
+        // that no simulation runs far ahead of the others: the device's work queues stay mixed to the end
         for (size_t k = 0; k < count; k++) {
             asph_simulation* s = sims[k];
-            while (left[k] > 0 && !refinement_due(s)) {
-                if (s->n == 0 && !s->refine_pending) {
+            for (uint32_t r = 0; r < kRoundSteps && left[k] > 0 && !refinement_due(s); r++) {
+                // an empty simulation, and a first step (no pending half-kick: its graph would replay only once),
+                // run eagerly
+                if ((s->n == 0 || !s->has_pending) && !s->refine_pending) {
                     if ((st = run_step(s, dts[k], ASPH_STAGE_ALL)) != ASPH_OK) return st;
                 } else if ((st = graph_step(s, *graphs[k], dts[k], stats)) != ASPH_OK) {
                     return st;
                 }
                 left[k]--;
+                any = true;
             }
         }
         // then the refinement frames, enqueued without waiting for their read-backs
         for (size_t k = 0; k < count; k++) {
-            if (left[k] == 0) continue;
+            if (left[k] == 0 || !refinement_due(sims[k])) continue;
             asph_simulation* s = sims[k];
             if ((st = refine_finish(s)) != ASPH_OK) return st;  // a pass starts from the previous one's count
             if ((st = run_step(s, dts[k], ASPH_STAGE_ALL, true)) != ASPH_OK) return st;
