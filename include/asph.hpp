@@ -171,6 +171,19 @@ public:
               "asph_simulation_export_host");
         return n;
     }
+    // Enqueues a copy of the particles into caller-owned host arrays (pinned for the copy to overlap later steps)
+    // and returns; the arrays hold them after waitForExport(). Returns the number of particles copied.
+    uint32_t readParticlesAsync(vec4* positions, vec4* velocities, float* densities, float* radii, uint32_t* ids,
+                                uint32_t capacity) {
+        const uint32_t n = getFluidParticlesCount();
+        check(asph_simulation_export_host_async(s_, positions ? positions->data() : nullptr,
+                                                velocities ? velocities->data() : nullptr, densities, radii, ids,
+                                                capacity),
+              "asph_simulation_export_host_async");
+        return n;
+    }
+    void waitForExport() { check(asph_simulation_export_wait(s_), "asph_simulation_export_wait"); }
+    void stepAsync(float deltaTime) { check(asph_simulation_step_async(s_, deltaTime), "asph_simulation_step_async"); }
     asph_simulation* handle() const noexcept { return s_; }
 
 private:

@@ -3,6 +3,7 @@
 //
 // usage: hpp_client <input> <output>   (formats as abi_client.cpp)
 #include <cstdio>
+#include <cstring>
 #include <optional>
 #include <stdexcept>
 #include <vector>
@@ -49,7 +50,21 @@ int main(int argc, char** argv) {
                                                  boundary.getParticleCount());
         if (simulation->getBoundaryParticlesCount() != boundary.getParticleCount())
             throw std::runtime_error("boundary count");
-        for (uint32_t k = 0; k < steps; k++) simulation->update(dt);
+        // the first half of the steps through update(), the rest enqueued with stepAsync() while the state after
+        // the first half is copied out asynchronously (it must equal a synchronous read taken at the same point)
+        const uint32_t half = steps / 2;
+        for (uint32_t k = 0; k < half; k++) simulation->update(dt);
+        std::vector<asph::vec4> mpos, mpos_async(simulation->getFluidParticlesCount());
+        std::vector<asph::vec4> mvel;
+        std::vector<float> mrho, mrad;
+        std::vector<uint32_t> mid;
+        simulation->readParticles(mpos, mvel, mrho, mrad, mid);
+        simulation->readParticlesAsync(mpos_async.data(), nullptr, nullptr, nullptr, nullptr,
+                                       static_cast<uint32_t>(mpos_async.size()));
+        for (uint32_t k = half; k < steps; k++) simulation->stepAsync(dt);
+        simulation->waitForExport();
+        if (std::memcmp(mpos.data(), mpos_async.data(), mpos.size() * sizeof(asph::vec4)) != 0)
+            throw std::runtime_error("asynchronous export differs from the synchronous one");
 
         std::vector<asph::vec4> opos, ovel;
         std::vector<float> orho, orad;
