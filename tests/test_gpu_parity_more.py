@@ -196,3 +196,20 @@ def test_async_export_overlapping_steps_bitexact():
     # a synchronous export after asynchronous ones sees the same state
     sync = sim.export_host()
     assert_bitexact("positions", sync["positions"], want[7][0])
+
+
+def test_dense_walls_bitexact():
+    """Walls generated at 1/15 of the fluid spacing, with 2h = 0.104 m reaching past them (they lie 0.05 m outside
+    the domain): a particle near a corner of the domain has thousands of wall neighbours in up to ~310 blocks of 32
+    members, more than its neighbour row holds after its fluid entries (about a dozen of the 154 particles that see
+    walls), so the force pass walks the wall cells for those instead of reading recorded wall entries, while the
+    others read theirs. Both must give the oracle's result bit for bit."""
+    sc = scenes.dam_break((8, 10, 6), 0.04, seed=13, tank=(0.6, 0.6, 0.4), viscosity=0.01)
+    sc = dataclasses.replace(sc, boundary_spacing=0.0027)
+    sim, orc = make_pair(sc)
+    assert sim.get_boundary_particles_count() > 300_000
+    for _ in range(4):
+        sim.update(sc.dt)
+        orc.step(sc.dt)
+    assert_state_bitexact(sim.read_state(), orc.arrays())
+    assert sim.device_errors() == 0
