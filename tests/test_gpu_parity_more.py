@@ -201,7 +201,7 @@ def test_async_export_overlapping_steps_bitexact():
 def test_dense_walls_bitexact():
     """Walls generated at 1/15 of the fluid spacing, with 2h = 0.104 m reaching past them (they lie 0.05 m outside
     the domain): a particle near a corner of the domain has thousands of wall neighbours in up to ~310 blocks of 32
-    members, more than its neighbour row holds after its fluid entries (about a dozen of the 154 particles that see
+    members, more than its neighbour row holds after its fluid entries (about a dozen of the 165 particles that see
     walls), so the force pass walks the wall cells for those instead of reading recorded wall entries, while the
     others read theirs. Both must give the oracle's result bit for bit."""
     sc = scenes.dam_break((8, 10, 6), 0.04, seed=13, tank=(0.6, 0.6, 0.4), viscosity=0.01)
