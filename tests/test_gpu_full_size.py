@@ -91,3 +91,40 @@ def test_adaptive_dam_break_1m_late_frames_bitexact():
         assert_state_bitexact(sim.read_state(), orc.arrays())
     assert refined, "the frames must include a refinement pass"
     assert sim.device_errors() == 0
+
+
+def test_taylor_green_128_cubed_bitexact_and_fp64():
+    """The periodic Taylor-Green vortex at 128^3 = 2,097,152 particles (Morris viscosity, Re = 100): two frames
+    bit-exact against the oracle over the whole state, then the third frame's densities and accelerations bit-exact
+    against the oracle's FP32 step and within 1e-5 of its FP64 step (density relative; force relative to the
+    magnitude the FP32 sum carries)."""
+    from adaptivesph_gb300 import _lib
+
+    sc = scenes.taylor_green(128)
+    n = sc.positions.shape[0]
+    bd = StaticBoundaryDomain.empty(sc.parameters.domain)
+    sim = create_simulation(sc.parameters, sc.positions, None, None, bd, None, n, 1)
+    orc = oracle.OracleSim(sc.parameters, sc.positions, None, None, None, capacity=n)
+    st = sim.read_state()
+    st["vel"] = sc.velocities.copy()
+    sim.write_state(st, next_id=n)
+    a = orc.arrays()
+    a["vel"] = sc.velocities.copy()
+    orc.load(a, next_id=n)
+    for _ in range(2):
+        sim.update(sc.dt)
+        orc.step(sc.dt)
+    assert_state_bitexact(sim.read_state(), orc.arrays())
+    sim.run_stages(sc.dt, _lib.STAGE_FORCES)
+    orc.integrate(sc.dt)
+    orc.grid_build()
+    orc.rho[: orc.n] = orc.density32()
+    g = sim.read_state()
+    np.testing.assert_array_equal(g["rho"].view(np.uint32), orc.rho[: orc.n].view(np.uint32))
+    np.testing.assert_array_equal(g["acc"].view(np.uint32), orc.forces32().view(np.uint32))
+    rho64 = orc.density64()
+    assert (np.abs(g["rho"] - rho64) / rho64).max() <= 1e-5
+    a64, scale = orc.forces64()
+    err = np.abs(g["acc"][:, :3].astype(np.float64) - a64[:, :3]).max(axis=1)
+    assert (err / scale).max() <= 1e-5
+    assert sim.device_errors() == 0
