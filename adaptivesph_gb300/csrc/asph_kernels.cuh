@@ -129,7 +129,7 @@ struct SortScratch {
     uint32_t max_tiles;
 };
 constexpr int kSortThreads = 256;
-constexpr int kSortItems = 8;
+constexpr int kSortItems = 12;
 constexpr int kSortTile = kSortThreads * kSortItems;
 size_t sort_scratch_bytes(uint32_t max_items);
 void sort_scratch_bind(SortScratch& s, void* base, uint32_t max_items);

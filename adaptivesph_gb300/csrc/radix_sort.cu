@@ -5,7 +5,7 @@
 // bits, after Adinets & Merrill, "Onesweep: A Faster Least Significant Digit Radix Sort for GPUs", 2022):
 //   1. one histogram kernel counts the digits of every pass at once;
 //   2. one scan kernel turns the counts into per-pass digit offsets;
-//   3. per pass, one onesweep kernel: each CTA takes the next tile (2048 keys) from an atomic counter, ranks its
+//   3. per pass, one onesweep kernel: each CTA takes the next tile (3072 keys) from an atomic counter, ranks its
 //      keys stably per digit (warp match + per-warp counters), publishes its per-digit tile counts, looks back
 //      over predecessor tiles for the exclusive prefix (decoupled look-back), and scatters.
 // Stability: within a tile items are ranked in index order; tiles are ordered by index; so equal keys keep
