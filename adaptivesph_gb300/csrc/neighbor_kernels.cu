@@ -221,7 +221,7 @@ __device__ __forceinline__ ForceCtx force_ctx(const StepArgs& a, uint32_t i) {
 }
 
 // Pressure, viscosity and cohesion terms of fluid neighbour j (Algorithm.cu:56-221).
-template <bool kMorris>
+template <bool kMorris, bool kSigma = true>
 __device__ __forceinline__ void force_term(const StepArgs& a, const ForceCtx& c, uint32_t j, float shx, float shy,
                                            float shz, ForceAcc& f) {
     const bool periodic = a.grid.periodic;
@@ -274,7 +274,7 @@ __device__ __forceinline__ void force_term(const StepArgs& a, const ForceCtx& c,
             for (int q = 0; q < 3; q++) f.av[q] = fmaf(sv, vd[q], f.av[q]);
         }
     }
-    if (c.sigma_on) {
+    if (kSigma && c.sigma_on) {
         const float ss = mj * kernel_w(r, kj.x, kj.y);
 #pragma unroll
         for (int q = 0; q < 3; q++) f.as[q] = fmaf(ss, u[q], f.as[q]);
@@ -283,7 +283,7 @@ __device__ __forceinline__ void force_term(const StepArgs& a, const ForceCtx& c,
 
 // force_term for two neighbours: the per-pair quantities in packed FP32x2 arithmetic (each half rounds as the
 // scalar operation; divisions and square roots stay scalar), each accumulator updated for j1, then j2.
-template <bool kMorris, bool kPeriodic>
+template <bool kMorris, bool kPeriodic, bool kSigma = true>
 __device__ __forceinline__ void force_pair(const StepArgs& a, const ForceCtx& c, uint32_t j1, float s1x, float s1y,
                                            float s1z, uint32_t j2, float s2x, float s2y, float s2z, ForceAcc& f) {
     const float4 p1 = __ldg(a.ph + j1), p2 = __ldg(a.ph + j2);
@@ -385,7 +385,7 @@ __device__ __forceinline__ void force_pair(const StepArgs& a, const ForceCtx& c,
             }
         }
     }
-    if (c.sigma_on) {
+    if (kSigma && c.sigma_on) {
         if (ok1) {
             const float ss = m.x * kernel_w(r.x, k1.x, k1.y);
             f.as[0] = fmaf(ss, ux.x, f.as[0]);
@@ -788,8 +788,8 @@ __global__ void __launch_bounds__(256, 1) k_density_heavy(StepArgs a, CellsDev c
 
 // Force pass, ordinary particles: walks the particle's neighbour list. Heavy particles and particles whose row
 // overflowed are left to k_forces_heavy.
-template <bool kMorris>
-__global__ void __launch_bounds__(256, 3) k_forces(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
+template <bool kMorris, bool kSigma>
+__global__ void __launch_bounds__(128, 7) k_forces(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count_of(a)) return;
     const uint32_t cnt = nl.cnt[i];
@@ -826,13 +826,13 @@ __global__ void __launch_bounds__(256, 3) k_forces(StepArgs a, CellsDev c, Bound
         float s1x, s1y, s1z, s2x, s2y, s2z;
         if (!pull(j1, s1x, s1y, s1z)) break;
         if (!pull(j2, s2x, s2y, s2z)) {
-            force_term<kMorris>(a, x, j1, s1x, s1y, s1z, f);
+            force_term<kMorris, kSigma>(a, x, j1, s1x, s1y, s1z, f);
             break;
         }
         if (periodic)
-            force_pair<kMorris, true>(a, x, j1, s1x, s1y, s1z, j2, s2x, s2y, s2z, f);
+            force_pair<kMorris, true, kSigma>(a, x, j1, s1x, s1y, s1z, j2, s2x, s2y, s2z, f);
         else
-            force_pair<kMorris, false>(a, x, j1, s1x, s1y, s1z, j2, s2x, s2y, s2z, f);
+            force_pair<kMorris, false, kSigma>(a, x, j1, s1x, s1y, s1z, j2, s2x, s2y, s2z, f);
     }
     const uint32_t bn = nl.bcnt[i];
     if (bn == kBoundaryWalk)
@@ -1011,10 +1011,17 @@ cudaError_t launch_forces(ForceKernel kind, bool morris, uint32_t blocks, cudaSt
         else
             k_forces_row<false><<<blocks, 256, 0, stream>>>(a, b, nl);
     } else {
-        if (morris)
-            k_forces<true><<<blocks, 256, 0, stream>>>(a, c, b, nl);
+        // the cohesion term is compiled out when the surface tension constant is zero (the reference's configs);
+        // blocks of 128 threads at 72 registers keep 28 warps per SM resident (blocks of 256 would allow 24)
+        const bool sigma = a.phys.sigma_on != 0;
+        if (morris && sigma)
+            k_forces<true, true><<<2 * blocks, 128, 0, stream>>>(a, c, b, nl);
+        else if (morris)
+            k_forces<true, false><<<2 * blocks, 128, 0, stream>>>(a, c, b, nl);
+        else if (sigma)
+            k_forces<false, true><<<2 * blocks, 128, 0, stream>>>(a, c, b, nl);
         else
-            k_forces<false><<<blocks, 256, 0, stream>>>(a, c, b, nl);
+            k_forces<false, false><<<2 * blocks, 128, 0, stream>>>(a, c, b, nl);
     }
     return cudaGetLastError();
 }

@@ -213,3 +213,32 @@ def test_dense_walls_bitexact():
         orc.step(sc.dt)
     assert_state_bitexact(sim.read_state(), orc.arrays())
     assert sim.device_errors() == 0
+
+
+@pytest.mark.parametrize("morris", [False, True])
+def test_cohesion_bitexact_and_fp64(morris):
+    """Surface tension on (computeSurfaceTensionAccelerations, Algorithm.cu:176-221; the reference's configs keep it
+    off, and the force kernel is compiled with the term only when it is on): a trajectory bit-exact against the
+    oracle, then one force pass against its FP32 and FP64 steps."""
+    from adaptivesph_gb300 import _lib
+    from adaptivesph_gb300.parameters import ViscosityModel
+
+    sc = small_dam_break()
+    p = dataclasses.replace(sc.parameters, surface_tension_constant=2.0)
+    if morris:
+        p = dataclasses.replace(p, viscosity_model=ViscosityModel.MORRIS, kinematic_viscosity=1e-3)
+    sc = dataclasses.replace(sc, parameters=p)
+    sim, orc = make_pair(sc)
+    for _ in range(6):
+        sim.update(sc.dt)
+        orc.step(sc.dt)
+    assert_state_bitexact(sim.read_state(), orc.arrays())
+    sim.run_stages(sc.dt, _lib.STAGE_FORCES)
+    orc.integrate(sc.dt)
+    orc.grid_build()
+    orc.rho[: orc.n] = orc.density32()
+    g = sim.read_state()
+    assert_bitexact("acc", g["acc"], orc.forces32())
+    a64, scale = orc.forces64()
+    err = np.abs(g["acc"][:, :3].astype(np.float64) - a64[:, :3]).max(axis=1)
+    assert (err / scale).max() <= 1e-5
