@@ -611,7 +611,7 @@ __device__ __forceinline__ void boundary_forces_rows(const StepArgs& a, const Bo
 
 // Density pass, ordinary particles; heavy particles are queued for k_density_heavy.
 template <bool kPeriodic>
-__global__ void __launch_bounds__(256, 4) k_density(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
+__global__ void __launch_bounds__(128, 7) k_density(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool in = i < count_of(a);
     const float4 pi = in ? a.ph[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -992,10 +992,10 @@ cudaError_t launch_density(DensityKernel kind, uint32_t blocks, cudaStream_t str
         k_density_heavy<<<blocks, 256, 0, stream>>>(a, c, b, nl, nl.dover, nl.dover_n, false);
     else if (kind == kDensityRow)
         k_density_row<<<blocks, 256, 0, stream>>>(a, b, nl);
-    else if (a.grid.periodic)
-        k_density<true><<<blocks, 256, 0, stream>>>(a, c, b, nl);
+    else if (a.grid.periodic)  // blocks of 128 threads at 72 registers: 28 warps per SM without spills
+        k_density<true><<<2 * blocks, 128, 0, stream>>>(a, c, b, nl);
     else
-        k_density<false><<<blocks, 256, 0, stream>>>(a, c, b, nl);
+        k_density<false><<<2 * blocks, 128, 0, stream>>>(a, c, b, nl);
     return cudaGetLastError();
 }
 
