@@ -9,9 +9,11 @@
 // candidate of its own cells (shared loads, no divergent loop control) and recording its accepted neighbours (self
 // included) in its row of the neighbour list. A row entry covers one block of up to 32 consecutive members of a
 // sub-cell: (first member | periodic image code, 32-bit acceptance mask), 8 bytes, written only for blocks holding
-// an accepted neighbour. Entries are staged in shared memory and flushed 8 at a time (64 bytes). Each lane then sums
-// its density over its row, and the force pass sums over the same row: the masks expanded in member order give the
-// accepted neighbours in the canonical order, one per loop iteration.
+// an accepted neighbour. Entries are written in 16-byte pairs (an even entry waits in registers for its partner).
+// Each lane then sums its density over its row, and the force pass sums over the same row: the masks expanded in
+// member order give the accepted neighbours in the canonical order, two per loop iteration in packed FP32x2. The
+// boundary density records the accepted wall blocks after the fluid entries in the same form, and the force pass
+// forms the wall terms from them.
 // Heavy particles (query box of more than 27 reference cells: smoothing lengths grown by merging) and particles
 // with more entries than a row holds: one warp per particle; the box's sub-cells are dealt to the lanes by their
 // canonical index (for_each_subcell_lane), each lane sums its sub-cells' members in order, and the lane sums are
