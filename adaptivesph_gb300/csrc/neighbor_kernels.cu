@@ -735,7 +735,7 @@ __global__ void __launch_bounds__(128, 7) k_density(StepArgs a, CellsDev c, Boun
 }
 
 // Density of the heavy particles: one warp per particle.
-__global__ void __launch_bounds__(256, 1) k_density_heavy(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl,
+__global__ void __launch_bounds__(128, 2) k_density_heavy(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl,
                                                           const uint32_t* queue, const uint32_t* queue_n, bool pooled) {
     const int lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -846,7 +846,7 @@ __global__ void __launch_bounds__(128, 7) k_forces(StepArgs a, CellsDev c, Bound
 
 // Forces of the heavy particles: one warp per particle.
 template <bool kMorris>
-__global__ void __launch_bounds__(256, 1) k_forces_heavy(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
+__global__ void __launch_bounds__(128, 2) k_forces_heavy(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
     const int lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -897,7 +897,7 @@ __global__ void __launch_bounds__(256, 1) k_forces_heavy(StepArgs a, CellsDev c,
 // Particles with long rows (kRowHeavy < cnt <= maxe): one warp per particle, row entry e on lane e mod 32, each
 // lane expanding its entries' masks in order; lane sums combined by the butterfly.
 
-__global__ void __launch_bounds__(256, 2) k_density_row(StepArgs a, BoundaryDev b, NbrDev nl) {
+__global__ void __launch_bounds__(128, 4) k_density_row(StepArgs a, BoundaryDev b, NbrDev nl) {
     const int lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -932,7 +932,7 @@ __global__ void __launch_bounds__(256, 2) k_density_row(StepArgs a, BoundaryDev 
 }
 
 template <bool kMorris>
-__global__ void __launch_bounds__(256, 2) k_forces_row(StepArgs a, BoundaryDev b, NbrDev nl) {
+__global__ void __launch_bounds__(128, 4) k_forces_row(StepArgs a, BoundaryDev b, NbrDev nl) {
     const int lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -974,8 +974,8 @@ template <class... Exp, class... Act>
 cudaError_t launch_with_priority(void (*kernel)(Exp...), uint32_t blocks, cudaStream_t stream, int priority,
                                  Act&&... args) {
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(blocks);
-    cfg.blockDim = dim3(256);
+    cfg.gridDim = dim3(2 * blocks);
+    cfg.blockDim = dim3(128);
     cfg.stream = stream;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributePriority;
@@ -991,9 +991,9 @@ cudaError_t launch_density(DensityKernel kind, uint32_t blocks, cudaStream_t str
         return launch_with_priority(k_density_heavy, blocks, stream, priority, a, c, b, nl, (const uint32_t*)nl.heavy,
                                     (const uint32_t*)nl.heavy_n, true);
     if (kind == kDensityOverflow)
-        k_density_heavy<<<blocks, 256, 0, stream>>>(a, c, b, nl, nl.dover, nl.dover_n, false);
+        k_density_heavy<<<2 * blocks, 128, 0, stream>>>(a, c, b, nl, nl.dover, nl.dover_n, false);
     else if (kind == kDensityRow)
-        k_density_row<<<blocks, 256, 0, stream>>>(a, b, nl);
+        k_density_row<<<2 * blocks, 128, 0, stream>>>(a, b, nl);
     else if (a.grid.periodic)  // blocks of 128 threads at 72 registers: 28 warps per SM without spills
         k_density<true><<<2 * blocks, 128, 0, stream>>>(a, c, b, nl);
     else
@@ -1009,9 +1009,9 @@ cudaError_t launch_forces(ForceKernel kind, bool morris, uint32_t blocks, cudaSt
     }
     if (kind == kForcesRow) {
         if (morris)
-            k_forces_row<true><<<blocks, 256, 0, stream>>>(a, b, nl);
+            k_forces_row<true><<<2 * blocks, 128, 0, stream>>>(a, b, nl);
         else
-            k_forces_row<false><<<blocks, 256, 0, stream>>>(a, b, nl);
+            k_forces_row<false><<<2 * blocks, 128, 0, stream>>>(a, b, nl);
     } else {
         // the cohesion term is compiled out when the surface tension constant is zero (the reference's configs);
         // blocks of 128 threads at 72 registers keep 28 warps per SM resident (blocks of 256 would allow 24)
