@@ -480,7 +480,7 @@ asph_status asph_server_stats(const asph_server* server, uint64_t* used_bytes, u
  * stall other streams (cudaFree synchronises the device) or could fail mid-frame.
  *
  * The call allocates nothing: its scratch is one fixed array of device memory inside this library
- * (about 5.1 MB, sized for ASPH_NOALLOC_MAX_PARTICLES). count > ASPH_NOALLOC_MAX_PARTICLES is
+ * (about 4.9 MB, sized for ASPH_NOALLOC_MAX_PARTICLES). count > ASPH_NOALLOC_MAX_PARTICLES is
  * rejected with ASPH_ERR_CAPACITY. The first call on each device looks up the scratch address with
  * that device current (and, with lazy module loading, loads the library's device code there); make
  * that first call before any stream capture. The scratch is shared by all calls on a device: calls
