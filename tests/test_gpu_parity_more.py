@@ -9,7 +9,8 @@ import pytest
 from adaptivesph_gb300 import StaticBoundaryDomain, create_simulation, scenes
 from adaptivesph_gb300.parameters import Criterion
 import oracle
-from helpers import adaptive_refinement, assert_bitexact, assert_state_bitexact, make_pair, small_dam_break
+from helpers import (adaptive_refinement, assert_bitexact, assert_state_bitexact, boundary_of, make_pair,
+                     small_dam_break)
 
 pytestmark = pytest.mark.gpu
 
@@ -242,3 +243,57 @@ def test_cohesion_bitexact_and_fp64(morris):
     a64, scale = orc.forces64()
     err = np.abs(g["acc"][:, :3].astype(np.float64) - a64[:, :3]).max(axis=1)
     assert (err / scale).max() <= 1e-5
+
+
+def test_update_domain_bitexact():
+    """Simulation::updateDomain (SphSimulation.cu:122-134; the reference's app calls it when the tank is resized,
+    app/App.cpp:369-373): the tank grows in x mid-run, with walls generated for the new tank. The oracle restarts
+    from the same state with the new domain and walls; both then run on, bit for bit."""
+    from adaptivesph_gb300.parameters import Domain
+
+    sc = small_dam_break()
+    _, orc = make_pair(sc)
+    bd0 = boundary_of(sc)
+    n = sc.positions.shape[0]
+    # the boundary capacity leaves room for the larger tank, as the reference's app sizes its buffers up front
+    sim = create_simulation(sc.parameters, sc.positions, None, None, bd0, None, n, 2 * bd0.get_particle_count())
+    for _ in range(5):
+        sim.update(sc.dt)
+        orc.step(sc.dt)
+    assert_state_bitexact(sim.read_state(), orc.arrays())
+    d0 = sc.parameters.domain
+    d1 = Domain(min=tuple(d0.min), max=(d0.max[0] + 0.2, d0.max[1], d0.max[2]), friction=d0.friction)
+    bd1 = StaticBoundaryDomain.generate(d1, sc.boundary_spacing, sc.parameters.rest_density,
+                                       sc.parameters.base_smoothing_radius)
+    sim.update_domain(d1, bd1)
+    assert sim.get_boundary_particles_count() == bd1.get_particle_count()
+    p1 = dataclasses.replace(sc.parameters, domain=d1)
+    orc1 = oracle.OracleSim(p1, sc.positions, bd1.positions, bd1.psi, None, capacity=n)
+    orc1.load(orc.arrays(), frame=int(orc.state.frame), next_id=int(orc.state.next_id),
+              pending_half=float(orc.state.pending_half) if orc.state.has_pending else None)
+    for _ in range(8):
+        sim.update(sc.dt)
+        orc1.step(sc.dt)
+    assert_state_bitexact(sim.read_state(), orc1.arrays())
+    # the fluid now spreads into the new part of the tank
+    assert sim.read_state()["pos"][:, 0].max() <= d1.max[0]
+
+
+def test_enable_adaptive_refinement_bitexact():
+    """Simulation::enableAdaptiveRefinement (AdaptiveSphSimulation.cu:87-90): the frame counter jumps to the initial
+    cooldown, so the next step runs a refinement pass; the oracle's counter is set the same way."""
+    ref = adaptive_refinement(initial_cooldown=50, cooldown=50)
+    sc = small_dam_break(refinement=ref)
+    sim, orc = make_pair(sc)
+    for _ in range(3):
+        sim.update(sc.dt)
+        assert not orc.step(sc.dt)
+    sim.enable_adaptive_refinement()
+    orc.state.frame = ref.initial_cooldown
+    sim.update(sc.dt)
+    assert orc.step(sc.dt), "the step after enableAdaptiveRefinement must refine"
+    rep, o = sim.last_refinement(), orc.last_report()
+    for key in ("merge_eligible", "merge_pairs", "split_candidates", "splits", "count_after"):
+        assert rep[key] == o[key], (key, rep[key], o[key])
+    assert rep["merge_pairs"] + rep["splits"] > 0
+    assert_state_bitexact(sim.read_state(), orc.arrays())
