@@ -99,8 +99,9 @@ __device__ __forceinline__ bool density_term(const StepArgs& a, float4 pi, uint3
 }
 
 // density_term for two neighbours, in packed FP32x2 arithmetic (each half rounds as the scalar operation), added in
-// order: j1 then j2.
-template <bool kPeriodic>
+// order: j1 then j2. kAccepted: both are members of the particle's row, accepted by the same support test (same
+// operands, same operations) in the scan, so the test is not repeated.
+template <bool kPeriodic, bool kAccepted = false>
 __device__ __forceinline__ void density_pair(const StepArgs& a, float4 pi, uint32_t j1, float s1x, float s1y,
                                              float s1z, uint32_t j2, float s2x, float s2y, float s2z, float& rho) {
     const float4 p1 = __ldg(a.ph + j1), p2 = __ldg(a.ph + j2);
@@ -126,8 +127,8 @@ __device__ __forceinline__ void density_pair(const StepArgs& a, float4 pi, uint3
     const float2 t4 = __fmul2_rn(tt, tt);
     const float2 w = __fmul2_rn(__fmul2_rn(make_float2(k1.y, k2.y), t4),
                                 __ffma2_rn(make_float2(2.0f, 2.0f), q, make_float2(1.0f, 1.0f)));
-    if (r2.x <= t2h.x) rho = fmaf(k1.w, q.x > 2.0f ? 0.0f : w.x, rho);
-    if (r2.y <= t2h.y) rho = fmaf(k2.w, q.y > 2.0f ? 0.0f : w.y, rho);
+    if (kAccepted || r2.x <= t2h.x) rho = fmaf(k1.w, q.x > 2.0f ? 0.0f : w.x, rho);
+    if (kAccepted || r2.y <= t2h.y) rho = fmaf(k2.w, q.y > 2.0f ? 0.0f : w.y, rho);
 }
 
 // Boundary density of particle i over the cells of lane `lane` (BoundaryAlgorithm.cu:15-51).
@@ -285,7 +286,7 @@ __device__ __forceinline__ void force_term(const StepArgs& a, const ForceCtx& c,
 
 // force_term for two neighbours: the per-pair quantities in packed FP32x2 arithmetic (each half rounds as the
 // scalar operation; divisions and square roots stay scalar), each accumulator updated for j1, then j2.
-template <bool kMorris, bool kPeriodic, bool kSigma = true>
+template <bool kMorris, bool kPeriodic, bool kSigma = true, bool kAccepted = false>
 __device__ __forceinline__ void force_pair(const StepArgs& a, const ForceCtx& c, uint32_t j1, float s1x, float s1y,
                                            float s1z, uint32_t j2, float s2x, float s2y, float s2z, ForceAcc& f) {
     const float4 p1 = __ldg(a.ph + j1), p2 = __ldg(a.ph + j2);
@@ -310,7 +311,7 @@ __device__ __forceinline__ void force_pair(const StepArgs& a, const ForceCtx& c,
     const float2 h = make_float2(p1.w, p2.w);
     const float2 twoh = __fadd2_rn(h, h);
     const float2 t2h = __fmul2_rn(twoh, twoh);
-    const bool ok1 = r2.x <= t2h.x, ok2 = r2.y <= t2h.y;
+    const bool ok1 = kAccepted || r2.x <= t2h.x, ok2 = kAccepted || r2.y <= t2h.y;
     const float2 r = make_float2(sqrtf(r2.x), sqrtf(r2.y));
     const float2 ir = make_float2(r.x > 0.0f ? 1.0f / r.x : 0.0f, r.y > 0.0f ? 1.0f / r.y : 0.0f);
     float2 ux = __fmul2_rn(dx, ir), uy = __fmul2_rn(dy, ir), uz = __fmul2_rn(dz, ir);
@@ -722,7 +723,7 @@ __global__ void __launch_bounds__(128, 7) k_density(StepArgs a, CellsDev c, Boun
                 density_term(a, pi, j1, s1x, s1y, s1z, rho);
                 break;
             }
-            density_pair<periodic>(a, pi, j1, s1x, s1y, s1z, j2, s2x, s2y, s2z, rho);
+            density_pair<periodic, true>(a, pi, j1, s1x, s1y, s1z, j2, s2x, s2y, s2z, rho);
         }
     }
     float rb = 0.0f;
@@ -832,9 +833,9 @@ __global__ void __launch_bounds__(128, 7) k_forces(StepArgs a, CellsDev c, Bound
             break;
         }
         if (periodic)
-            force_pair<kMorris, true, kSigma>(a, x, j1, s1x, s1y, s1z, j2, s2x, s2y, s2z, f);
+            force_pair<kMorris, true, kSigma, true>(a, x, j1, s1x, s1y, s1z, j2, s2x, s2y, s2z, f);
         else
-            force_pair<kMorris, false, kSigma>(a, x, j1, s1x, s1y, s1z, j2, s2x, s2y, s2z, f);
+            force_pair<kMorris, false, kSigma, true>(a, x, j1, s1x, s1y, s1z, j2, s2x, s2y, s2z, f);
     }
     const uint32_t bn = nl.bcnt[i];
     if (bn == kBoundaryWalk)
