@@ -884,9 +884,8 @@ asph_status export_stage(asph_simulation* s, const void* positions, const void* 
 }
 
 // Device-to-host copies of a staged export on `stream`.
-asph_status export_copies(asph_simulation* s, cudaStream_t stream, const ExportStage& x, float* positions,
-                          float* velocities, float* densities, float* radii, uint32_t* ids) {
-    (void)s;
+asph_status export_copies(cudaStream_t stream, const ExportStage& x, float* positions, float* velocities,
+                          float* densities, float* radii, uint32_t* ids) {
     if (positions) CK(cudaMemcpyAsync(positions, x.pos, 16 * x.n, cudaMemcpyDeviceToHost, stream));
     if (velocities) CK(cudaMemcpyAsync(velocities, x.vel, 16 * x.n, cudaMemcpyDeviceToHost, stream));
     if (densities) CK(cudaMemcpyAsync(densities, x.rho, 4 * x.n, cudaMemcpyDeviceToHost, stream));
@@ -1508,7 +1507,7 @@ asph_status asph_simulation_export_host(asph_simulation* sim, float* positions, 
     if (n == 0) return ASPH_OK;
     ExportStage x;
     if ((st = export_stage(sim, positions, velocities, densities, radii, ids, x)) != ASPH_OK) return st;
-    if ((st = export_copies(sim, sim->stream, x, positions, velocities, densities, radii, ids)) != ASPH_OK) return st;
+    if ((st = export_copies(sim->stream, x, positions, velocities, densities, radii, ids)) != ASPH_OK) return st;
     CK(cudaStreamSynchronize(sim->stream));
     return check_errors(sim, false);
 }
@@ -1533,7 +1532,7 @@ asph_status asph_simulation_export_host_async(asph_simulation* sim, float* posit
     if (st != ASPH_OK) return st;
     CK(cudaEventRecord(sim->ev_export_ready, sim->stream));
     CK(cudaStreamWaitEvent(sim->copy, sim->ev_export_ready, 0));
-    if ((st = export_copies(sim, sim->copy, x, positions, velocities, densities, radii, ids)) != ASPH_OK) return st;
+    if ((st = export_copies(sim->copy, x, positions, velocities, densities, radii, ids)) != ASPH_OK) return st;
     CK(cudaEventRecord(sim->ev_export_done, sim->copy));
     sim->export_inflight = true;
     return ASPH_OK;
