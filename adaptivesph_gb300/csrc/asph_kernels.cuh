@@ -112,9 +112,14 @@ constexpr int kHeavyCells = 27;
 __global__ void k_neighbor_counts(StepArgs a, CellsDev c, uint32_t* counts, unsigned long long* total);
 __global__ void k_export(StepArgs a, float pending_half, int has_pending, float4* pos_out, float4* vel_out,
                          float* rho_out, float* rad_out, uint32_t* id_out);
-__global__ void k_totals(StepArgs a, float pending_half, int has_pending, double* out, unsigned int* cfl_min_bits);
-__global__ void k_density_info(StepArgs a, float threshold, float rest, double* sum, unsigned int* minmax,
-                               unsigned int* counts);
+// fixed-order reductions: kRedBlocks blocks of 256 threads write one row of kRedCols partials each, which
+// k_reduce_rows combines in a fixed order (bit-identical results from run to run)
+constexpr uint32_t kRedBlocks = 304;
+constexpr uint32_t kRedCols = 8;
+__global__ void k_totals(StepArgs a, float pending_half, int has_pending, double* rows);
+__global__ void k_density_info(StepArgs a, float threshold, float rest, double* rows);
+__global__ void k_reduce_rows(const double* rows, uint32_t nrows, uint32_t ncols, uint32_t min_mask, uint32_t max_mask,
+                              double* out);
 
 // ------------------------------------------------------------------ radix sort (radix_sort.cu)
 // Stable LSD radix sort of (uint32 key, uint32 value) pairs, 8-bit digits, one onesweep pass per digit with

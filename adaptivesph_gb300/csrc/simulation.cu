@@ -68,7 +68,8 @@ uint32_t heavy_blocks(uint32_t n) {
 }
 
 // bytes of the per-simulation reduction scratch (totals, CFL minimum, density info)
-static constexpr size_t kRedBytes = 256;
+// reduction scratch: 8 result doubles, then kRedBlocks rows of kRedCols partials (k_totals, k_density_info)
+static constexpr size_t kRedBytes = 64 + sizeof(double) * kRedBlocks * kRedCols;
 
 // ------------------------------------------------------------------------------------------------ memory
 struct asph_memory {
@@ -179,7 +180,7 @@ struct asph_simulation {
     unsigned long long* q3 = nullptr;
     uint32_t* err = nullptr;
     uint32_t* d_count = nullptr;
-    uint8_t* red = nullptr;  // [kRedBytes] reduction scratch of totals, CFL and density info
+    uint8_t* red = nullptr;  // [kRedBytes] reduction scratch of totals, CFL and density info (fixed order)
     uint64_t device_bytes = 0;  // device memory held (device_bytes_for at creation)
 
     // boundary
@@ -251,6 +252,9 @@ struct asph_simulation {
     // set while a step is captured as a graph: kernels read the count from d_count, grids cover grid_n
     bool graph_mode = false;
     uint32_t grid_n = 0;
+    // bumped by every call that changes what a captured step holds by value or by pointer (grid, cell and boundary
+    // tables, parameters, particle arrays); a batch's cached graphs are recaptured when it changes
+    uint64_t generation = 0;
     uint32_t span() const { return graph_mode ? grid_n : n; }
 
     StepArgs args(int s) const {
@@ -1293,21 +1297,39 @@ asph_status asph_simulation_synchronize(asph_simulation* sim) {
     return check_errors(sim, true);
 }
 
+// Fixed-order FP64 reduction of the current state into h[0..ncols): k_totals or k_density_info, then k_reduce_rows.
+static asph_status reduce_state(asph_simulation* sim, bool density_info, float threshold, double* h) {
+    double* out = reinterpret_cast<double*>(sim->red);
+    double* rows = out + 8;
+    const uint32_t blocks = std::min<uint32_t>(kRedBlocks, blocks_for(sim->n));
+    uint32_t ncols, min_mask, max_mask;
+    if (density_info) {
+        k_density_info<<<blocks, 256, 0, sim->stream>>>(sim->args(sim->cur), threshold, sim->P.rest_density, rows);
+        CK_LAUNCH("k_density_info");
+        ncols = 6, min_mask = 1u << 1, max_mask = 1u << 2;
+    } else {
+        k_totals<<<blocks, 256, 0, sim->stream>>>(sim->args(sim->cur), sim->pending_half, sim->has_pending ? 1 : 0,
+                                                  rows);
+        CK_LAUNCH("k_totals");
+        ncols = 7, min_mask = 1u << 6, max_mask = 0;
+    }
+    k_reduce_rows<<<1, 256, 0, sim->stream>>>(rows, blocks, ncols, min_mask, max_mask, out);
+    CK_LAUNCH("k_reduce_rows");
+    sim->launches += 2;
+    CK(cudaMemcpyAsync(h, out, sizeof(double) * ncols, cudaMemcpyDeviceToHost, sim->stream));
+    CK(cudaStreamSynchronize(sim->stream));
+    return ASPH_OK;
+}
+
 asph_status asph_simulation_totals(asph_simulation* sim, asph_totals* out) {
     API_ENTRY();
     if (!sim || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
     std::memset(out, 0, sizeof(*out));
     out->count = sim->n;
     if (sim->n == 0) return ASPH_OK;
-    double* d = reinterpret_cast<double*>(sim->red);
-    CK(cudaMemsetAsync(d, 0, sizeof(double) * 6, sim->stream));
-    k_totals<<<blocks_for(sim->n), 256, 0, sim->stream>>>(sim->args(sim->cur), sim->pending_half,
-                                                          sim->has_pending ? 1 : 0, d, nullptr);
-    CK_LAUNCH("k_totals");
-    sim->launches++;
-    double h[6];
-    CK(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, sim->stream));
-    CK(cudaStreamSynchronize(sim->stream));
+    double h[8];
+    asph_status st = reduce_state(sim, false, 0.0f, h);
+    if (st != ASPH_OK) return st;
     out->mass = h[0];
     out->momentum[0] = h[1];
     out->momentum[1] = h[2];
@@ -1322,19 +1344,10 @@ asph_status asph_simulation_step_cfl(asph_simulation* sim, float cfl, float dt_m
     if (!sim || !(cfl > 0.0f)) return fail(ASPH_ERR_INVALID_ARGUMENT, "simulation and cfl > 0 required");
     float dt = dt_max > 0.0f ? dt_max : 3.402823466e38f;
     if (sim->n > 0) {
-        double* d = reinterpret_cast<double*>(sim->red);
-        CK(cudaMemsetAsync(d, 0, sizeof(double) * 8, sim->stream));
-        unsigned int* bits = reinterpret_cast<unsigned int*>(d + 6);
-        CK(cudaMemsetAsync(bits, 0x7f, sizeof(unsigned int), sim->stream));
-        k_totals<<<blocks_for(sim->n), 256, 0, sim->stream>>>(sim->args(sim->cur), sim->pending_half,
-                                                              sim->has_pending ? 1 : 0, d, bits);
-        CK_LAUNCH("k_totals");
-        sim->launches++;
-        unsigned int hb = 0;
-        CK(cudaMemcpyAsync(&hb, bits, sizeof(hb), cudaMemcpyDeviceToHost, sim->stream));
-        CK(cudaStreamSynchronize(sim->stream));
-        float m;
-        std::memcpy(&m, &hb, sizeof(m));
+        double h[8];
+        asph_status st = reduce_state(sim, false, 0.0f, h);
+        if (st != ASPH_OK) return st;
+        const float m = (float)h[6];  // a float converted to double and back: exact
         const float c = cfl * m;
         if (c < dt) dt = c;
     }
@@ -1358,6 +1371,7 @@ asph_status asph_simulation_update_domain(asph_simulation* sim, const asph_domai
         return fail(ASPH_ERR_CAPACITY, "more boundary particles than the sort capacity of this simulation");
     sim->P = P;
     sim->grid = g;
+    sim->generation++;
     if ((st = alloc_cells(sim)) != ASPH_OK) return st;
     if ((st = setup_boundary(sim, boundary, boundary_count)) != ASPH_OK) return st;
     sim->grid_valid = false;
@@ -1436,33 +1450,13 @@ asph_status asph_simulation_density_info(asph_simulation* sim, float threshold, 
         out->average_density = NAN;  // 0 / 0 as in the reference (SphSimulation.cu:283)
         return ASPH_OK;
     }
-    uint8_t* d = sim->red;
-    double* sum = reinterpret_cast<double*>(d);
-    unsigned int* mm = reinterpret_cast<unsigned int*>(d + 8);
-    unsigned int* cnt = reinterpret_cast<unsigned int*>(d + 16);
-    CK(cudaMemsetAsync(d, 0, 64, sim->stream));
-    CK(cudaMemsetAsync(mm, 0xff, sizeof(unsigned int), sim->stream));
-    k_density_info<<<blocks_for(sim->n), 256, 0, sim->stream>>>(sim->args(sim->cur), threshold, sim->P.rest_density,
-                                                                sum, mm, cnt);
-    CK_LAUNCH("k_density_info");
-    sim->launches++;
-    uint8_t h[64];
-    CK(cudaMemcpyAsync(h, d, 64, cudaMemcpyDeviceToHost, sim->stream));
-    CK(cudaStreamSynchronize(sim->stream));
-    double hs;
-    unsigned int hm[2], hc[3];
-    std::memcpy(&hs, h, 8);
-    std::memcpy(hm, h + 8, 8);
-    std::memcpy(hc, h + 16, 12);
-    auto unmap = [](unsigned int s) {
-        const uint32_t u = (s & 0x80000000u) ? (s & 0x7fffffffu) : ~s;
-        float f;
-        std::memcpy(&f, &u, 4);
-        return f;
-    };
-    out->min_density = unmap(hm[0]);
-    out->max_density = unmap(hm[1]);
-    out->average_density = (float)(hs / (double)sim->n);
+    double h[8];
+    asph_status st = reduce_state(sim, true, threshold, h);
+    if (st != ASPH_OK) return st;
+    out->min_density = (float)h[1];
+    out->max_density = (float)h[2];
+    out->average_density = (float)(h[0] / (double)sim->n);
+    const uint32_t hc[3] = {(uint32_t)h[3], (uint32_t)h[4], (uint32_t)h[5]};
     out->under_density_count = hc[0];
     out->normal_density_count = hc[1];
     out->over_density_count = hc[2];
@@ -1625,6 +1619,7 @@ asph_status asph_simulation_write_fluid(asph_simulation* sim, const asph_state_i
         return fail(ASPH_ERR_INVALID_ARGUMENT, "all state arrays are required");
     CK(cudaStreamSynchronize(sim->stream));
     sim->n = n;
+    sim->generation++;
     if (n > 0) {
         uint8_t* stage = nullptr;
         const size_t bytes = (size_t)n * (16 * 3 + 4 * 5);
@@ -1806,13 +1801,22 @@ __global__ void __launch_bounds__(256) k_noalloc_keys(GridDev g, const float4* _
     vals[i] = i;
 }
 
-// Scratch address on the current device, looked up once per device.
-asph_status noalloc_base(void** out) {
+// Scratch address on the current device. It is looked up again on every call made outside stream capture (the
+// lookup is cheap), so a device reset or a re-created primary context between calls finds the array's new address;
+// a call inside a capture uses the address of the last call outside one, which is why the first call on a device
+// must come before any capture.
+asph_status noalloc_base(cudaStream_t stream, void** out) {
     int dev = 0;
     CK(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(ASPH_ERR_UNSUPPORTED, "device ordinal out of range");
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(stream, &cs));
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (g_noalloc_base[dev] == nullptr) CK(cudaGetSymbolAddress(&g_noalloc_base[dev], g_noalloc_scratch));
+    if (cs == cudaStreamCaptureStatusNone) {
+        CK(cudaGetSymbolAddress(&g_noalloc_base[dev], g_noalloc_scratch));
+    } else if (g_noalloc_base[dev] == nullptr) {
+        return fail(ASPH_ERR_UNSUPPORTED, "asph_grid_sort_noalloc: the first call on a device must not be captured");
+    }
     *out = g_noalloc_base[dev];
     return ASPH_OK;
 }
@@ -1842,9 +1846,9 @@ extern "C" asph_status asph_grid_sort_noalloc(const asph_parameters* params, con
         return fail(ASPH_ERR_CAPACITY, "cell tables need " + std::to_string(g.ncells) + " entries");
     if (sort_scratch_bytes(kNoAllocMax) > kNoAllocSortBytes)
         return fail(ASPH_ERR_UNSUPPORTED, "sort scratch layout larger than the fixed array");
-    void* base = nullptr;
-    if ((st = noalloc_base(&base)) != ASPH_OK) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    void* base = nullptr;
+    if ((st = noalloc_base(s, &base)) != ASPH_OK) return st;
     uint32_t* d_n = static_cast<uint32_t*>(base);
     SortScratch ss;
     sort_scratch_bind(ss, static_cast<unsigned char*>(base) + kNoAllocHead, kNoAllocMax);
@@ -1886,9 +1890,11 @@ struct StepKey {
     uint32_t bound = 0;
     float dt = 0.0f, pending_half = 0.0f;
     bool has_pending = false;
+    uint64_t generation = 0;  // asph_simulation::generation at capture
     bool replays(const StepKey& o, uint32_t n) const {
         return n <= bound && bound == o.bound && std::memcmp(&dt, &o.dt, 4) == 0 &&
-               std::memcmp(&pending_half, &o.pending_half, 4) == 0 && has_pending == o.has_pending;
+               std::memcmp(&pending_half, &o.pending_half, 4) == 0 && has_pending == o.has_pending &&
+               generation == o.generation;
     }
 };
 
@@ -1964,7 +1970,7 @@ asph_status capture_step(asph_simulation* s, SceneGraph& g, float dt) {
         g.exec[parity] = nullptr;
         return cuda_fail(ie, "cudaGraphInstantiate");
     }
-    g.key[parity] = StepKey{bound, dt, s->pending_half, s->has_pending};
+    g.key[parity] = StepKey{bound, dt, s->pending_half, s->has_pending, s->generation};
     return ASPH_OK;
 }
 
@@ -1972,7 +1978,7 @@ asph_status capture_step(asph_simulation* s, SceneGraph& g, float dt) {
 // read-back is taken only when its worst case exceeds the graph's bound.
 asph_status graph_step(asph_simulation* s, SceneGraph& g, float dt, AdvanceStats& stats) {
     const int parity = s->cur;
-    const StepKey key{g.key[parity].bound, dt, s->pending_half, s->has_pending};
+    const StepKey key{g.key[parity].bound, dt, s->pending_half, s->has_pending, s->generation};
     const uint32_t n_max = s->refine_pending ? count_after_refine_bound(s) : s->n;
     if (!g.exec[parity] || !g.key[parity].replays(key, n_max)) {
         asph_status st = refine_finish(s);

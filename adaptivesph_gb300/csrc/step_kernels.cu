@@ -240,13 +240,37 @@ __global__ void __launch_bounds__(256) k_export(StepArgs a, float pending_half, 
     if (id_out) id_out[i] = a.id[i];
 }
 
-// FP64 totals (mass, momentum, kinetic energy, volume) and min_i h_i / (c0 + |v_i|) for the CFL step.
-__global__ void __launch_bounds__(256) k_totals(StepArgs a, float pending_half, int has_pending, double* out,
-                                                unsigned int* cfl_min_bits) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    double v[6] = {0, 0, 0, 0, 0, 0};
-    float cfl = 3.402823466e38f;
-    if (i < a.n) {
+// Fixed-order reductions. A grid of kRedBlocks blocks strides over the particles (the thread that handles particle i
+// depends only on i), every block reduces its threads in a fixed tree and writes one row of kRedCols partials, and
+// k_reduce_rows adds the rows in a fixed order: the results are bit-identical from run to run, which FP64 atomics
+// across blocks would not be.
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();  // sh may still be read from the previous column
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = sh[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) t += sh[w];
+    return t;
+}
+
+__device__ __forceinline__ double block_min(double v, double* sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = sh[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) t = fmin(t, sh[w]);
+    return t;
+}
+
+// FP64 totals (mass, momentum, kinetic energy, volume; columns 0-5) and min_i h_i / (c0 + |v_i|) for the CFL step
+// (column 6), one row of partials per block.
+__global__ void __launch_bounds__(256) k_totals(StepArgs a, float pending_half, int has_pending, double* rows) {
+    double v[7] = {0, 0, 0, 0, 0, 0, 1.0e300};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
         const float4 ph = a.ph[i];
         float4 vm = a.vm[i];
         if (has_pending) {
@@ -254,58 +278,70 @@ __global__ void __launch_bounds__(256) k_totals(StepArgs a, float pending_half, 
             kick(vm.x, vm.y, vm.z, ac.x, ac.y, ac.z, pending_half, a.phys.max_velocity);
         }
         const double m = vm.w;
-        v[0] = m;
-        v[1] = m * vm.x;
-        v[2] = m * vm.y;
-        v[3] = m * vm.z;
-        v[4] = 0.5 * m * ((double)vm.x * vm.x + (double)vm.y * vm.y + (double)vm.z * vm.z);
+        v[0] += m;
+        v[1] += m * vm.x;
+        v[2] += m * vm.y;
+        v[3] += m * vm.z;
+        v[4] += 0.5 * m * ((double)vm.x * vm.x + (double)vm.y * vm.y + (double)vm.z * vm.z);
         const float rho = a.rp[i].x;
-        v[5] = rho > 0.0f ? m / (double)rho : 0.0;
+        v[5] += rho > 0.0f ? m / (double)rho : 0.0;
         const float speed = sqrtf(fmaf(vm.z, vm.z, fmaf(vm.y, vm.y, vm.x * vm.x)));
-        cfl = ph.w / (a.phys.c0 + speed);
+        v[6] = fmin(v[6], (double)(ph.w / (a.phys.c0 + speed)));
     }
-    __shared__ double s[8][6];
-    __shared__ float sc[8];
+    __shared__ double sh[8];
+    double* row = rows + (size_t)blockIdx.x * kRedCols;
 #pragma unroll
     for (int k = 0; k < 6; k++) {
-        double t = v[k];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        v[k] = t;
+        const double t = block_sum(v[k], sh);
+        if (threadIdx.x == 0) row[k] = t;
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) cfl = fminf(cfl, __shfl_xor_sync(0xffffffffu, cfl, o));
-    if ((threadIdx.x & 31) == 0) {
-        for (int k = 0; k < 6; k++) s[threadIdx.x >> 5][k] = v[k];
-        sc[threadIdx.x >> 5] = cfl;
+    const double t = block_min(v[6], sh);
+    if (threadIdx.x == 0) row[6] = t;
+}
+
+// getDensityInfo (cuda/src/simulation/SphSimulation.cu:249-285): sum of densities (FP64), min, max, and the
+// under / normal / over counts (columns 0-5), one row of partials per block.
+__global__ void __launch_bounds__(256) k_density_info(StepArgs a, float threshold, float rest, double* rows) {
+    double v[6] = {0, 1.0e300, -1.0e300, 0, 0, 0};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
+        const float d = a.rp[i].x;
+        const float ratio = d / rest - 1.0f;
+        v[0] += (double)d;
+        v[1] = fmin(v[1], (double)d);
+        v[2] = fmax(v[2], (double)d);
+        if (ratio < -threshold) v[3] += 1.0;
+        if (ratio >= -threshold && ratio <= threshold) v[4] += 1.0;
+        if (ratio > threshold) v[5] += 1.0;
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
-            for (int k = 0; k < 6; k++) s[0][k] += s[w][k];
-            sc[0] = fminf(sc[0], sc[w]);
-        }
-        for (int k = 0; k < 6; k++) atomicAdd(out + k, s[0][k]);
-        if (cfl_min_bits) atomicMin(cfl_min_bits, __float_as_uint(sc[0]));
+    __shared__ double sh[8];
+    double* row = rows + (size_t)blockIdx.x * kRedCols;
+    double t = block_sum(v[0], sh);
+    if (threadIdx.x == 0) row[0] = t;
+    t = block_min(v[1], sh);
+    if (threadIdx.x == 0) row[1] = t;
+    t = -block_min(-v[2], sh);
+    if (threadIdx.x == 0) row[2] = t;
+    for (int k = 3; k < 6; k++) {
+        t = block_sum(v[k], sh);
+        if (threadIdx.x == 0) row[k] = t;
     }
 }
 
-// getDensityInfo (cuda/src/simulation/SphSimulation.cu:249-285); the mean is accumulated in FP64.
-__global__ void __launch_bounds__(256) k_density_info(StepArgs a, float threshold, float rest, double* sum,
-                                                      unsigned int* minmax, unsigned int* counts) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
-    const float d = a.rp[i].x;
-    const float ratio = d / rest - 1.0f;
-    atomicAdd(sum, (double)d);
-    // order-preserving integer image of the float for min/max
-    const uint32_t u = __float_as_uint(d);
-    const uint32_t s = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-    atomicMin(minmax, s);
-    atomicMax(minmax + 1, s);
-    if (ratio < -threshold) atomicAdd(counts, 1u);
-    if (ratio >= -threshold && ratio <= threshold) atomicAdd(counts + 1, 1u);
-    if (ratio > threshold) atomicAdd(counts + 2, 1u);
+// out[k] = the sum (or, for the columns in min_mask / max_mask, the min / max) of column k over `nrows` rows,
+// added in a fixed order. One block of 256 threads.
+__global__ void __launch_bounds__(256) k_reduce_rows(const double* rows, uint32_t nrows, uint32_t ncols,
+                                                     uint32_t min_mask, uint32_t max_mask, double* out) {
+    __shared__ double sh[8];
+    for (uint32_t k = 0; k < ncols; k++) {
+        const bool is_min = (min_mask >> k) & 1u, is_max = (max_mask >> k) & 1u;
+        double v = is_min ? 1.0e300 : (is_max ? -1.0e300 : 0.0);
+        for (uint32_t r = threadIdx.x; r < nrows; r += blockDim.x) {
+            const double x = rows[(size_t)r * kRedCols + k];
+            v = is_min ? fmin(v, x) : (is_max ? fmax(v, x) : v + x);
+        }
+        const double t = is_min ? block_min(v, sh) : (is_max ? -block_min(-v, sh) : block_sum(v, sh));
+        if (threadIdx.x == 0) out[k] = t;
+    }
 }
 
 }  // namespace asph

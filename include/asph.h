@@ -481,9 +481,11 @@ asph_status asph_server_stats(const asph_server* server, uint64_t* used_bytes, u
  *
  * The call allocates nothing: its scratch is one fixed array of device memory inside this library
  * (about 4.9 MB, sized for ASPH_NOALLOC_MAX_PARTICLES). count > ASPH_NOALLOC_MAX_PARTICLES is
- * rejected with ASPH_ERR_CAPACITY. The first call on each device looks up the scratch address with
- * that device current (and, with lazy module loading, loads the library's device code there); make
- * that first call before any stream capture. The scratch is shared by all calls on a device: calls
+ * rejected with ASPH_ERR_CAPACITY. Every call made outside stream capture looks up the scratch
+ * address on the current device (the first one, with lazy module loading, also loads the library's
+ * device code there), so a device reset between calls is followed; a captured call reuses the address
+ * of the last uncaptured call on that device, so make the first call on each device before any stream
+ * capture (a first call inside a capture is refused). The scratch is shared by all calls on a device: calls
  * that may overlap (different streams, or several host threads) race on it and must be serialised
  * by the caller. The sort's counters are zeroed by the call itself on `stream`; nothing in the
  * scratch has to start at zero. The caller zeroes `device_errors` before its first use.

@@ -64,6 +64,45 @@ def test_noalloc_sort_matches_simulation_grid_two_calls():
     _check_against_simulation(sim, sc.parameters, np.ascontiguousarray(sim.read_state()["pos"]))
 
 
+def test_noalloc_sort_at_the_limit_three_digit_passes_no_device_memory_change():
+    """ASPH_NOALLOC_MAX_PARTICLES seeded random positions in the reference's 1.6 x 1.0 x 0.67 m tank at dx = 0.01 m
+    (62 x 40 x 26 sub-cells: 18-bit keys, three digit passes, so the sorted result comes back out of the scratch half
+    and 171 tiles exercise the look-back across tiles), against the simulation's grid build of the same positions;
+    two calls in a row, with the device's free memory unchanged across both."""
+    from adaptivesph_gb300 import StaticBoundaryDomain, create_simulation, scenes
+
+    limit = 524288
+    sc = scenes.dam_break((40, 80, 40), 0.01, seed=1)
+    d = sc.parameters.domain
+    rng = np.random.default_rng(7)
+    lo = np.array(d.min, np.float32)
+    hi = np.array(d.max, np.float32)
+    pos4 = np.zeros((limit, 4), np.float32)
+    pos4[:, :3] = (lo + (hi - lo) * rng.random((limit, 3), dtype=np.float32)).astype(np.float32)
+    sim = create_simulation(sc.parameters, pos4, None, None, StaticBoundaryDomain.empty(d), None, limit, 1)
+    info = sim.grid_info()
+    assert int(info["key_bits"]) > 16, "three digit passes wanted"
+    sim.run_stages(0.0, _lib.STAGE_GRID)
+    _check_against_simulation(sim, sc.parameters, pos4)  # also loads the library's device code, if not yet
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(2):
+        got_keys, order, got_start, got_end, err = _noalloc_sort(sc.parameters, pos4, int(info["cell_count"]))
+        assert err == 0
+        keys, start, end = sim.read_grid()
+        assert_bitexact("sorted keys", got_keys, keys)
+        assert_bitexact("cell_start", got_start, start)
+        assert_bitexact("cell_end", got_end, end)
+        input_keys = np.empty_like(got_keys)
+        input_keys[order] = got_keys
+        assert_bitexact("order", order, np.argsort(input_keys, kind="stable").astype(np.uint32))
+    torch.cuda.synchronize()
+    # the device arrays of _noalloc_sort are freed back to torch's cache, not to the device: the driver's free
+    # memory moves only if something allocated device memory
+    assert torch.cuda.mem_get_info()[0] == free0
+    sim.close()
+
+
 def test_noalloc_sort_rejects_count_above_limit():
     sc = small_dam_break()
     L = _lib.load()
