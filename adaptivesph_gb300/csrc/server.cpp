@@ -65,7 +65,10 @@ struct asph_server {
     std::vector<Request*> active;                        // admitted and running
     std::map<uint64_t, std::unique_ptr<Request>> all;    // every request not yet taken
     asph::AdvanceStats stats;
-    std::mutex lock;  // submissions may come from another thread than the one polling
+    // Submissions, status and stats may come from other threads than the one polling: every change of the queue,
+    // the active list, a request's state and the budget is made under this lock (the polling thread alone changes
+    // the active list, so it reads it without the lock).
+    mutable std::mutex lock;
 
     double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
 };
@@ -87,12 +90,14 @@ void admit(asph_server* sv, Request* r) {
     }
     if (st != ASPH_OK) {
         if (sim) asph_simulation_destroy(sim);
+        std::lock_guard<std::mutex> g(sv->lock);
         r->state = ASPH_REQUEST_FAILED;
         r->error = st;
         r->message = asph_last_error();
         r->t_finish = sv->now();
         return;
     }
+    std::lock_guard<std::mutex> g(sv->lock);
     r->sim = sim;
     r->state = ASPH_REQUEST_ACTIVE;
     sv->used += r->bytes;
@@ -101,7 +106,8 @@ void admit(asph_server* sv, Request* r) {
     std::vector<float>().swap(r->positions);
 }
 
-// Copies a finished request's particles to host memory and returns its device memory to the budget.
+// Copies a finished request's particles to host memory and returns its device memory to the budget. Called with
+// the server's lock held.
 void retire(asph_server* sv, Request* r) {
     uint32_t n = 0;
     asph_status st = asph_simulation_fluid_count(r->sim, &n);
@@ -206,9 +212,13 @@ asph_status asph_server_poll(asph_server* sv, uint32_t max_steps, uint32_t* outs
             left[k] = std::min(max_steps ? max_steps : r->steps, r->steps - r->done);
             before[k] = left[k];
         }
-        const asph_status st = asph::advance_scenes(sims.data(), graphs.data(), dts.data(), left.data(), S,
-                                                    sv->stats);
+        asph::AdvanceStats adv{};
+        const asph_status st = asph::advance_scenes(sims.data(), graphs.data(), dts.data(), left.data(), S, adv);
         std::vector<Request*> still;
+        std::lock_guard<std::mutex> g(sv->lock);
+        sv->stats.graph_steps += adv.graph_steps;
+        sv->stats.eager_steps += adv.eager_steps;
+        sv->stats.captures += adv.captures;
         for (size_t k = 0; k < S; k++) {
             Request* r = sv->active[k];
             r->done += before[k] - left[k];
@@ -281,6 +291,7 @@ asph_status asph_server_take(asph_server* sv, uint64_t ticket, float* positions,
 asph_status asph_server_stats(const asph_server* sv, uint64_t* used_bytes, uint32_t* queued, uint32_t* active,
                               uint64_t* graph_steps, uint64_t* eager_steps) {
     if (!sv) return ASPH_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(sv->lock);
     if (used_bytes) *used_bytes = sv->used;
     if (queued) *queued = (uint32_t)sv->queue.size();
     if (active) *active = (uint32_t)sv->active.size();

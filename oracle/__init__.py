@@ -102,6 +102,25 @@ class OrcState(ctypes.Structure):
     ]
 
 
+class OrcState64(ctypes.Structure):
+    _fields_ = [
+        ("n", ctypes.c_uint32),
+        ("cap", ctypes.c_uint32),
+        ("pos", c_double_p),
+        ("vel", c_double_p),
+        ("acc", c_double_p),
+        ("rho", c_double_p),
+        ("rad", c_double_p),
+        ("h", c_double_p),
+        ("m", c_double_p),
+        ("id", c_u32_p),
+        ("frame", ctypes.c_uint32),
+        ("next_id", ctypes.c_uint32),
+        ("has_pending", ctypes.c_uint32),
+        ("pending_half", ctypes.c_double),
+    ]
+
+
 class OrcCells(ctypes.Structure):
     _fields_ = [("start", c_u32_p), ("end", c_u32_p), ("keys", c_u32_p), ("ex", ctypes.c_uint32 * 2)]
 
@@ -179,6 +198,10 @@ def lib():
         L.orc32_kernel_w.argtypes = [ctypes.c_float, ctypes.c_float]
         L.orc32_kernel_w.restype = ctypes.c_float
         L.orc_icosahedron.argtypes = [c_float_p]
+        L.orc64s_step.argtypes = [P(OrcGrid), P(OrcParams), P(OrcRefine), P(OrcState64), P(OrcCells), P(OrcBoundary),
+                                  ctypes.c_double, P(OrcReport)]
+        L.orc64s_step.restype = ctypes.c_int
+        L.orc64s_totals.argtypes = [P(OrcParams), P(OrcState64), c_double_p]
         L.orc_set_threads.argtypes = [ctypes.c_int]
         L.orc_get_threads.restype = ctypes.c_int
         _lib = L
@@ -431,3 +454,40 @@ class OracleSim:
 
     def excluded(self):
         return int(self.cells.ex[0]), int(self.cells.ex[1])
+
+
+class OracleSim64(OracleSim):
+    """The FP64 step: the same state layout and step as OracleSim, held and advanced in double precision throughout
+    (integrate, grid, density, forces, refinement). Created from the same FP32 inputs."""
+
+    def __init__(self, params, positions: np.ndarray, boundary_pos: Optional[np.ndarray] = None,
+                 boundary_psi: Optional[np.ndarray] = None, refinement=None, capacity: Optional[int] = None):
+        super().__init__(params, positions, boundary_pos, boundary_psi, refinement, capacity)
+        n = self.n
+        for k in ("pos", "vel", "acc", "rho", "rad", "h", "m"):
+            setattr(self, k, getattr(self, k).astype(np.float64))
+        self.state = OrcState64(n, self.cap, dptr(self.pos), dptr(self.vel), dptr(self.acc), dptr(self.rho),
+                                dptr(self.rad), dptr(self.h), dptr(self.m), uptr(self.id), 0, n, 0, 0.0)
+
+    def load(self, arrays: dict, frame: int = 0, next_id: Optional[int] = None, pending_half: Optional[float] = None):
+        super().load({k: np.asarray(v, np.float64) if k != "id" else v for k, v in arrays.items()}, frame, next_id,
+                     pending_half)
+
+    def step(self, dt: float) -> bool:
+        self._report_buffers()
+        refined = self.L.orc64s_step(ctypes.byref(self.grid), ctypes.byref(self.P),
+                                     ctypes.byref(self.R) if self.R is not None else None, ctypes.byref(self.state),
+                                     ctypes.byref(self.cells), ctypes.byref(self.boundary), float(dt),
+                                     ctypes.byref(self.report))
+        return bool(refined)
+
+    def totals(self) -> np.ndarray:
+        out = np.zeros(6, np.float64)
+        self.L.orc64s_totals(ctypes.byref(self.P), ctypes.byref(self.state), dptr(out))
+        return out
+
+    def _fp32_only(self, *a, **k):
+        raise NotImplementedError("an FP32-state stage; use OracleSim")
+
+    integrate = grid_build = density32 = density64 = forces32 = forces64 = refine = _fp32_only
+    neighbor_counts = list_entries = sum_kinds = export_velocities = _fp32_only

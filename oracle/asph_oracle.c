@@ -524,13 +524,56 @@ static int sum_kind(const orc_grid* g, const orc_state* s, const orc_cells* c, i
     return n > ORC_ROW_HEAVY ? ORC_DEAL_ENTRY : ORC_DEAL_NONE;
 }
 
+/* selection records of the top-k sorts: (key, id) orders them, ids being unique */
+typedef struct orc_sel {
+    uint64_t key;
+    uint32_t id, slot;
+} orc_sel;
+
+static int cmp_sel(const void* a, const void* b)
+{
+    const orc_sel* x = (const orc_sel*)a;
+    const orc_sel* y = (const orc_sel*)b;
+    if (x->key != y->key) {
+        return x->key < y->key ? -1 : 1;
+    }
+    return x->id < y->id ? -1 : (x->id > y->id ? 1 : 0);
+}
+
+static uint32_t sortable_f(float f)
+{
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+static uint64_t sortable_d(double f)
+{
+    uint64_t u;
+    memcpy(&u, &f, 8);
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+
+static const float ORC_PHI_F = 1.6180339887498949f;
+static const float ORC_INVNORM_F = 0.5257311121f;
+
+/* FP32 canonical arithmetic on the FP32 state (the bit-exact checker) */
 #define REAL float
+#define SREAL float
+#define STATE orc_state
+#define ITPOS(p, tmp) ((void)(tmp), (p))
+#define SUM_KIND(g, s, c, i) sum_kind(g, s, c, i)
 #define F(name) name##_f32
 #define FMA fmaf
 #define SQRT sqrtf
+#define CBRT orc_cbrtf
+#define PI_R ORC_PI_F
+#define SORTABLE(x) ((uint64_t)sortable_f(x))
+#define SORTABLE_DESC(x) ((uint64_t)(uint32_t)~sortable_f(x))
 #define WCOEF (21.0f / (16.0f * ORC_PI_F))
 #define DCOEF (-5.0f * (21.0f / (16.0f * ORC_PI_F)))
 #include "oracle_body.h"
+#include "refine_body.h"
 #undef REAL
 #undef F
 #undef FMA
@@ -539,6 +582,7 @@ static int sum_kind(const orc_grid* g, const orc_state* s, const orc_cells* c, i
 #undef DCOEF
 #undef NBR
 
+/* FP64 arithmetic on the FP32 state (accuracy reference of one stage on the GPU's own inputs) */
 #define REAL double
 #define F(name) name##_f64
 #define FMA fma
@@ -546,10 +590,49 @@ static int sum_kind(const orc_grid* g, const orc_state* s, const orc_cells* c, i
 #define WCOEF (21.0 / (16.0 * 3.14159265358979323846))
 #define DCOEF (-5.0 * (21.0 / (16.0 * 3.14159265358979323846)))
 #include "oracle_body.h"
+#undef NBR
+#undef F
+#undef SREAL
+#undef STATE
+#undef ITPOS
+#undef SUM_KIND
+#undef CBRT
+#undef PI_R
+#undef SORTABLE
+#undef SORTABLE_DESC
+
+/* FP64 arithmetic on the FP64 state: the FP64 step */
+static inline const float* itpos_d64(const double* p, float* tmp)
+{
+    tmp[0] = (float)p[0];
+    tmp[1] = (float)p[1];
+    tmp[2] = (float)p[2];
+    tmp[3] = 0.0f;
+    return tmp;
+}
+#define SREAL double
+#define STATE orc_state64
+#define ITPOS(p, tmp) itpos_d64((p), (tmp))
+#define SUM_KIND(g, s, c, i) ORC_DEAL_NONE
+#define F(name) name##_d64
+#define CBRT cbrt
+#define PI_R 3.14159265358979323846
+#define SORTABLE(x) sortable_d(x)
+#define SORTABLE_DESC(x) (~sortable_d(x))
+#include "oracle_body.h"
+#include "refine_body.h"
 #undef REAL
+#undef SREAL
+#undef STATE
+#undef ITPOS
+#undef SUM_KIND
 #undef F
 #undef FMA
 #undef SQRT
+#undef CBRT
+#undef PI_R
+#undef SORTABLE
+#undef SORTABLE_DESC
 #undef WCOEF
 #undef DCOEF
 #undef NBR
@@ -698,447 +781,12 @@ void orc_totals(const orc_params* P, const orc_state* s, double out[6])
 }
 
 /* ------------------------------------------------------------------ refinement */
-static uint32_t sortable_f(float f)
-{
-    uint32_t u;
-    memcpy(&u, &f, 4);
-    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-}
-
-static int cmp_u64(const void* a, const void* b)
-{
-    const uint64_t x = *(const uint64_t*)a, y = *(const uint64_t*)b;
-    return x < y ? -1 : (x > y ? 1 : 0);
-}
-
-/* checkIfParticleCanBeSplitInsideDomain (cuda/src/simulation/refinement/criteria/Common.cuh:6-20) */
-static int inside_domain(const orc_params* P, const float* p, float h, float eps)
-{
-    const float mo = eps * h;
-    if (p[0] - mo < P->dmin[0] || p[0] + mo > P->dmax[0] || p[1] - mo < P->dmin[1] || p[1] + mo > P->dmax[1] ||
-        p[2] - mo < P->dmin[2] || p[2] + mo > P->dmax[2]) {
-        return 0;
-    }
-    return 1;
-}
-
-/* velocity-gradient sum of VorticityCriterion.cuh:198-229 (search radius h_i); returns |curl v| or -1 when
- * fewer than 4 neighbours qualify */
-static float vorticity_mag(const orc_grid* g, const orc_state* s, const orc_cells* c, uint32_t i)
-{
-    const float* pi = s->pos + 4 * (size_t)i;
-    const float* vi = s->vel + 4 * (size_t)i;
-    const float hi = s->h[i];
-    float invh, wc, dwc;
-    kernel_consts_f32(hi, &invh, &wc, &dwc);
-    float d[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    int valid = 0;
-    orc_iter it;
-    uint32_t jb, je;
-    float sh[3];
-    it_init(&it, g, c->start, c->end, c->ex, pi, hi);
-    while (it_next(&it, &jb, &je, sh)) {
-        for (uint32_t j = jb; j < je; j++) {
-            if (j == i) {
-                continue;
-            }
-            const float* pj = s->pos + 4 * (size_t)j;
-            const float rx = pj[0] - pi[0], ry = pj[1] - pi[1], rz = pj[2] - pi[2];
-            const float dist = sqrtf(fmaf(rz, rz, fmaf(ry, ry, rx * rx)));
-            if (dist < hi && dist > 1e-6f) {
-                const float* vj = s->vel + 4 * (size_t)j;
-                const float vd[3] = {vj[0] - vi[0], vj[1] - vi[1], vj[2] - vi[2]};
-                const float gw = kernel_dw_f32(dist, invh, dwc);
-                const float w = s->m[j] / s->rho[j];
-                const float gd[3] = {rx / dist, ry / dist, rz / dist};
-                for (int a = 0; a < 3; a++) {
-                    for (int bb = 0; bb < 3; bb++) {
-                        d[3 * a + bb] = fmaf((w * vd[a]) * gd[bb], gw, d[3 * a + bb]);
-                    }
-                }
-                valid++;
-            }
-        }
-    }
-    if (valid < 4) {
-        return -1.0f;
-    }
-    /* d[3a+b] = dv_a/dx_b ; omega = (dvz/dy - dvy/dz, dvx/dz - dvz/dx, dvy/dx - dvx/dy) */
-    const float ox = d[7] - d[5], oy = d[2] - d[6], oz = d[3] - d[1];
-    return sqrtf(fmaf(oz, oz, fmaf(oy, oy, ox * ox)));
-}
-
-/* calculateMinSurfaceDistance (InterfaceCriterion.cuh:52-67) */
-static void min_surface_distance(const orc_params* P, const float* p, float out[3])
-{
-    for (int a = 0; a < 3; a++) {
-        const float lo = p[a] - P->dmin[a];
-        const float hi = P->dmax[a] - p[a];
-        const float m = hi < lo ? hi : lo;
-        out[a] = m < 0.0f ? 0.0f : m;
-    }
-}
-
-static float compmin3(const float v[3])
-{
-    float m = v[0];
-    m = v[1] < m ? v[1] : m;
-    m = v[2] < m ? v[2] : m;
-    return m;
-}
-
-/* merge criterion generators: VelocityCriterion.cuh:208-227, InterfaceCriterion.cuh:97-115,
- * VorticityCriterion.cuh:248-312 */
-static float merge_score(const orc_grid* g, const orc_params* P, const orc_refine* R, const orc_state* s,
-                         const orc_cells* c, uint32_t i, float maxMass)
-{
-    if (s->m[i] > maxMass) {
-        return -1.0f;
-    }
-    const float* p = s->pos + 4 * (size_t)i;
-    if (R->criterion == 1u) {
-        float md[3], nd[3];
-        min_surface_distance(P, p, md);
-        for (int a = 0; a < 3; a++) {
-            nd[a] = md[a] / (R->iface_merge * (P->dmax[a] - P->dmin[a]));
-        }
-        return compmin3(nd) - 1.0f;
-    }
-    if (R->criterion == 2u) {
-        const float mag = vorticity_mag(g, s, c, i);
-        if (mag < 0.0f) {
-            return -1.0f;
-        }
-        if (mag < R->vort_merge) {
-            return mag / R->vort_merge;
-        }
-        return -1.0f;
-    }
-    const float* v = s->vel + 4 * (size_t)i;
-    const float sp = sqrtf(fmaf(v[2], v[2], fmaf(v[1], v[1], v[0] * v[0])));
-    if (sp < R->vel_merge) {
-        return sp / R->vel_merge;
-    }
-    return -1.0f;
-}
-
-/* split criterion generators: VelocityCriterion.cuh:180-206, InterfaceCriterion.cuh:69-95,
- * VorticityCriterion.cuh:170-246 */
-static float split_score(const orc_grid* g, const orc_params* P, const orc_refine* R, const orc_state* s,
-                         const orc_cells* c, uint32_t i, float minMass)
-{
-    if (s->m[i] < minMass) {
-        return -1.0f;
-    }
-    const float* p = s->pos + 4 * (size_t)i;
-    const float h = s->h[i];
-    if (R->criterion == 1u) {
-        float md[3], nd[3];
-        min_surface_distance(P, p, md);
-        if (compmin3(md) < R->eps * h) {
-            return -1.0f;
-        }
-        for (int a = 0; a < 3; a++) {
-            nd[a] = md[a] / (R->iface_split * (P->dmax[a] - P->dmin[a]));
-        }
-        return 1.0f - compmin3(nd);
-    }
-    if (!inside_domain(P, p, h, R->eps)) {
-        return -1.0f;
-    }
-    if (R->criterion == 2u) {
-        const float mag = vorticity_mag(g, s, c, i);
-        if (mag < 0.0f) {
-            return -1.0f;
-        }
-        return mag > R->vort_split ? mag : -1.0f;
-    }
-    const float* v = s->vel + 4 * (size_t)i;
-    const float sp = sqrtf(fmaf(v[2], v[2], fmaf(v[1], v[1], v[0] * v[0])));
-    if (sp < R->vel_split) {
-        return -1.0f;
-    }
-    return sp;
-}
-
-/* identifyMergeCandidates (cuda/src/algorithm/AdaptiveAlgorithm.cu:159-206): nearest neighbour with
- * r^2 < min(h_i,h_j)^2 and m_j < maxMass within the cells of [x - h_i, x + h_i]. Exact r^2 ties go to the
- * smaller id (the reference keeps the first one its loop meets). */
-static uint32_t merge_candidate(const orc_grid* g, const orc_state* s, const orc_cells* c, uint32_t e,
-                                float maxMass)
-{
-    const float* pe = s->pos + 4 * (size_t)e;
-    const float he = s->h[e];
-    float best = 3.402823466e38f;
-    uint32_t bj = ORC_NONE;
-    orc_iter it;
-    uint32_t jb, je;
-    float sh[3];
-    it_init(&it, g, c->start, c->end, c->ex, pe, he);
-    while (it_next(&it, &jb, &je, sh)) {
-        for (uint32_t j = jb; j < je; j++) {
-            if (j == e) {
-                continue;
-            }
-            const float* pj = s->pos + 4 * (size_t)j;
-            const float dx = pj[0] - pe[0], dy = pj[1] - pe[1], dz = pj[2] - pe[2];
-            const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-            const float hj = s->h[j];
-            const float hm = hj < he ? hj : he;
-            if (r2 < hm * hm && s->m[j] < maxMass) {
-                if (r2 < best || (r2 == best && s->id[j] < s->id[bj])) {
-                    best = r2;
-                    bj = j;
-                }
-            }
-        }
-    }
-    return bj;
-}
-
-static const float ORC_PHI_F = 1.6180339887498949f;
-static const float ORC_INVNORM_F = 0.5257311121f;
-
-/* icosahedronVertices (cuda/src/algorithm/AdaptiveAlgorithm.cu:35-48), same order */
-static void icosahedron(float v[12][3])
-{
-    const float A = ORC_PHI_F * ORC_INVNORM_F, B = ORC_INVNORM_F;
-    const float t[12][3] = {{0.0f, A, B},  {0.0f, A, -B},  {0.0f, -A, -B}, {0.0f, -A, B},
-                            {B, 0.0f, A},  {-B, 0.0f, A},  {B, 0.0f, -A},  {-B, 0.0f, -A},
-                            {A, B, 0.0f},  {A, -B, 0.0f},  {-A, B, 0.0f},  {-A, -B, 0.0f}};
-    memcpy(v, t, sizeof(t));
-}
-
-/* performMerges + calculateMergedSmoothingLength (cuda/src/algorithm/AdaptiveAlgorithm.cu:50-67, 236-275) */
-static void merge_pair(const orc_params* P, orc_state* s, uint32_t i, uint32_t c)
-{
-    const float m1 = s->m[i], m2 = s->m[c];
-    const float M = m1 + m2;
-    float np[3], nv[3], na[3];
-    for (int a = 0; a < 3; a++) {
-        np[a] = fmaf(m1, s->pos[4 * (size_t)i + a], m2 * s->pos[4 * (size_t)c + a]) / M;
-        nv[a] = fmaf(m1, s->vel[4 * (size_t)i + a], m2 * s->vel[4 * (size_t)c + a]) / M;
-        na[a] = fmaf(m1, s->acc[4 * (size_t)i + a], m2 * s->acc[4 * (size_t)c + a]) / M;
-    }
-    float d[2], W[2];
-    const uint32_t idx[2] = {i, c};
-    for (int k = 0; k < 2; k++) {
-        const float* p = s->pos + 4 * (size_t)idx[k];
-        const float dx = p[0] - np[0], dy = p[1] - np[1], dz = p[2] - np[2];
-        d[k] = sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
-        float invh, wc, dwc;
-        kernel_consts_f32(s->h[idx[k]], &invh, &wc, &dwc);
-        W[k] = kernel_w_f32(d[k], invh, wc);
-    }
-    const float denom = fmaf(m1, W[0], m2 * W[1]);
-    const float coef = (16.0f * ORC_PI_F) / 21.0f;
-    const float hn = orc_cbrtf((coef * M) / denom);
-    const float rn = P->r0 * orc_cbrtf(M / P->m0);
-    for (int a = 0; a < 3; a++) {
-        s->pos[4 * (size_t)i + a] = np[a];
-        s->vel[4 * (size_t)i + a] = nv[a];
-        s->acc[4 * (size_t)i + a] = na[a];
-    }
-    s->pos[4 * (size_t)i + 3] = 0.0f;
-    s->vel[4 * (size_t)i + 3] = 0.0f;
-    s->acc[4 * (size_t)i + 3] = 0.0f;
-    s->m[i] = M;
-    s->rad[i] = rn;
-    s->h[i] = hn;
-    s->rho[i] = 0.0f;
-}
-
-/* splitParticles (cuda/src/algorithm/AdaptiveAlgorithm.cu:69-117) with daughters at base .. base+11 */
-static void split_one(const orc_refine* R, orc_state* s, uint32_t p, uint32_t base, uint32_t base_id)
-{
-    float ico[12][3];
-    icosahedron(ico);
-    const float m = s->m[p], r = s->rad[p], h = s->h[p];
-    const float dm = m * R->vertex_ratio, cm = m * R->center_ratio;
-    const float nr = r * orc_cbrtf(dm / m);
-    const float nh = R->alpha * h;
-    float x[4], v[4], a[4];
-    memcpy(x, s->pos + 4 * (size_t)p, sizeof(x));
-    memcpy(v, s->vel + 4 * (size_t)p, sizeof(v));
-    memcpy(a, s->acc + 4 * (size_t)p, sizeof(a));
-    s->m[p] = cm;
-    s->rad[p] = r * orc_cbrtf(cm / m);
-    s->h[p] = nh;
-    for (uint32_t k = 0; k < 12; k++) {
-        const size_t q = base + k;
-        for (int c = 0; c < 3; c++) {
-            s->pos[4 * q + c] = x[c] + (ico[k][c] * R->eps) * h;
-        }
-        s->pos[4 * q + 3] = x[3];
-        memcpy(s->vel + 4 * q, v, sizeof(v));
-        memcpy(s->acc + 4 * q, a, sizeof(a));
-        s->m[q] = dm;
-        s->rad[q] = nr;
-        s->h[q] = nh;
-        s->rho[q] = 0.0f;
-        s->id[q] = base_id + k;
-    }
-}
-
-/* One refinement pass: performAdaptiveRefinement (cuda/src/simulation/AdaptiveSphSimulation.cu:102-113) with
- * identifyAndMergeParticles (:195-252) then, if particles were removed, identifyAndSplitParticles (:135-193).
- * Selection follows findTopParticlesToMerge/ToSplit (AdaptiveAlgorithm.cuh:56-131): stable sort of
- * (score, array slot) ascending for merge, descending for split; k = min(#score > 0, round(N*maxBatchRatio)).
- * Merge: non-eligible particles keep the reset candidate value 0, i.e. the particle in slot 0; pairs are
- * mutual candidates, the lower slot keeps. Split: the device count k bounds the kernel while the launch covers
- * ceil(budget/threadsPerBlock) blocks, budget = min(k, removed/12). Daughters are appended in split order. */
+/* One refinement pass: performAdaptiveRefinement (cuda/src/simulation/AdaptiveSphSimulation.cu:102-113), the body
+ * in refine_body.h, on the FP32 state in the canonical FP32 arithmetic */
 void orc32_refine(const orc_grid* g, const orc_params* P, const orc_refine* R, orc_state* s, orc_cells* c,
                   orc_report* rep)
 {
-    orc_report local;
-    if (rep == NULL) {
-        memset(&local, 0, sizeof(local));
-        rep = &local;
-    }
-    const uint32_t n = s->n;
-    rep->frame = s->frame;
-    rep->count_before = n;
-    rep->merge_eligible = rep->merge_pairs = rep->removed = 0;
-    rep->split_candidates = rep->split_budget = rep->splits = 0;
-    rep->capacity_hit = 0;
-    rep->count_after = n;
-    if (n <= 1) {
-        return;
-    }
-    const float minMass = R->min_mass_ratio * P->m0;
-    const float maxMass = R->max_mass_ratio * P->m0;
-    float* score = (float*)malloc(sizeof(float) * n);
-    uint32_t* cand = (uint32_t*)malloc(sizeof(uint32_t) * n);
-    uint8_t* flag = (uint8_t*)calloc(n, 1);
-
-    uint32_t cpos = 0;
-    for (uint32_t i = 0; i < n; i++) {
-        score[i] = merge_score(g, P, R, s, c, i, maxMass);
-        cpos += score[i] > 0.0f;
-    }
-    const uint32_t lim = (uint32_t)roundf((float)n * R->max_batch_ratio);
-    const uint32_t k = cpos < lim ? cpos : lim;
-    rep->merge_eligible = k;
-    uint32_t pairs = 0;
-    if (k > 0) {
-        /* (score, slot) ascending; ids are unique, so (sortable score, id) is a total order */
-        uint32_t* sel = (uint32_t*)malloc(sizeof(uint32_t) * n);
-        {
-            uint64_t* tmp = (uint64_t*)malloc(sizeof(uint64_t) * n * 2);
-            for (uint32_t i = 0; i < n; i++) {
-                tmp[2 * i] = ((uint64_t)sortable_f(score[i]) << 32) | s->id[i];
-                tmp[2 * i + 1] = i;
-            }
-            qsort(tmp, n, sizeof(uint64_t) * 2, cmp_u64);
-            for (uint32_t i = 0; i < n; i++) {
-                sel[i] = (uint32_t)tmp[2 * i + 1];
-            }
-            free(tmp);
-        }
-        uint32_t slot0 = 0;
-        for (uint32_t i = 1; i < n; i++) {
-            if (s->id[i] < s->id[slot0]) {
-                slot0 = i;
-            }
-        }
-        for (uint32_t i = 0; i < n; i++) {
-            cand[i] = slot0;
-        }
-        for (uint32_t q = 0; q < k; q++) {
-            const uint32_t e = sel[q];
-            cand[e] = merge_candidate(g, s, c, e, maxMass);
-        }
-        free(sel);
-        for (uint32_t i = 0; i < n; i++) {
-            const uint32_t cc = cand[i];
-            if (cc == ORC_NONE) {
-                continue;
-            }
-            if (cand[cc] == i && s->id[i] < s->id[cc]) {
-                if (rep->keep_ids) {
-                    rep->keep_ids[pairs] = s->id[i];
-                }
-                if (rep->removed_ids) {
-                    rep->removed_ids[pairs] = s->id[cc];
-                }
-                merge_pair(P, s, i, cc);
-                flag[cc] = 1;
-                pairs++;
-            }
-        }
-    }
-    rep->merge_pairs = pairs;
-    if (pairs > 0) {
-        /* stable compaction (compactParticles, AdaptiveAlgorithm.cu:130-157, done out of place) */
-        uint32_t w = 0;
-        for (uint32_t i = 0; i < n; i++) {
-            if (flag[i]) {
-                continue;
-            }
-            if (w != i) {
-                memcpy(s->pos + 4 * (size_t)w, s->pos + 4 * (size_t)i, 16);
-                memcpy(s->vel + 4 * (size_t)w, s->vel + 4 * (size_t)i, 16);
-                memcpy(s->acc + 4 * (size_t)w, s->acc + 4 * (size_t)i, 16);
-                s->rho[w] = s->rho[i];
-                s->rad[w] = s->rad[i];
-                s->h[w] = s->h[i];
-                s->m[w] = s->m[i];
-                s->id[w] = s->id[i];
-                c->keys[w] = c->keys[i];
-            }
-            w++;
-        }
-        const uint32_t removed = n - w;
-        rep->removed = removed;
-        s->n = w;
-        const uint32_t n2 = w;
-        if (R->criterion == 2u) {
-            orc_cells_from_keys(g, n2, c->keys, c->start, c->end);
-        }
-        uint32_t cs = 0;
-        for (uint32_t i = 0; i < n2; i++) {
-            score[i] = split_score(g, P, R, s, c, i, minMass);
-            cs += score[i] > 0.0f;
-        }
-        const uint32_t lim2 = (uint32_t)roundf((float)n2 * R->max_batch_ratio);
-        const uint32_t ks = cs < lim2 ? cs : lim2;
-        rep->split_candidates = ks;
-        const uint32_t budget = ks < removed / 12u ? ks : removed / 12u;
-        rep->split_budget = budget;
-        if (budget > 0) {
-            const uint32_t tpb = P->threads_per_block ? P->threads_per_block : 256u;
-            uint64_t launched = (uint64_t)((budget + tpb - 1) / tpb) * tpb;
-            const uint32_t M = (uint64_t)ks < launched ? ks : (uint32_t)launched;
-            uint64_t* tmp = (uint64_t*)malloc(sizeof(uint64_t) * n2 * 2);
-            for (uint32_t i = 0; i < n2; i++) {
-                tmp[2 * i] = ((uint64_t)(~sortable_f(score[i])) << 32) | s->id[i];
-                tmp[2 * i + 1] = i;
-            }
-            qsort(tmp, n2, sizeof(uint64_t) * 2, cmp_u64);
-            uint32_t done = 0;
-            for (uint32_t r = 0; r < M; r++) {
-                const uint64_t end = (uint64_t)n2 + 12ull * (r + 1);
-                if (end > s->cap) {
-                    rep->capacity_hit = 1;
-                    break;
-                }
-                const uint32_t p = (uint32_t)tmp[2 * r + 1];
-                if (rep->split_ids) {
-                    rep->split_ids[r] = s->id[p];
-                }
-                split_one(R, s, p, n2 + 12u * r, s->next_id + 12u * r);
-                done++;
-            }
-            free(tmp);
-            rep->splits = done;
-            s->n = n2 + 12u * done;
-            s->next_id += 12u * done;
-        }
-    }
-    rep->count_after = s->n;
-    free(score);
-    free(cand);
-    free(flag);
+    refine_impl_f32(g, P, R, s, c, rep);
 }
 
 int orc32_step(const orc_grid* g, const orc_params* P, const orc_refine* R, orc_state* s, orc_cells* c,
@@ -1160,6 +808,170 @@ int orc32_step(const orc_grid* g, const orc_params* P, const orc_refine* R, orc_
     s->has_pending = 1;
     s->frame++;
     return refined;
+}
+
+/* ------------------------------------------------------------------ the FP64 step */
+/* The same step as orc32_step on an FP64 state in double arithmetic throughout: integrate, grid, density,
+ * forces, refinement (SphSimulation.cu:101-120, AdaptiveSphSimulation.cu:59-85). The grid's cell keys are taken
+ * from the positions rounded to float (cells are an acceleration structure: any key of a cell containing the
+ * particle visits the same candidates up to the clamp at the box edge). */
+static void kick64(double* v, const double* a, double hdt, double maxv)
+{
+    v[0] = fma(a[0], hdt, v[0]);
+    v[1] = fma(a[1], hdt, v[1]);
+    v[2] = fma(a[2], hdt, v[2]);
+    const double len = sqrt(fma(v[2], v[2], fma(v[1], v[1], v[0] * v[0])));
+    if (len > maxv) {
+        const double sc = maxv / len;
+        v[0] = v[0] * sc;
+        v[1] = v[1] * sc;
+        v[2] = v[2] * sc;
+    }
+}
+
+void orc64s_integrate(orc_state64* s, const orc_params* P, double dt)
+{
+    const double half = dt / 2.0;
+    const int64_t n = s->n;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; i++) {
+        double* v = s->vel + 4 * i;
+        const double* a = s->acc + 4 * i;
+        double* x = s->pos + 4 * i;
+        if (s->has_pending) {
+            kick64(v, a, s->pending_half, P->max_velocity);
+        }
+        kick64(v, a, half, P->max_velocity);
+        v[3] = 0.0;
+        for (int c = 0; c < 3; c++) {
+            double xc = fma(v[c], dt, x[c]);
+            if (!P->periodic) {
+                xc = xc < P->dmin[c] ? P->dmin[c] : xc;
+                xc = xc > P->dmax[c] ? P->dmax[c] : xc;
+            } else {
+                const double L = (double)P->dmax[c] - (double)P->dmin[c];
+                if (xc < P->dmin[c]) {
+                    xc = xc + L;
+                } else if (xc >= P->dmax[c]) {
+                    xc = xc - L;
+                }
+            }
+            x[c] = xc;
+        }
+    }
+    s->has_pending = 0;
+}
+
+static void permute_d(double* a, const uint32_t* perm, uint32_t n, int width, double* tmp)
+{
+    for (uint32_t k = 0; k < n; k++) {
+        memcpy(tmp + (size_t)width * k, a + (size_t)width * perm[k], sizeof(double) * width);
+    }
+    memcpy(a, tmp, sizeof(double) * width * n);
+}
+
+void orc64s_grid_build(const orc_grid* g, orc_state64* s, orc_cells* c)
+{
+    const uint32_t n = s->n;
+    const size_t nn = n ? n : 1;
+    uint32_t* keys = (uint32_t*)malloc(sizeof(uint32_t) * nn);
+    uint32_t* refk = (uint32_t*)malloc(sizeof(uint32_t) * nn);
+    uint32_t* perm = (uint32_t*)malloc(sizeof(uint32_t) * nn);
+    double* tmp = (double*)malloc(sizeof(double) * 4 * nn);
+    for (uint32_t i = 0; i < n; i++) {
+        float pf[4];
+        orc_cell_of(g, itpos_d64(s->pos + 4 * (size_t)i, pf), &keys[i], &refk[i], NULL);
+    }
+    if (!g->periodic) {
+        orc_excluded_cells(n, refk, s->id, c->ex);
+    } else {
+        c->ex[0] = c->ex[1] = ORC_NONE;
+    }
+    orc_sort_stable(n, keys, 3 * g->bits, perm);
+    permute_d(s->pos, perm, n, 4, tmp);
+    permute_d(s->vel, perm, n, 4, tmp);
+    permute_d(s->acc, perm, n, 4, tmp);
+    permute_d(s->rho, perm, n, 1, tmp);
+    permute_d(s->rad, perm, n, 1, tmp);
+    permute_d(s->h, perm, n, 1, tmp);
+    permute_d(s->m, perm, n, 1, tmp);
+    {
+        uint32_t* t = (uint32_t*)tmp;
+        for (uint32_t k = 0; k < n; k++) {
+            t[k] = s->id[perm[k]];
+        }
+        memcpy(s->id, t, sizeof(uint32_t) * n);
+    }
+    for (uint32_t k = 0; k < n; k++) {
+        c->keys[k] = keys[perm[k]];
+    }
+    orc_cells_from_keys(g, n, c->keys, c->start, c->end);
+    free(keys);
+    free(refk);
+    free(perm);
+    free(tmp);
+}
+
+void orc64s_density(const orc_grid* g, const orc_params* P, const orc_state64* s, const orc_cells* c,
+                    const orc_boundary* b, double* rho_out)
+{
+    orc_density_impl_d64(g, P, s, c, b, rho_out);
+}
+
+void orc64s_forces(const orc_grid* g, const orc_params* P, const orc_state64* s, const orc_cells* c,
+                   const orc_boundary* b, double* acc_out)
+{
+    orc_forces_impl_d64(g, P, s, c, b, s->rho, acc_out, NULL);
+}
+
+void orc64s_refine(const orc_grid* g, const orc_params* P, const orc_refine* R, orc_state64* s, orc_cells* c,
+                   orc_report* rep)
+{
+    refine_impl_d64(g, P, R, s, c, rep);
+}
+
+int orc64s_step(const orc_grid* g, const orc_params* P, const orc_refine* R, orc_state64* s, orc_cells* c,
+                const orc_boundary* b, double dt, orc_report* rep)
+{
+    orc64s_integrate(s, P, dt);
+    orc64s_grid_build(g, s, c);
+    orc64s_density(g, P, s, c, b, s->rho);
+    orc64s_forces(g, P, s, c, b, s->acc);
+    int refined = 0;
+    if (R != NULL && R->enabled && R->cooldown > 0) {
+        const uint32_t f = s->frame;
+        if (f == R->initial_cooldown || (f > R->initial_cooldown && f % R->cooldown == 0)) {
+            orc64s_refine(g, P, R, s, c, rep);
+            refined = 1;
+        }
+    }
+    s->pending_half = dt / 2.0;
+    s->has_pending = 1;
+    s->frame++;
+    return refined;
+}
+
+void orc64s_totals(const orc_params* P, const orc_state64* s, double out[6])
+{
+    double M = 0, px = 0, py = 0, pz = 0, ke = 0;
+    for (uint32_t i = 0; i < s->n; i++) {
+        double v[4] = {s->vel[4 * i], s->vel[4 * i + 1], s->vel[4 * i + 2], 0.0};
+        if (s->has_pending) {
+            kick64(v, s->acc + 4 * (size_t)i, s->pending_half, P->max_velocity);
+        }
+        const double m = s->m[i];
+        M += m;
+        px += m * v[0];
+        py += m * v[1];
+        pz += m * v[2];
+        ke += 0.5 * m * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    }
+    out[0] = M;
+    out[1] = px;
+    out[2] = py;
+    out[3] = pz;
+    out[4] = ke;
+    out[5] = (double)s->n;
 }
 
 /* ------------------------------------------------------------------ boundary generation */
@@ -1340,7 +1152,7 @@ float orc32_kernel_w(float r, float h)
 void orc_icosahedron(float* out36)
 {
     float v[12][3];
-    icosahedron(v);
+    icosahedron_f32(v);
     memcpy(out36, v, sizeof(v));
 }
 

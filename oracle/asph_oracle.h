@@ -141,6 +141,29 @@ void orc64_density(const orc_grid* g, const orc_params* P, const orc_state* s, c
 void orc64_forces(const orc_grid* g, const orc_params* P, const orc_state* s, const orc_cells* c,
                   const orc_boundary* b, double* acc_out, double* scale_out);
 
+/* The FP64 step: an FP64 state (same layout and order as orc_state, double arrays) advanced in double arithmetic
+ * throughout (integrate, grid, density, forces, refinement), the CPU step the FP32 pipeline is measured against. */
+typedef struct orc_state64 {
+    uint32_t n, cap;
+    double *pos, *vel, *acc; /* 4 * cap */
+    double *rho, *rad, *h, *m;
+    uint32_t* id;
+    uint32_t frame, next_id, has_pending;
+    double pending_half;
+} orc_state64;
+
+void orc64s_integrate(orc_state64* s, const orc_params* P, double dt);
+void orc64s_grid_build(const orc_grid* g, orc_state64* s, orc_cells* c);
+void orc64s_density(const orc_grid* g, const orc_params* P, const orc_state64* s, const orc_cells* c,
+                    const orc_boundary* b, double* rho_out);
+void orc64s_forces(const orc_grid* g, const orc_params* P, const orc_state64* s, const orc_cells* c,
+                   const orc_boundary* b, double* acc_out);
+void orc64s_refine(const orc_grid* g, const orc_params* P, const orc_refine* R, orc_state64* s, orc_cells* c,
+                   orc_report* rep);
+int orc64s_step(const orc_grid* g, const orc_params* P, const orc_refine* R, orc_state64* s, orc_cells* c,
+                const orc_boundary* b, double dt, orc_report* rep);
+void orc64s_totals(const orc_params* P, const orc_state64* s, double out[6]);
+
 /* Wendland kernel W(r, h) and dW/dr (WendlandKernel.cuh:39-84) in both precisions; the 12 split directions
  * (AdaptiveAlgorithm.cu:35-48) as 12 xyz triples */
 double orc64_kernel_w(double r, double h);

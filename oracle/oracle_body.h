@@ -1,7 +1,10 @@
 /*
  * oracle_body.h — precision-generic part of the oracle (TEST INFRASTRUCTURE ONLY, see asph_oracle.h).
- * Included twice by asph_oracle.c: with REAL=float (FP32 canonical mirror, suffix 32) and REAL=double
- * (FP64 restatement, suffix 64). Requires: REAL, F(name), FMA, SQRT, WCOEF, DCOEF.
+ * Included three times by asph_oracle.c: REAL=float on the FP32 state (the canonical mirror, suffix f32),
+ * REAL=double on the FP32 state (FP64 arithmetic on the GPU's inputs, suffix f64) and REAL=double on the FP64 state
+ * of the FP64 step (suffix d64). Requires: REAL, F(name), FMA, SQRT, WCOEF, DCOEF; STATE and SREAL (the state struct
+ * and its element type), ITPOS(p, tmp) (a float pointer to the position p for the cell iterator) and
+ * SUM_KIND(g, s, c, i) (how a particle's sums are dealt to lanes; always sequential on the FP64 state).
  *
  * Formulas (reference file:line):
  *   Wendland C2 kernel and derivative ........ cuda/src/algorithm/WendlandKernel.cuh:39-52, 69-84
@@ -99,12 +102,13 @@ static REAL F(butterfly)(REAL* s)
  * of up to 32 (the blocks of the neighbour-list row, see list_entries). deal = ORC_DEAL_SUBCELL: the box's sub-cell
  * t goes to lane t mod lanes; ORC_DEAL_ENTRY: the e-th block holding an accepted neighbour (row entry e) goes to
  * lane e mod lanes; lanes = 1 is the sequential sum. */
-static void F(density_fluid)(const orc_grid* g, const orc_state* s, const orc_cells* c, int64_t i, int deal,
+static void F(density_fluid)(const orc_grid* g, const STATE* s, const orc_cells* c, int64_t i, int deal,
                              int lanes, REAL* out)
 {
-    const float* pi = s->pos + 4 * i;
+    const SREAL* pi = s->pos + 4 * i;
     const REAL xi = pi[0], yi = pi[1], zi = pi[2];
-    const float R = s->h[i] + s->h[i];
+    const float R = (float)(s->h[i] + s->h[i]);
+    float pif[4];
     for (int l = 0; l < lanes; l++) {
         out[l] = 0;
     }
@@ -112,14 +116,14 @@ static void F(density_fluid)(const orc_grid* g, const orc_state* s, const orc_ce
     orc_iter it;
     uint32_t jb, je;
     float sh[3];
-    it_init(&it, g, c->start, c->end, c->ex, pi, R);
+    it_init(&it, g, c->start, c->end, c->ex, ITPOS(pi, pif), R);
     while (it_next(&it, &jb, &je, sh)) {
         for (uint32_t blk0 = jb; blk0 < je; blk0 += 32) {
             const uint32_t blk1 = je - blk0 < 32u ? je : blk0 + 32u;
             REAL* rho = out + (deal == ORC_DEAL_ENTRY ? e : it.t) % (uint32_t)lanes;
             int any = 0;
             for (uint32_t j = blk0; j < blk1; j++) {
-                const float* pj = s->pos + 4 * (size_t)j;
+                const SREAL* pj = s->pos + 4 * (size_t)j;
                 const REAL dx = NBR(pj, 0) - xi;
                 const REAL dy = NBR(pj, 1) - yi;
                 const REAL dz = NBR(pj, 2) - zi;
@@ -142,7 +146,7 @@ static void F(density_fluid)(const orc_grid* g, const orc_state* s, const orc_ce
 
 /* boundary part of the density into out[lanes]: member k of each boundary cell (counted from its first member) on
  * lane k mod lanes */
-static void F(density_boundary)(const orc_grid* g, const orc_state* s, const orc_boundary* b, int64_t i,
+static void F(density_boundary)(const orc_grid* g, const STATE* s, const orc_boundary* b, int64_t i,
                                 int lanes, REAL* out)
 {
     for (int l = 0; l < lanes; l++) {
@@ -151,10 +155,11 @@ static void F(density_boundary)(const orc_grid* g, const orc_state* s, const orc
     if (b == NULL || b->n == 0) {
         return;
     }
-    const float* pi = s->pos + 4 * i;
+    const SREAL* pi = s->pos + 4 * i;
     const REAL xi = pi[0], yi = pi[1], zi = pi[2];
     const REAL hi = s->h[i];
-    const float R = s->h[i] + s->h[i];
+    const float R = (float)(s->h[i] + s->h[i]);
+    float pif[4];
     REAL invh, wc, dwc;
     F(kernel_consts)(hi, &invh, &wc, &dwc);
     const REAL twoh = hi + hi;
@@ -162,7 +167,7 @@ static void F(density_boundary)(const orc_grid* g, const orc_state* s, const orc
     orc_iter it;
     uint32_t jb, je;
     float sh[3];
-    it_init(&it, g, b->start, b->end, b->ex, pi, R);
+    it_init(&it, g, b->start, b->end, b->ex, ITPOS(pi, pif), R);
     while (it_next(&it, &jb, &je, sh)) {
         for (uint32_t k = jb; k < je; k++) {
             REAL* rb = out + (k - jb) % (uint32_t)lanes;
@@ -180,7 +185,7 @@ static void F(density_boundary)(const orc_grid* g, const orc_state* s, const orc
     }
 }
 
-void F(orc_density_impl)(const orc_grid* g, const orc_params* P, const orc_state* s, const orc_cells* c,
+void F(orc_density_impl)(const orc_grid* g, const orc_params* P, const STATE* s, const orc_cells* c,
                          const orc_boundary* b, REAL* rho_out)
 {
     (void)P;
@@ -188,7 +193,7 @@ void F(orc_density_impl)(const orc_grid* g, const orc_params* P, const orc_state
 #pragma omp parallel for schedule(dynamic, 256)
     for (int64_t i = 0; i < n; i++) {
         REAL rho, rb;
-        const int deal = sum_kind(g, s, c, i);
+        const int deal = SUM_KIND(g, s, c, i);
         if (deal != ORC_DEAL_NONE) {
             REAL pf[ORC_LANES], pb[ORC_LANES];
             F(density_fluid)(g, s, c, i, deal, ORC_LANES, pf);
@@ -211,16 +216,16 @@ typedef struct F(facc) {
 
 /* force terms of particle i into fl[lanes], the fluid blocks dealt as in density_fluid, boundary member k of each
  * boundary cell on lane k mod lanes */
-static void F(forces_part)(const orc_grid* g, const orc_params* P, const orc_state* s, const orc_cells* c,
-                           const orc_boundary* b, const float* rho_in, int64_t i, int deal, int lanes, F(facc) * fl)
+static void F(forces_part)(const orc_grid* g, const orc_params* P, const STATE* s, const orc_cells* c,
+                           const orc_boundary* b, const SREAL* rho_in, int64_t i, int deal, int lanes, F(facc) * fl)
 {
     const REAL rho0 = P->rho0, c0 = P->c0;
     const REAL alpha = P->alpha, nu_k = P->nu;
     const int morris = P->viscosity_model == 1u;
     const int visc_on = morris ? (P->nu != 0.0f) : (P->alpha != 0.0f);
     const int sigma_on = P->sigma != 0.0f;
-    const float* pi = s->pos + 4 * i;
-    const float* vi4 = s->vel + 4 * i;
+    const SREAL* pi = s->pos + 4 * i;
+    const SREAL* vi4 = s->vel + 4 * i;
     const REAL xi = pi[0], yi = pi[1], zi = pi[2];
     const REAL vxi = vi4[0], vyi = vi4[1], vzi = vi4[2];
     const REAL hi = s->h[i], mi = s->m[i];
@@ -228,13 +233,14 @@ static void F(forces_part)(const orc_grid* g, const orc_params* P, const orc_sta
     const REAL pti = F(pressure_term)(rhoi, rho0, c0);
     const REAL Ki = (((REAL)2 * alpha) * hi) * c0;
     const REAL ei = ((REAL)0.01 * hi) * hi;
-    const float R = s->h[i] + s->h[i];
+    const float R = (float)(s->h[i] + s->h[i]);
+    float pif[4];
     memset(fl, 0, sizeof(*fl) * (size_t)lanes);
     uint32_t e = 0;
     orc_iter it;
     uint32_t jb, je;
     float sh[3];
-    it_init(&it, g, c->start, c->end, c->ex, pi, R);
+    it_init(&it, g, c->start, c->end, c->ex, ITPOS(pi, pif), R);
     while (it_next(&it, &jb, &je, sh)) {
         for (uint32_t blk0 = jb; blk0 < je; blk0 += 32) {
             const uint32_t blk1 = je - blk0 < 32u ? je : blk0 + 32u;
@@ -245,7 +251,7 @@ static void F(forces_part)(const orc_grid* g, const orc_params* P, const orc_sta
                     any = 1; /* the particle itself is accepted (its row holds it) but adds no force */
                     continue;
                 }
-                const float* pj = s->pos + 4 * (size_t)j;
+                const SREAL* pj = s->pos + 4 * (size_t)j;
                 const REAL dx = xi - NBR(pj, 0);
                 const REAL dy = yi - NBR(pj, 1);
                 const REAL dz = zi - NBR(pj, 2);
@@ -282,7 +288,7 @@ static void F(forces_part)(const orc_grid* g, const orc_params* P, const orc_sta
                     f->scale += fabs((double)sp);
                 }
                 if (visc_on) {
-                    const float* vj4 = s->vel + 4 * (size_t)j;
+                    const SREAL* vj4 = s->vel + 4 * (size_t)j;
                     const REAL vd[3] = {vxi - (REAL)vj4[0], vyi - (REAL)vj4[1], vzi - (REAL)vj4[2]};
                     if (!morris) {
                         const REAL comp = FMA(vd[2], dz, FMA(vd[1], dy, vd[0] * dx));
@@ -321,7 +327,7 @@ static void F(forces_part)(const orc_grid* g, const orc_params* P, const orc_sta
         F(kernel_consts)(hi, &invh, &wc, &dwc);
         const REAL twoh = hi + hi;
         const REAL cut = twoh * twoh;
-        it_init(&it, g, b->start, b->end, b->ex, pi, R);
+        it_init(&it, g, b->start, b->end, b->ex, ITPOS(pi, pif), R);
         while (it_next(&it, &jb, &je, sh)) {
             for (uint32_t k = jb; k < je; k++) {
                 F(facc)* f = fl + (k - jb) % (uint32_t)lanes;
@@ -368,8 +374,8 @@ static void F(forces_part)(const orc_grid* g, const orc_params* P, const orc_sta
 }
 
 /* Force pass. rho: densities of the state (FP32 values, as the GPU holds them). */
-void F(orc_forces_impl)(const orc_grid* g, const orc_params* P, const orc_state* s, const orc_cells* c,
-                        const orc_boundary* b, const float* rho_in, REAL* acc_out, double* scale_out)
+void F(orc_forces_impl)(const orc_grid* g, const orc_params* P, const STATE* s, const orc_cells* c,
+                        const orc_boundary* b, const SREAL* rho_in, REAL* acc_out, double* scale_out)
 {
     const int64_t n = s->n;
     const int morris = P->viscosity_model == 1u;
@@ -378,7 +384,7 @@ void F(orc_forces_impl)(const orc_grid* g, const orc_params* P, const orc_state*
 #pragma omp parallel for schedule(dynamic, 256)
     for (int64_t i = 0; i < n; i++) {
         F(facc) f;
-        const int deal = sum_kind(g, s, c, i);
+        const int deal = SUM_KIND(g, s, c, i);
         if (deal != ORC_DEAL_NONE) {
             F(facc) part[ORC_LANES];
             F(forces_part)(g, P, s, c, b, rho_in, i, deal, ORC_LANES, part);

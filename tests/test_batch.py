@@ -47,3 +47,106 @@ def test_batch_matches_oracle():
         for _ in range(20):
             orc.step(sc.dt)
         assert_state_bitexact(sim.read_state(), orc.arrays())
+
+
+def _sim(sc):
+    from adaptivesph_gb300 import create_simulation
+    from helpers import boundary_of
+
+    bd = boundary_of(sc)
+    cap = sc.refinement.max_particle_count if sc.refinement else sc.positions.shape[0]
+    return create_simulation(sc.parameters, sc.positions, None, None, bd, sc.refinement, cap,
+                             max(bd.get_particle_count(), 1))
+
+
+def _oracle(sc):
+    import oracle
+    from helpers import boundary_of
+
+    bd = boundary_of(sc)
+    cap = sc.refinement.max_particle_count if sc.refinement else sc.positions.shape[0]
+    return oracle.OracleSim(sc.parameters, sc.positions, bd.positions, bd.psi, sc.refinement, capacity=cap)
+
+
+def _mix_slice():
+    """28 scenes of the 256-scene mix (counts log-uniform in 4k-256k, Morris nu log-uniform in 1e-6..1e-3,
+    refinement on the even scenes): the first 28, as generated."""
+    from adaptivesph_gb300 import scenes
+
+    return scenes.batched_mix()[:28]
+
+
+def test_batched_mix_slice_alone_vs_batch_and_oracle():
+    """Each of 28 scenes of the batched mix gives, in one batch with the 27 others, the state it gives alone, bit for
+    bit, over 25 frames (refinement frames 10 and 20 included); the 3 smallest (one adaptive) also match the oracle."""
+    mix = _mix_slice()
+    counts = [sc.positions.shape[0] for sc in mix]
+    assert min(counts) < 16384 and max(counts) > 65536, "uneven counts wanted"
+    steps = 25
+    alone = [_sim(sc) for sc in mix]
+    for sim, sc in zip(alone, mix):
+        for _ in range(steps):
+            sim.update(sc.dt)
+    mixed = [_sim(sc) for sc in mix]
+    batch = Batch(mixed)
+    batch.step([sc.dt for sc in mix], steps)
+    refined = 0
+    for a, m, sc in zip(alone, mixed, mix):
+        assert m.get_fluid_particles_count() == a.get_fluid_particles_count(), sc.name
+        assert_state_bitexact(m.read_state(), a.read_state())
+        refined += int(sc.refinement is not None and m.get_fluid_particles_count() != sc.positions.shape[0])
+    assert refined > 0, "some adaptive scene must have changed its particle count"
+    assert batch.stats()["graph_steps"] > 0
+    batch.close()
+    order = np.argsort(counts, kind="stable")
+    smallest = [int(k) for k in order[:3]]
+    if not any(mix[k].refinement is not None for k in smallest):
+        smallest[-1] = next(int(k) for k in order if mix[int(k)].refinement is not None)
+    for k in smallest:
+        sc = mix[k]
+        orc = _oracle(sc)
+        for _ in range(steps):
+            orc.step(sc.dt)
+        assert_state_bitexact(mixed[k].read_state(), orc.arrays())
+    for s in alone + mixed:
+        s.close()
+
+
+def test_batch_member_update_domain_recaptures():
+    """A batch member whose domain shrinks between batch steps (updateDomain, no reallocation of its tables) steps
+    on the new grid and walls: the same sequence run alone gives the same state bit for bit."""
+    from helpers import boundary_of
+    from adaptivesph_gb300.parameters import Domain
+
+    scenes_ = _scenes()[:2]
+    runs = []
+    for batched in (False, True):
+        sims = [make_pair(sc)[0] for sc in scenes_]
+        dts = [sc.dt for sc in scenes_]
+        batch = Batch(sims) if batched else None
+
+        def advance(k):
+            if batch is not None:
+                batch.step(dts, k)
+            else:
+                for sim, dt in zip(sims, dts):
+                    for _ in range(k):
+                        sim.update(dt)
+
+        advance(12)
+        captures0 = batch.stats()["captures"] if batch is not None else 0
+        sc = scenes_[0]
+        d = sc.parameters.domain
+        small = Domain(min=tuple(d.min), max=(d.max[0] * 0.9, d.max[1], d.max[2] * 0.95), friction=d.friction)
+        sc_small = small_dam_break()
+        sc_small.parameters.domain = small
+        sims[0].update_domain(small, boundary_of(sc_small))
+        advance(12)
+        runs.append([s.read_state() for s in sims])
+        if batch is not None:
+            assert batch.stats()["captures"] > captures0, "the changed member must be captured again"
+            batch.close()
+        for s in sims:
+            s.close()
+    for a, m in zip(runs[0], runs[1]):
+        assert_state_bitexact(m, a)

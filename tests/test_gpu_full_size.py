@@ -1,7 +1,7 @@
 """Parity at the benchmark sizes, through the C ABI, bit for bit against the oracle.
 
 * The plain 3D dam break (40x80x40 = 128,000 particles at dx = 0.01 m, walls from StaticBoundaryDomain::generate):
-  the whole trajectory of 20 frames from the initial lattice.
+  the whole trajectory of its stated 500 steps from the initial lattice.
 * The adaptive dam break of the headline measurement (100x200x50 = 1,000,000 particles at dx = 0.004 m, 503,100
   wall particles, velocity criterion, capacity 4M): the GPU runs it alone to frame 155, where merged particles have
   grown to several h0 and every summation kind occurs (heavy boxes, long rows, ordinary rows); its state then goes
@@ -27,16 +27,35 @@ def _scene_pair(sc, capacity):
     return sim, orc, bd
 
 
-def test_plain_dam_break_128k_trajectory_bitexact():
+def test_plain_dam_break_128k_500_steps_bitexact():
+    """The plain dam break at its stated length: 500 fixed-dt steps from the lattice (the app's fixed-dt frame loop,
+    app/App.cpp:230), compared bit for bit every 50 steps."""
     sc = scenes.c1_plain()
     sim, orc, _ = _scene_pair(sc, sc.positions.shape[0])
-    for k in range(20):
+    for k in range(500):
         sim.step_async(sc.dt)
         orc.step(sc.dt)
-        if k % 5 == 4:
+        if k % 50 == 49:
             sim.synchronize()
             assert_state_bitexact(sim.read_state(), orc.arrays())
     assert sim.device_errors() == 0
+
+
+def test_totals_run_to_run_bit_identical_128k():
+    """FP64 totals come from fixed-order reductions: two simulations from the same input give bit-identical totals
+    after 30 steps, and so do repeated reads of one state (many blocks: 128k particles)."""
+    sc = scenes.c1_plain()
+    totals = []
+    for _ in range(2):
+        sim, _, _ = _scene_pair(sc, sc.positions.shape[0])
+        for _ in range(30):
+            sim.step_async(sc.dt)
+        sim.synchronize()
+        a, b = sim.totals(), sim.totals()
+        assert a == b
+        totals.append(a)
+        sim.close()
+    assert totals[0] == totals[1]
 
 
 def _transfer(sim, orc):

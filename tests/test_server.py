@@ -103,3 +103,65 @@ def test_estimate_matches_device_memory():
     used = free0 - free1
     assert abs(used - est) <= 0.05 * est + (64 << 20), (used, est)
     sim.close()
+
+
+@pytest.mark.gpu
+def test_server_requests_arriving_while_polling_equal_alone():
+    """Continuous batching: a second thread submits requests one by one while the main thread polls (so requests
+    arrive while others are on the GPU and are admitted as memory frees up); every result equals the request run
+    alone, bit for bit, and the budget holds throughout."""
+    import threading
+    import time
+
+    reqs = _requests() + [(small_dam_break(counts=(9, 14, 9), seed=12, refinement=adaptive_refinement()), 33),
+                          (small_dam_break(counts=(7, 9, 7), seed=13), 20)]
+    sizes = [_bytes(sc) for sc, _ in reqs]
+    budget = int(sum(sorted(sizes)[-3:]) * 1.01)
+    server = Server(budget)
+    tickets = [None] * len(reqs)
+    first_admitted = threading.Event()
+    submitted_all = threading.Event()
+    errors = []
+    arrived_while_running = [0]
+
+    def submitter():
+        try:
+            for k, (sc, steps) in enumerate(reqs):
+                if server.stats()["active"] > 0:
+                    arrived_while_running[0] += 1
+                tickets[k] = server.submit(sc.parameters, sc.positions, boundary_of(sc), sc.refinement, sc.dt, steps,
+                                           sc.refinement.max_particle_count if sc.refinement else None)
+                if k == 0:
+                    first_admitted.wait(timeout=60)  # the rest arrive once the first one runs
+                time.sleep(0.02)
+        except Exception as e:  # surfaced by the main thread
+            errors.append(e)
+        finally:
+            submitted_all.set()
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    polls = 0
+    while True:
+        if server.stats()["active"] > 0:
+            first_admitted.set()
+        left = server.poll(3)
+        polls += 1
+        assert server.stats()["used_bytes"] <= budget
+        if left == 0 and submitted_all.is_set() and all(t is not None for t in tickets):
+            if server.poll(1) == 0:
+                break
+        if left == 0:
+            time.sleep(0.005)
+        assert polls < 100000
+    th.join()
+    assert not errors, errors
+    assert arrived_while_running[0] >= 3, "requests must arrive while others are running"
+    for (sc, steps), t in zip(reqs, tickets):
+        s = server.status(t)
+        assert s["state"] == "done" and s["steps_done"] == steps
+        got = server.take(t)
+        want = _alone(sc, steps)
+        for k in ("ids", "positions", "velocities", "densities", "radii"):
+            assert_bitexact(k, got[k], want[k])
+    server.close()
