@@ -10,9 +10,9 @@ minMassRatio 0.05, maxMassRatio 8, capacity 4M, batch ratio 0.2, cooldowns 10/10
 One JSON line from rank 0. `value` times K steps with the state resident in HBM (CUDA events on the simulation's
 stream, barrier + synchronize on both sides, max over ranks). `e2e` times the same steps through the public C ABI
 with host buffers: the simulation is created from host positions inside the timed region and every step's result
-(positions, velocities, densities, radii) is exported to pinned host memory. `--impl reference` times the
-reference algorithm's CPU restatement (the oracle; the reference itself has no CPU path and its CUDA library
-cannot be built here) on all host cores.
+(positions, velocities, densities, radii) is exported to pinned host memory. `late` continues the simulation to
+frame 150 and times 20 frames there. `--impl reference` times the reference algorithm as the oracle's FP64 step
+on all host cores (the reference itself has no CPU path) over the same frames, without loading the CUDA library.
 """
 from __future__ import annotations
 
@@ -44,6 +44,8 @@ DENSITY_BYTES_PER_PARTICLE = 28.0
 # cell tables 4, reorder 88, density 28, force 60)
 STEP_BYTES_PER_PARTICLE = 332.0
 L2_BYTES = 129e6
+LATE_FRAME = 150  # first frame of the late-frame leg
+LATE_STEPS = 20
 
 
 def measured_peaks():
@@ -133,18 +135,50 @@ def build_scene():
     return sc, bd
 
 
+def build_scene_cpu():
+    """The same scene for the CPU legs: the seeded lattice (pure numpy) and walls from the oracle's restatement of
+    StaticBoundaryDomain::generate, so that the CUDA library is never loaded (bit-identical walls: the parity
+    tests compare both generators)."""
+    import oracle
+    from adaptivesph_gb300 import scenes
+
+    sc = scenes.c2_adaptive()
+    d = sc.parameters.domain
+    pos, psi = oracle.boundary_generate(d.min, d.max, sc.boundary_spacing, sc.parameters.rest_density,
+                                        sc.parameters.base_smoothing_radius)
+    return sc, pos, psi
+
+
+def workload_config(sc, nb: int, world: int) -> dict:
+    """The workload as both arms report it (identical dicts)."""
+    n0 = int(sc.positions.shape[0])
+    return {
+        "workload": WORKLOAD,
+        "particles_initial": n0,
+        "boundary_particles": nb,
+        "capacity": int(sc.refinement.max_particle_count),
+        "dt": sc.dt,
+        "l2": f"inputs larger than L2: ~{device_state_bytes(sc.refinement.max_particle_count, n0, nb) / 1e6:.0f} MB "
+              f"of device state touched per step vs {L2_BYTES / 1e6:.0f} MB L2; no flush",
+        "parallelism": f"replicas x{world}",
+    }
+
+
 def device_state_bytes(n_cap: int, n: int, nb: int) -> int:
     # two buffer sets of (ph, vm, acc, rp, rad, id) + kernel constants + sort buffers, per particle
     return n * (2 * 64 + 16 + 16) + nb * 24
 
 
 # ------------------------------------------------------------------------------------------------ CPU leg
-def cpu_throughput(sc, bd, steps: int, warmup: int):
-    """The oracle (the reference algorithm restated on the CPU) on the same workload, all host threads."""
+def cpu_throughput(steps: int, warmup: int):
+    """The oracle's FP64 step (the reference algorithm restated on the CPU, double precision throughout) on the same
+    workload, all host threads: `warmup` untimed steps, then `steps` timed ones. Returns (particle-steps/s, threads,
+    seconds, frames timed)."""
     import oracle
 
-    o = oracle.OracleSim(sc.parameters, sc.positions, bd.positions, bd.psi, sc.refinement,
-                         capacity=sc.refinement.max_particle_count)
+    sc, bpos, bpsi = build_scene_cpu()
+    o = oracle.OracleSim64(sc.parameters, sc.positions, bpos, bpsi, sc.refinement,
+                           capacity=sc.refinement.max_particle_count)
     for _ in range(warmup):
         o.step(sc.dt)
     ps = 0
@@ -153,7 +187,7 @@ def cpu_throughput(sc, bd, steps: int, warmup: int):
         ps += o.n
         o.step(sc.dt)
     dt = time.perf_counter() - t0
-    return ps / dt, oracle.get_threads(), dt
+    return ps / dt, oracle.get_threads(), dt, (warmup, warmup + steps - 1)
 
 
 # ------------------------------------------------------------------------------------------------ replicas
@@ -224,6 +258,33 @@ def run_ours(args, rank: int, world: int, dist):
     particle_steps = float(sum(counts))
     errors = sim.device_errors()
     n_end = sim.get_fluid_particles_count()
+    frame_end = args.warmup + args.steps
+
+    # ---------------- late frames: the same simulation continued, untimed, to frame LATE_FRAME (merged particles of
+    # several h0 exist from about frame 100 on), then LATE_STEPS frames timed like the main leg
+    late = None
+    if not args.no_late and frame_end <= LATE_FRAME:
+        for _ in range(LATE_FRAME - frame_end):
+            sim.step_async(sc.dt)
+        sim.synchronize()
+        late_counts = []
+        ls, le = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            ls.record(stream)
+            for _ in range(LATE_STEPS):
+                late_counts.append(sim.get_fluid_particles_count())
+                sim.step_async(sc.dt)
+            le.record(stream)
+        torch.cuda.synchronize()
+        late_ms = ls.elapsed_time(le)
+        late = {"value": float(sum(late_counts)) / (late_ms / 1e3), "unit": UNIT,
+                "ms_per_step": late_ms / LATE_STEPS, "frames": [LATE_FRAME, LATE_FRAME + LATE_STEPS - 1],
+                "particles": [late_counts[0], sim.get_fluid_particles_count()],
+                "what": "the same simulation continued untimed to frame 150, then 20 frames timed with the state "
+                        "resident (CUDA events on the simulation's stream); merged particles of several h0 make "
+                        "these frames the slower part of the 2000-step run"}
+        errors |= sim.device_errors()
     sim.close()
 
     # ---------------- end to end through the C ABI with host buffers: the simulation is created from host arrays
@@ -283,19 +344,10 @@ def run_ours(args, rank: int, world: int, dist):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded lattice + jitter; no dataset involved)",
-        "config": {
-            "workload": WORKLOAD,
-            "particles_initial": n0,
-            "particles_final": n_end,
-            "boundary_particles": bd.get_particle_count(),
-            "capacity": cap,
-            "dt": sc.dt,
-            "refinement_frames_timed": sum(1 for f in range(args.warmup, args.warmup + args.steps)
-                                           if f == 10 or (f > 10 and f % 10 == 0)),
-            "l2": f"inputs larger than L2: ~{device_state_bytes(cap, n0, bd.get_particle_count()) / 1e6:.0f} MB of "
-                  f"device state touched per step vs {L2_BYTES / 1e6:.0f} MB L2; no flush",
-            "parallelism": f"replicas x{world}",
-        },
+        "config": workload_config(sc, bd.get_particle_count(), world),
+        "frames_timed": [args.warmup, frame_end - 1],
+        "particles_final": n_end,
+        "refinement_frames_timed": sum(1 for f in range(args.warmup, frame_end) if f == 10 or (f > 10 and f % 10 == 0)),
         "roofline": {
             "bound": "hbm",
             "kernel": "density pass (k_density with its heavy and long-row kernels)",
@@ -327,41 +379,50 @@ def run_ours(args, rank: int, world: int, dist):
         "device_errors": errors,
         "clocks": clocks,
     }
+    if late is not None:
+        line["late"] = late
     if not args.no_cpu:
-        cps, cores, secs = cpu_throughput(sc, bd, args.cpu_steps, 1)
+        cps, cores, secs, (f0, f1) = cpu_throughput(args.cpu_steps, 1)
         line["cpu_baseline"] = {"value": cps, "unit": UNIT, "cores": cores, "kind": "port",
-                                "sample": f"{args.cpu_steps} steps of the same 1M-particle workload after 1 warm-up "
-                                          f"step (frames 1..{args.cpu_steps}, refinement at frame 10), {secs:.1f} s"}
+                                "sample": f"the oracle's FP64 step: {args.cpu_steps} steps of the same 1M-particle "
+                                          f"workload after 1 warm-up step (frames {f0}..{f1}, refinement at frame 10), "
+                                          f"{secs:.1f} s"}
     return line
 
 
-def run_reference(args, rank: int):
+def run_reference(args, rank: int, world: int):
+    """The reference arm: the reference has no CPU path and no published number, and its CUDA library is not part of
+    this arm; the algorithm runs as the oracle's FP64 step (a restatement of the reference's step, double precision
+    throughout) on all host cores, over the same frames as the GPU arm (`warmup` untimed, then `steps` timed, at
+    most --ref-steps of them). The CUDA library of this repository is never loaded here."""
     if rank != 0:
         return None
-    sc, bd = build_scene()
-    steps = min(args.steps, args.cpu_steps)
-    warm = min(args.warmup, 1)
-    cps, cores, secs = cpu_throughput(sc, bd, steps, warm)
+    import adaptivesph_gb300._lib as product_lib
+
+    steps = min(args.steps, args.ref_steps)
+    sc, bpos, _ = build_scene_cpu()
+    cps, cores, secs, (f0, f1) = cpu_throughput(steps, args.warmup)
+    if product_lib._lib is not None:
+        raise RuntimeError("the reference arm must not load the CUDA library")
     return {
         "impl": "reference",
         "metric": METRIC,
         "value": cps,
         "unit": UNIT,
-        "n_gpus": 1,
+        "n_gpus": world,
         "steps": steps,
-        "warmup": warm,
+        "warmup": args.warmup,
         "ms_per_step": secs / steps * 1e3,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32",
+        "dtype": "f64",
         "data": "synthetic (seeded lattice + jitter; no dataset involved)",
-        "config": {"workload": WORKLOAD, "particles_initial": int(sc.positions.shape[0]),
-                   "boundary_particles": bd.get_particle_count()},
+        "config": workload_config(sc, int(bpos.shape[0]), world),
+        "frames_timed": [f0, f1],
         "cpu_baseline": {"value": cps, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{steps} steps of the 1M-particle workload after {warm} warm-up step(s), "
-                                   f"{secs:.1f} s; the reference has no CPU path and its CUDA library needs glm and "
-                                   f"nanoflann (absent), so its algorithm runs as the oracle's C restatement"},
+                         "sample": f"frames {f0}..{f1} of the 1M-particle workload ({steps} steps after {args.warmup} "
+                                   f"untimed), {secs:.1f} s: the oracle's FP64 step (the reference has no CPU path)"},
         "e2e": {"value": cps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -556,7 +617,9 @@ def main():
     ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--cpu-steps", type=int, default=10)
+    ap.add_argument("--cpu-steps", type=int, default=10, help="steps of the CPU baseline sample in the GPU arm")
+    ap.add_argument("--ref-steps", type=int, default=40, help="most steps the reference arm times")
+    ap.add_argument("--no-late", action="store_true", help="skip the late-frame leg")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--workload", choices=["adaptive1m", "batched", "served"], default="adaptive1m",
@@ -576,7 +639,7 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
-        line = run_reference(args, rank)
+        line = run_reference(args, rank, world)
         if line is not None:
             print(json.dumps(line), flush=True)
         return
