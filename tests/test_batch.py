@@ -118,9 +118,9 @@ def test_batch_member_update_domain_recaptures():
     from helpers import boundary_of
     from adaptivesph_gb300.parameters import Domain
 
-    scenes_ = _scenes()[:2]
     runs = []
     for batched in (False, True):
+        scenes_ = _scenes()[:2]  # fresh scenes: update_domain writes the new domain into the scene's parameters
         sims = [make_pair(sc)[0] for sc in scenes_]
         dts = [sc.dt for sc in scenes_]
         batch = Batch(sims) if batched else None
