@@ -113,10 +113,12 @@ def test_server_requests_arriving_while_polling_equal_alone():
     import threading
     import time
 
-    reqs = _requests() + [(small_dam_break(counts=(9, 14, 9), seed=12, refinement=adaptive_refinement()), 33),
-                          (small_dam_break(counts=(7, 9, 7), seed=13), 20)]
+    # the first request runs long enough (400 steps) that the others arrive while it is on the GPU
+    reqs = [(small_dam_break(counts=(12, 24, 12), seed=21), 400)] + _requests() + [
+        (small_dam_break(counts=(9, 14, 9), seed=12, refinement=adaptive_refinement()), 33),
+        (small_dam_break(counts=(7, 9, 7), seed=13), 20)]
     sizes = [_bytes(sc) for sc, _ in reqs]
-    budget = int(sum(sorted(sizes)[-3:]) * 1.01)
+    budget = int(sum(sorted(sizes)[-3:]) * 1.01)  # room for about three requests at a time
     server = Server(budget)
     tickets = [None] * len(reqs)
     first_admitted = threading.Event()
@@ -133,7 +135,7 @@ def test_server_requests_arriving_while_polling_equal_alone():
                                            sc.refinement.max_particle_count if sc.refinement else None)
                 if k == 0:
                     first_admitted.wait(timeout=60)  # the rest arrive once the first one runs
-                time.sleep(0.02)
+                time.sleep(0.002)
         except Exception as e:  # surfaced by the main thread
             errors.append(e)
         finally:
