@@ -38,7 +38,8 @@ struct RefineArgs {
     float min_mass, max_mass, max_batch_ratio;
     float eps, alpha, center_ratio, vertex_ratio;
     float vel_split, vel_merge, vort_split, vort_merge, iface_split, iface_merge;
-    float r0, m0;
+    float fs_split, fs_merge;  // free-surface criterion: neighbour-count deficit thresholds
+    float r0, m0, rho0;
     uint32_t criterion;
 };
 

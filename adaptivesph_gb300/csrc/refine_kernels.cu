@@ -93,6 +93,32 @@ __device__ float vorticity_mag(const StepArgs& a, const CellsDev& c, uint32_t i)
     return sqrtf(fmaf(oz, oz, fmaf(oy, oy, ox * ox)));
 }
 
+// Neighbour-count deficit of the free-surface criterion (no reference counterpart): N = #{j != i : r^2 <= (2 h_j)^2}
+// over the candidate cells of [x - 2h_i, x + 2h_i] (the per-particle count of sumAllNeighbors, Algorithm.cu:234-268)
+// against N_ref = (4 pi / 3) (2 h_i)^3 rho0 / m_i - 1, the count a uniform medium of the particle's own volume gives;
+// returns 1 - N / N_ref (positive where neighbours are missing: at the free surface).
+template <bool kCull>
+__device__ float neighbour_deficit(const StepArgs& a, const CellsDev& c, uint32_t i, float rho0) {
+    const float4 pi = a.ph[i];
+    const bool periodic = a.grid.periodic;
+    const float R = pi.w + pi.w;
+    uint32_t cnt = 0;
+    for_each_cell<kCull>(a.grid, c.start, c.end, c.hmax, c.hmax_ref, c.ex[0], c.ex[1], pi.x, pi.y, pi.z, R, 0.0f,
+                         [&](uint32_t jb, uint32_t je, float shx, float shy, float shz) {
+                             for (uint32_t j = jb; j < je; ++j) {
+                                 if (j == i) continue;
+                                 const float4 pj = __ldg(a.ph + j);
+                                 const float dx = (periodic ? pj.x + shx : pj.x) - pi.x;
+                                 const float dy = (periodic ? pj.y + shy : pj.y) - pi.y;
+                                 const float dz = (periodic ? pj.z + shz : pj.z) - pi.z;
+                                 const float twoh = pj.w + pj.w;
+                                 cnt += dist2(dx, dy, dz) <= twoh * twoh;
+                             }
+                         });
+    const float nref = ((4.18879020478639f * ((R * R) * R)) * rho0) / a.vm[i].w - 1.0f;
+    return 1.0f - (float)cnt / nref;
+}
+
 __device__ __forceinline__ void min_surface_distance(const GridDev& g, float4 p, float out[3]) {
     const float pp[3] = {p.x, p.y, p.z};
 #pragma unroll
@@ -114,7 +140,7 @@ __device__ __forceinline__ float compmin3(const float v[3]) {
 }  // namespace
 
 // merge criterion per particle (VelocityCriterion.cuh:208-227, InterfaceCriterion.cuh:97-115,
-// VorticityCriterion.cuh:248-312); slot-0 particle (smallest id) found on the way.
+// VorticityCriterion.cuh:248-312; free surface: neighbour_deficit); slot-0 particle (smallest id) found on the way.
 __global__ void __launch_bounds__(256, 2) k_merge_score(StepArgs a, CellsDev c, RefineArgs r) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     float s = -1.0f;
@@ -133,6 +159,10 @@ __global__ void __launch_bounds__(256, 2) k_merge_score(StepArgs a, CellsDev c, 
             } else if (r.criterion == 2u) {
                 const float mag = vorticity_mag<true>(a, c, i);
                 s = (mag >= 0.0f && mag < r.vort_merge) ? mag / r.vort_merge : -1.0f;
+            } else if (r.criterion == 3u) {
+                const float d = neighbour_deficit<true>(a, c, i, r.rho0);
+                const float t = r.fs_merge;
+                s = d <= t ? ((d > 0.0f ? d : 0.0f) + t) / (t + t) : -1.0f;
             } else {
                 const float sp = sqrtf(fmaf(v.z, v.z, fmaf(v.y, v.y, v.x * v.x)));
                 s = sp < r.vel_merge ? sp / r.vel_merge : -1.0f;
@@ -171,6 +201,14 @@ __global__ void __launch_bounds__(256, 2) k_split_score(StepArgs a, CellsDev c, 
                 if (r.criterion == 2u) {
                     const float mag = vorticity_mag<false>(a, c, i);
                     s = (mag >= 0.0f && mag > r.vort_split) ? mag : -1.0f;
+                } else if (r.criterion == 3u) {
+                    // within 2h of a domain face the clamp, not the air, truncates the support: no split there
+                    float md[3];
+                    min_surface_distance(a.grid, p, md);
+                    if (a.grid.periodic || !(compmin3(md) < p.w + p.w)) {
+                        const float d = neighbour_deficit<false>(a, c, i, r.rho0);
+                        s = d >= r.fs_split ? d : -1.0f;
+                    }
                 } else {
                     const float sp = sqrtf(fmaf(v.z, v.z, fmaf(v.y, v.y, v.x * v.x)));
                     s = sp < r.vel_split ? -1.0f : sp;

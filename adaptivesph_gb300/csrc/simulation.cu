@@ -648,8 +648,11 @@ RefineArgs refine_args(asph_simulation* s) {
     r.vort_merge = R.vorticity_merge_max;
     r.iface_split = R.interface_split_distance_ratio;
     r.iface_merge = R.interface_merge_distance_ratio;
+    r.fs_split = R.free_surface_split_deficit;
+    r.fs_merge = R.free_surface_merge_deficit;
     r.r0 = s->P.base_particle_radius;
     r.m0 = s->P.base_particle_mass;
+    r.rho0 = s->P.rest_density;
     r.criterion = R.criterion;
     return r;
 }
@@ -675,7 +678,9 @@ asph_status refine_enqueue(asph_simulation* s) {
     s->h_ctr[kCtrNextId] = s->next_id;
     CK(cudaMemcpyAsync(s->ctr, s->h_ctr, sizeof(uint32_t) * kCtrNum, cudaMemcpyHostToDevice, s->stream));
     CK(cudaMemsetAsync(s->slot0, 0xff, sizeof(unsigned long long), s->stream));
-    if (s->R.criterion == ASPH_CRITERION_VORTICITY) {
+    // criteria that walk neighbours evaluate the split scores on the cells of the compacted set
+    const bool walks = s->R.criterion == ASPH_CRITERION_VORTICITY || s->R.criterion == ASPH_CRITERION_FREE_SURFACE;
+    if (walks) {
         // keep the cell keys of this step: the selection sorts reuse the sort buffers
         CK(cudaMemcpyAsync(s->rkeys, s->keys, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s->stream));
     }
@@ -698,20 +703,19 @@ asph_status refine_enqueue(asph_simulation* s) {
     k_merge_candidates_heavy<<<heavy_blocks(n), 256, 0, s->stream>>>(a, s->cells(), r);
     k_merge_pairs<<<nbk, 256, 0, s->stream>>>(a, r);
     CK_LAUNCH("merge");
-    // stable compaction into the other buffer set (also carries the cell keys for the vorticity split pass)
+    // stable compaction into the other buffer set (also carries the cell keys for a split pass that walks cells)
     k_compact_count<<<nbk, 256, 0, s->stream>>>(s->flag, n, s->block_counts);
     k_compact_scan<<<1, 1024, 0, s->stream>>>(s->block_counts, nbk, n, r);
     const int nxt = 1 - s->cur;
     StepArgs b = s->args(nxt);
-    const bool vort = s->R.criterion == ASPH_CRITERION_VORTICITY;
     uint32_t* keys_c = s->rkeys + s->cap;
-    k_compact_scatter<<<nbk, 256, 0, s->stream>>>(a, b, s->flag, s->block_counts, vort ? s->rkeys : nullptr,
+    k_compact_scatter<<<nbk, 256, 0, s->stream>>>(a, b, s->flag, s->block_counts, walks ? s->rkeys : nullptr,
                                                    keys_c);
     CK_LAUNCH("compaction");
     s->launches += 8;
     s->cur = nxt;
     StepArgs c = s->args(s->cur);
-    if (vort) {
+    if (walks) {
         // the compacted keys are still cell-sorted: rebuild the tables for the split criterion's search
         CK(cudaMemsetAsync(s->cell_start, 0xff, sizeof(uint32_t) * s->grid.ncells, s->stream));
         CK(cudaMemsetAsync(s->cell_end, 0, sizeof(uint32_t) * s->grid.ncells, s->stream));
@@ -1017,6 +1021,8 @@ void asph_refinement_parameters_default(asph_refinement_parameters* p) {
     p->curvature_merge_max = 0.6f;
     p->interface_split_distance_ratio = 0.05f;
     p->interface_merge_distance_ratio = 0.15f;
+    p->free_surface_split_deficit = 0.25f;
+    p->free_surface_merge_deficit = 0.05f;
 }
 
 // ---------------------------------------------------------------------------------------------- memory
@@ -1114,7 +1120,10 @@ asph_status asph_simulation_create(const asph_parameters* parameters, const floa
     const bool adaptive = refinement && refinement->enabled;
     if (adaptive) {
         if (refinement->cooldown == 0) return fail(ASPH_ERR_INVALID_ARGUMENT, "refinement cooldown must be > 0");
-        if (refinement->criterion > 2u) return fail(ASPH_ERR_INVALID_ARGUMENT, "unknown refinement criterion");
+        if (refinement->criterion > 3u) return fail(ASPH_ERR_INVALID_ARGUMENT, "unknown refinement criterion");
+        if (refinement->criterion == ASPH_CRITERION_FREE_SURFACE &&
+            !(refinement->free_surface_merge_deficit > 0.0f && refinement->free_surface_split_deficit > 0.0f))
+            return fail(ASPH_ERR_INVALID_ARGUMENT, "free-surface deficits must be positive");
         if (P.boundary_mode == ASPH_BOUNDARY_PERIODIC)
             return fail(ASPH_ERR_UNSUPPORTED, "refinement in a periodic box is not supported");
     }

@@ -22,6 +22,7 @@ class Criterion(enum.IntEnum):
     VELOCITY = 0
     INTERFACE = 1
     VORTICITY = 2
+    FREE_SURFACE = 3  # neighbour-count deficit; no reference counterpart
 
 
 class ViscosityModel(enum.IntEnum):
@@ -107,6 +108,9 @@ class RefinementParameters:
     curvature_merge_max: float = 0.6
     interface_split_distance_ratio: float = 0.05
     interface_merge_distance_ratio: float = 0.15
+    # extension: the free-surface criterion's neighbour-count deficits (split at or above, merge at or below)
+    free_surface_split_deficit: float = 0.25
+    free_surface_merge_deficit: float = 0.05
 
 
 @dataclass
@@ -169,6 +173,8 @@ class CRefinementParameters(ctypes.Structure):
         ("curvature_merge_max", ctypes.c_float),
         ("interface_split_distance_ratio", ctypes.c_float),
         ("interface_merge_distance_ratio", ctypes.c_float),
+        ("free_surface_split_deficit", ctypes.c_float),
+        ("free_surface_merge_deficit", ctypes.c_float),
     ]
 
 
@@ -309,4 +315,6 @@ def to_c_refinement(r: RefinementParameters) -> CRefinementParameters:
         r.curvature_merge_max,
         r.interface_split_distance_ratio,
         r.interface_merge_distance_ratio,
+        r.free_surface_split_deficit,
+        r.free_surface_merge_deficit,
     )

@@ -74,16 +74,19 @@ def c1_plain(seed: int = 1) -> Scene:
     return s
 
 
-def c2_refinement(max_particle_count: int = 4_000_000) -> RefinementParameters:
+def c2_refinement(max_particle_count: int = 4_000_000, criterion: Criterion = Criterion.VELOCITY) -> RefinementParameters:
     return RefinementParameters(enabled=True, min_mass_ratio=0.05, max_mass_ratio=8.0,
                                 max_particle_count=max_particle_count, max_batch_ratio=0.2, initial_cooldown=10,
-                                cooldown=10, criterion=Criterion.VELOCITY)
+                                cooldown=10, criterion=criterion)
 
 
-def c2_adaptive(seed: int = 2, counts=(100, 200, 50), max_particle_count: int = 4_000_000) -> Scene:
-    """Adaptive dam break: 100x200x50 = 1,000,000 particles at dx = 0.004 m, velocity criterion, minMassRatio 0.05
-    (two split levels), maxMassRatio 8, capacity 4M, batch ratio 0.2, cooldowns 10/10."""
-    s = dam_break(counts, 0.004, seed=seed, refinement=c2_refinement(max_particle_count), column_height=0.8)
+def c2_adaptive(seed: int = 2, counts=(100, 200, 50), max_particle_count: int = 4_000_000,
+                criterion: Criterion = Criterion.VELOCITY) -> Scene:
+    """Adaptive dam break: 100x200x50 = 1,000,000 particles at dx = 0.004 m, velocity criterion (the reference's
+    default; Criterion.FREE_SURFACE splits at the free surface instead), minMassRatio 0.05 (two split levels),
+    maxMassRatio 8, capacity 4M, batch ratio 0.2, cooldowns 10/10."""
+    s = dam_break(counts, 0.004, seed=seed, refinement=c2_refinement(max_particle_count, criterion),
+                  column_height=0.8)
     s.name = "dam_break_adaptive_1m"
     return s
 

@@ -126,34 +126,43 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------------------------------------ scene
-def build_scene():
-    from adaptivesph_gb300 import StaticBoundaryDomain, scenes
+def c2_scene(args):
+    from adaptivesph_gb300 import scenes
+    from adaptivesph_gb300.parameters import Criterion
 
-    sc = scenes.c2_adaptive()
+    return scenes.c2_adaptive(criterion=Criterion.FREE_SURFACE if args.criterion == "free_surface"
+                              else Criterion.VELOCITY)
+
+
+def build_scene(args):
+    from adaptivesph_gb300 import StaticBoundaryDomain
+
+    sc = c2_scene(args)
     bd = StaticBoundaryDomain.generate(sc.parameters.domain, sc.boundary_spacing, sc.parameters.rest_density,
                                        sc.parameters.base_smoothing_radius)
     return sc, bd
 
 
-def build_scene_cpu():
+def build_scene_cpu(args):
     """The same scene for the CPU legs: the seeded lattice (pure numpy) and walls from the oracle's restatement of
     StaticBoundaryDomain::generate, so that the CUDA library is never loaded (bit-identical walls: the parity
     tests compare both generators)."""
     import oracle
-    from adaptivesph_gb300 import scenes
 
-    sc = scenes.c2_adaptive()
+    sc = c2_scene(args)
     d = sc.parameters.domain
     pos, psi = oracle.boundary_generate(d.min, d.max, sc.boundary_spacing, sc.parameters.rest_density,
                                         sc.parameters.base_smoothing_radius)
     return sc, pos, psi
 
 
-def workload_config(sc, nb: int, world: int) -> dict:
+def workload_config(sc, nb: int, world: int, args) -> dict:
     """The workload as both arms report it (identical dicts)."""
     n0 = int(sc.positions.shape[0])
+    workload = WORKLOAD if args.criterion == "velocity" else WORKLOAD.replace("velocity criterion",
+                                                                             "free-surface criterion")
     return {
-        "workload": WORKLOAD,
+        "workload": workload,
         "particles_initial": n0,
         "boundary_particles": nb,
         "capacity": int(sc.refinement.max_particle_count),
@@ -170,13 +179,13 @@ def device_state_bytes(n_cap: int, n: int, nb: int) -> int:
 
 
 # ------------------------------------------------------------------------------------------------ CPU leg
-def cpu_throughput(steps: int, warmup: int):
+def cpu_throughput(args, steps: int, warmup: int):
     """The oracle's FP64 step (the reference algorithm restated on the CPU, double precision throughout) on the same
     workload, all host threads: `warmup` untimed steps, then `steps` timed ones. Returns (particle-steps/s, threads,
     seconds, frames timed)."""
     import oracle
 
-    sc, bpos, bpsi = build_scene_cpu()
+    sc, bpos, bpsi = build_scene_cpu(args)
     o = oracle.OracleSim64(sc.parameters, sc.positions, bpos, bpsi, sc.refinement,
                            capacity=sc.refinement.max_particle_count)
     for _ in range(warmup):
@@ -218,7 +227,7 @@ def run_ours(args, rank: int, world: int, dist):
 
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
-    sc, bd = build_scene()
+    sc, bd = build_scene(args)
     n0 = sc.positions.shape[0]
     if args.capacity:
         sc.refinement.max_particle_count = args.capacity
@@ -344,7 +353,7 @@ def run_ours(args, rank: int, world: int, dist):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded lattice + jitter; no dataset involved)",
-        "config": workload_config(sc, bd.get_particle_count(), world),
+        "config": workload_config(sc, bd.get_particle_count(), world, args),
         "frames_timed": [args.warmup, frame_end - 1],
         "particles_final": n_end,
         "refinement_frames_timed": sum(1 for f in range(args.warmup, frame_end) if f == 10 or (f > 10 and f % 10 == 0)),
@@ -382,7 +391,7 @@ def run_ours(args, rank: int, world: int, dist):
     if late is not None:
         line["late"] = late
     if not args.no_cpu:
-        cps, cores, secs, (f0, f1) = cpu_throughput(args.cpu_steps, 1)
+        cps, cores, secs, (f0, f1) = cpu_throughput(args, args.cpu_steps, 1)
         line["cpu_baseline"] = {"value": cps, "unit": UNIT, "cores": cores, "kind": "port",
                                 "sample": f"the oracle's FP64 step: {args.cpu_steps} steps of the same 1M-particle "
                                           f"workload after 1 warm-up step (frames {f0}..{f1}, refinement at frame 10), "
@@ -400,8 +409,8 @@ def run_reference(args, rank: int, world: int):
     import adaptivesph_gb300._lib as product_lib
 
     steps = min(args.steps, args.ref_steps)
-    sc, bpos, _ = build_scene_cpu()
-    cps, cores, secs, (f0, f1) = cpu_throughput(steps, args.warmup)
+    sc, bpos, _ = build_scene_cpu(args)
+    cps, cores, secs, (f0, f1) = cpu_throughput(args, steps, args.warmup)
     if product_lib._lib is not None:
         raise RuntimeError("the reference arm must not load the CUDA library")
     return {
@@ -418,7 +427,7 @@ def run_reference(args, rank: int, world: int):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded lattice + jitter; no dataset involved)",
-        "config": workload_config(sc, int(bpos.shape[0]), world),
+        "config": workload_config(sc, int(bpos.shape[0]), world, args),
         "frames_timed": [f0, f1],
         "cpu_baseline": {"value": cps, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"frames {f0}..{f1} of the 1M-particle workload ({steps} steps after {args.warmup} "
@@ -620,6 +629,9 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=10, help="steps of the CPU baseline sample in the GPU arm")
     ap.add_argument("--ref-steps", type=int, default=40, help="most steps the reference arm times")
     ap.add_argument("--no-late", action="store_true", help="skip the late-frame leg")
+    ap.add_argument("--criterion", choices=["velocity", "free_surface"], default="velocity",
+                    help="split/merge criterion of the 1M adaptive dam break: the reference's velocity criterion, or "
+                         "the neighbour-count deficit that splits at the free surface")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--workload", choices=["adaptive1m", "batched", "served"], default="adaptive1m",

@@ -77,6 +77,13 @@ typedef struct asph_parameters {
 #define ASPH_CRITERION_VELOCITY 0u  /* refinement/criteria/VelocityCriterion.cuh */
 #define ASPH_CRITERION_INTERFACE 1u /* refinement/criteria/InterfaceCriterion.cuh */
 #define ASPH_CRITERION_VORTICITY 2u /* refinement/criteria/VorticityCriterion.cuh */
+/* Free surface (no reference counterpart): neighbour-count deficit d = 1 - N / N_ref, N the particle's neighbours
+ * (|x_i - x_j|^2 <= (2 h_j)^2 over the candidate cells of [x - 2h_i, x + 2h_i], self excluded) and
+ * N_ref = (4 pi / 3) (2 h_i)^3 rho0 / m_i - 1 the count a uniform medium of its own volume would give. Split where
+ * d >= free_surface_split_deficit (score d), except within 2 h_i of a domain face (there the domain clamp, not the
+ * air, truncates the support) and where the daughters would leave the domain (as for the other criteria); merge where
+ * d <= free_surface_merge_deficit (score (max(d, 0) + t) / 2t, t the merge deficit: deep bulk first). */
+#define ASPH_CRITERION_FREE_SURFACE 3u
 
 /* refinement::RefinementParameters with its nested parameter structs
  * (cuda/include/cuda/refinement/RefinementParameters.cuh:6-104), flattened. */
@@ -106,6 +113,9 @@ typedef struct asph_refinement_parameters {
     /* InterfaceParameters (:56-70) */
     float interface_split_distance_ratio;
     float interface_merge_distance_ratio;
+    /* extension (no reference counterpart): the free-surface criterion's thresholds */
+    float free_surface_split_deficit;
+    float free_surface_merge_deficit;
 } asph_refinement_parameters;
 
 /* Fills *p with the reference's defaults (RefinementParameters.cuh:8-104). */

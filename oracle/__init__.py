@@ -66,6 +66,8 @@ class OrcRefine(ctypes.Structure):
         ("curv_merge", ctypes.c_float),
         ("iface_split", ctypes.c_float),
         ("iface_merge", ctypes.c_float),
+        ("fs_split", ctypes.c_float),
+        ("fs_merge", ctypes.c_float),
     ]
 
 
@@ -252,7 +254,8 @@ def make_refine(r) -> OrcRefine:
         int(r.initial_cooldown), int(r.cooldown), int(r.criterion), r.split_epsilon, r.split_alpha,
         r.split_center_mass_ratio, r.split_vertex_mass_ratio, r.velocity_split_min_speed,
         r.velocity_merge_max_speed, r.vorticity_split_min, r.vorticity_merge_max, r.curvature_split_min,
-        r.curvature_merge_max, r.interface_split_distance_ratio, r.interface_merge_distance_ratio)
+        r.curvature_merge_max, r.interface_split_distance_ratio, r.interface_merge_distance_ratio,
+        r.free_surface_split_deficit, r.free_surface_merge_deficit)
 
 
 def set_threads(n: int) -> None:

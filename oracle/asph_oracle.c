@@ -555,6 +555,7 @@ static uint64_t sortable_d(double f)
 }
 
 static const float ORC_PHI_F = 1.6180339887498949f;
+#define ORC_FOUR_THIRDS_PI 4.18879020478639098461685784437267051226289253250014109463325945641042187504827866483737976712282275730953078202
 static const float ORC_INVNORM_F = 0.5257311121f;
 
 /* FP32 canonical arithmetic on the FP32 state (the bit-exact checker) */

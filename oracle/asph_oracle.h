@@ -48,6 +48,7 @@ typedef struct orc_refine {
     uint32_t initial_cooldown, cooldown, criterion;
     float eps, alpha, center_ratio, vertex_ratio;
     float vel_split, vel_merge, vort_split, vort_merge, curv_split, curv_merge, iface_split, iface_merge;
+    float fs_split, fs_merge; /* free-surface criterion (3): neighbour-count deficit thresholds */
 } orc_refine;
 
 typedef struct orc_grid {

@@ -9,7 +9,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "asph_oracle.c")
-DEPS = [SRC, os.path.join(HERE, "oracle_body.h"), os.path.join(HERE, "asph_oracle.h")]
+DEPS = [SRC, os.path.join(HERE, "oracle_body.h"), os.path.join(HERE, "refine_body.h"), os.path.join(HERE, "asph_oracle.h")]
 LIB = os.path.join(HERE, "libasph_oracle.so")
 
 

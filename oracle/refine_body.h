@@ -84,8 +84,41 @@ static REAL F(compmin3)(const REAL v[3])
     return m;
 }
 
+/* Neighbour-count deficit of the free-surface criterion (no reference counterpart): N = #{j != i : r^2 <= (2 h_j)^2}
+ * over the candidate cells of [x - 2h_i, x + 2h_i] (the count of sumAllNeighbors, Algorithm.cu:234-268), against
+ * N_ref = (4 pi / 3) (2 h_i)^3 rho0 / m_i - 1; returns 1 - N / N_ref. */
+static REAL F(neighbour_deficit)(const orc_grid* g, const orc_params* P, const STATE* s, const orc_cells* c,
+                                 uint32_t i)
+{
+    const REAL* pi = s->pos + 4 * (size_t)i;
+    const REAL xi = pi[0], yi = pi[1], zi = pi[2];
+    const REAL R2 = s->h[i] + s->h[i];
+    uint32_t cnt = 0;
+    orc_iter it;
+    uint32_t jb, je;
+    float sh[3];
+    float pif[4];
+    it_init(&it, g, c->start, c->end, c->ex, ITPOS(pi, pif), (float)R2);
+    while (it_next(&it, &jb, &je, sh)) {
+        for (uint32_t j = jb; j < je; j++) {
+            if (j == i) {
+                continue;
+            }
+            const SREAL* pj = s->pos + 4 * (size_t)j;
+            const REAL dx = NBR(pj, 0) - xi;
+            const REAL dy = NBR(pj, 1) - yi;
+            const REAL dz = NBR(pj, 2) - zi;
+            const REAL r2 = F(dist2)(dx, dy, dz);
+            const REAL twoh = s->h[j] + s->h[j];
+            cnt += r2 <= twoh * twoh;
+        }
+    }
+    const REAL nref = (((REAL)ORC_FOUR_THIRDS_PI * ((R2 * R2) * R2)) * (REAL)P->rho0) / s->m[i] - (REAL)1;
+    return (REAL)1 - (REAL)cnt / nref;
+}
+
 /* merge criterion generators: VelocityCriterion.cuh:208-227, InterfaceCriterion.cuh:97-115,
- * VorticityCriterion.cuh:248-312 */
+ * VorticityCriterion.cuh:248-312; free surface (3): see neighbour_deficit */
 static REAL F(merge_score)(const orc_grid* g, const orc_params* P, const orc_refine* R, const STATE* s,
                          const orc_cells* c, uint32_t i, REAL maxMass)
 {
@@ -110,6 +143,11 @@ static REAL F(merge_score)(const orc_grid* g, const orc_params* P, const orc_ref
             return mag / R->vort_merge;
         }
         return -1.0f;
+    }
+    if (R->criterion == 3u) {
+        const REAL d = F(neighbour_deficit)(g, P, s, c, i);
+        const REAL t = R->fs_merge;
+        return d <= t ? ((d > (REAL)0 ? d : (REAL)0) + t) / (t + t) : (REAL)-1;
     }
     const REAL* v = s->vel + 4 * (size_t)i;
     const REAL sp = SQRT(FMA(v[2], v[2], FMA(v[1], v[1], v[0] * v[0])));
@@ -149,6 +187,16 @@ static REAL F(split_score)(const orc_grid* g, const orc_params* P, const orc_ref
             return -1.0f;
         }
         return mag > R->vort_split ? mag : -1.0f;
+    }
+    if (R->criterion == 3u) {
+        /* within 2h of a domain face the clamp, not the air, truncates the support: no split there */
+        REAL md[3];
+        F(min_surface_distance)(P, p, md);
+        if (!g->periodic && F(compmin3)(md) < h + h) {
+            return -1.0f;
+        }
+        const REAL d = F(neighbour_deficit)(g, P, s, c, i);
+        return d >= R->fs_split ? d : (REAL)-1;
     }
     const REAL* v = s->vel + 4 * (size_t)i;
     const REAL sp = SQRT(FMA(v[2], v[2], FMA(v[1], v[1], v[0] * v[0])));
@@ -389,7 +437,7 @@ void F(refine_impl)(const orc_grid* g, const orc_params* P, const orc_refine* R,
         rep->removed = removed;
         s->n = w;
         const uint32_t n2 = w;
-        if (R->criterion == 2u) {
+        if (R->criterion == 2u || R->criterion == 3u) { /* criteria that walk neighbours: cells of the compacted set */
             orc_cells_from_keys(g, n2, c->keys, c->start, c->end);
         }
         uint32_t cs = 0;

@@ -15,7 +15,7 @@ from helpers import (adaptive_refinement, assert_bitexact, assert_state_bitexact
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("criterion", [Criterion.VORTICITY, Criterion.INTERFACE])
+@pytest.mark.parametrize("criterion", [Criterion.VORTICITY, Criterion.INTERFACE, Criterion.FREE_SURFACE])
 def test_criterion_trajectory_bitexact(criterion):
     ref = adaptive_refinement(criterion=criterion, velocity_split_min_speed=2.0, velocity_merge_max_speed=0.1)
     sc = small_dam_break(refinement=ref)
