@@ -7,7 +7,7 @@ from .parameters import (BoundaryMode, Criterion, DensityInfo, Domain, Parameter
                          ViscosityModel)
 from .simulation import (Batch, BoundaryParticlesDataImportedBuffer, FluidParticlesDataImportedBuffer, ImportedMemory,
                          Server, Simulation, StaticBoundaryDomain, allocate_buffer, create_simulation,
-                         estimate_device_bytes, import_buffer)
+                         create_simulation_with_walls, estimate_device_bytes, import_buffer)
 from ._lib import AsphError, load as load_library
 
 __all__ = [
@@ -28,6 +28,7 @@ __all__ = [
     "ViscosityModel",
     "allocate_buffer",
     "create_simulation",
+    "create_simulation_with_walls",
     "estimate_device_bytes",
     "import_buffer",
     "load_library",

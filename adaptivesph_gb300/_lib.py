@@ -56,6 +56,9 @@ SIGNATURES = {
     "asph_memory_size": (ctypes.c_int, [_vp, P(ctypes.c_size_t)]),
     "asph_memory_release": (None, [_vp]),
     "asph_boundary_generate": (ctypes.c_int, [P(_p.CDomain), _f32, _f32, _f32, _vp, _u32, _up]),
+    "asph_boundary_generate_gpu": (ctypes.c_int, [P(_p.CDomain), _f32, _f32, _f32, _vp, _u32, _up]),
+    "asph_simulation_create_with_walls": (ctypes.c_int, [P(_p.CParameters), _fp, _u32, _vp, _vp, _f32,
+                                                         P(_p.CRefinementParameters), _u32, _u32, P(_vp)]),
     "asph_simulation_create": (ctypes.c_int, [P(_p.CParameters), _fp, _u32, _vp, _vp, _vp, _u32,
                                               P(_p.CRefinementParameters), _u32, _u32, P(_vp)]),
     "asph_simulation_destroy": (None, [_vp]),

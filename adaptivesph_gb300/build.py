@@ -19,9 +19,10 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libasph_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-CU_SOURCES = ["step_kernels.cu", "neighbor_kernels.cu", "refine_kernels.cu", "radix_sort.cu", "simulation.cu"]
+CU_SOURCES = ["step_kernels.cu", "neighbor_kernels.cu", "refine_kernels.cu", "radix_sort.cu", "boundary_kernels.cu",
+              "simulation.cu"]
 CPP_SOURCES = ["boundary_domain.cpp", "server.cpp"]
-HEADERS = ["asph_device.cuh", "asph_kernels.cuh", "asph_refine.cuh", "batch_internal.h"]
+HEADERS = ["asph_device.cuh", "asph_kernels.cuh", "asph_refine.cuh", "batch_internal.h", "boundary_internal.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -32,6 +32,8 @@ struct Request {
     uint32_t capacity = 0;
     float dt = 0.0f;
     uint32_t steps = 0;
+    float wall_spacing = 0.0f;   // > 0: walls generated on the GPU at admission
+    uint32_t wall_count = 0;     // their count (known at submission from the lattice loops)
     uint64_t bytes = 0;  // estimated device memory
 
     uint32_t state = ASPH_REQUEST_QUEUED;
@@ -80,10 +82,14 @@ void admit(asph_server* sv, Request* r) {
     r->t_admit = sv->now();
     asph_simulation* sim = nullptr;
     const uint32_t n = (uint32_t)(r->positions.size() / 4);
-    asph_status st = asph_simulation_create(&r->params, r->positions.data(), n, nullptr, nullptr,
-                                            r->boundary.empty() ? nullptr : r->boundary.data(),
-                                            (uint32_t)r->boundary.size(), r->adaptive ? &r->refine : nullptr,
-                                            r->capacity, (uint32_t)r->boundary.size(), &sim);
+    asph_status st =
+        r->wall_spacing > 0.0f
+            ? asph_simulation_create_with_walls(&r->params, r->positions.data(), n, nullptr, nullptr, r->wall_spacing,
+                                                r->adaptive ? &r->refine : nullptr, r->capacity, r->wall_count, &sim)
+            : asph_simulation_create(&r->params, r->positions.data(), n, nullptr, nullptr,
+                                     r->boundary.empty() ? nullptr : r->boundary.data(), (uint32_t)r->boundary.size(),
+                                     r->adaptive ? &r->refine : nullptr, r->capacity, (uint32_t)r->boundary.size(),
+                                     &sim);
     if (st == ASPH_OK) {
         r->graph = asph::scene_graph_new();
         if (!r->graph) st = ASPH_ERR_OUT_OF_MEMORY;
@@ -168,9 +174,17 @@ asph_status asph_server_submit(asph_server* sv, const asph_request* rq, uint64_t
     r->capacity = rq->max_fluid_capacity;
     r->dt = rq->delta_time;
     r->steps = rq->steps;
-    asph_status st = asph_estimate_device_bytes(&r->params, rq->count, rq->boundary_count,
-                                                r->adaptive ? &r->refine : nullptr, r->capacity, rq->boundary_count,
-                                                &r->bytes);
+    uint32_t nb = rq->boundary_count;
+    if (rq->boundary_count == 0 && rq->wall_spacing > 0.0f) {
+        r->wall_spacing = rq->wall_spacing;
+        asph_status sw = asph_boundary_generate_gpu(&rq->parameters.domain, rq->wall_spacing,
+                                                    rq->parameters.rest_density,
+                                                    rq->parameters.base_smoothing_radius, nullptr, 0, &r->wall_count);
+        if (sw != ASPH_OK) return sw;
+        nb = r->wall_count;
+    }
+    asph_status st = asph_estimate_device_bytes(&r->params, rq->count, nb, r->adaptive ? &r->refine : nullptr,
+                                                r->capacity, nb, &r->bytes);
     if (st != ASPH_OK) return st;
     std::lock_guard<std::mutex> g(sv->lock);
     if (r->bytes > sv->budget) return ASPH_ERR_CAPACITY;  // could never be admitted

@@ -20,6 +20,7 @@
 #include "asph_kernels.cuh"
 #include "asph_refine.cuh"
 #include "batch_internal.h"
+#include "boundary_internal.h"
 
 using namespace asph;
 
@@ -37,6 +38,11 @@ static asph_status cuda_fail(cudaError_t e, const char* what) {
     if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return ASPH_ERR_NO_DEVICE;
     return ASPH_ERR_CUDA;
 }
+
+namespace asph {
+asph_status report_error(asph_status s, const std::string& msg) { return fail(s, msg); }
+asph_status report_cuda_error(cudaError_t e, const char* what) { return cuda_fail(e, what); }
+}  // namespace asph
 
 #define CK(call)                                                   \
     do {                                                           \
@@ -440,9 +446,10 @@ asph_status alloc_cells(asph_simulation* s) {
     return ASPH_OK;
 }
 
-// Uploads the boundary particles, sorts them by sub-cell and builds their tables; also writes the caller's
-// imported boundary buffers in the caller's order (initializeBoundaryParticles, SphSimulation.cu:287-333).
-asph_status setup_boundary(asph_simulation* s, const asph_boundary_particle* b, uint32_t nb) {
+// Sorts the boundary particles (device arrays d_pos / d_psi, nb of them) by sub-cell and builds their tables; also
+// writes the caller's imported boundary buffers in the caller's order (initializeBoundaryParticles,
+// SphSimulation.cu:287-333).
+asph_status setup_boundary_device(asph_simulation* s, const float4* d_pos, const float* d_psi, uint32_t nb) {
     if (nb > s->bcap) {
         dfree(s->bpos);
         dfree(s->bfric);
@@ -466,22 +473,6 @@ asph_status setup_boundary(asph_simulation* s, const asph_boundary_particle* b, 
     CK(cudaMemsetAsync(s->brefflag, 0, refcells, s->stream));
     s->bex[0] = s->bex[1] = kNone;
     if (nb == 0) return ASPH_OK;
-    std::vector<float4> pos(nb);
-    std::vector<float> psi(nb);
-    for (uint32_t i = 0; i < nb; i++) {
-        pos[i] = make_float4(b[i].position[0], b[i].position[1], b[i].position[2], b[i].position[3]);
-        psi[i] = b[i].psi;
-    }
-    float4* d_pos = nullptr;
-    float* d_psi = nullptr;
-    asph_status st;
-    if ((st = dalloc(d_pos, nb)) != ASPH_OK) return st;
-    if ((st = dalloc(d_psi, nb)) != ASPH_OK) {
-        dfree(d_pos);
-        return st;
-    }
-    CK(cudaMemcpyAsync(d_pos, pos.data(), sizeof(float4) * nb, cudaMemcpyHostToDevice, s->stream));
-    CK(cudaMemcpyAsync(d_psi, psi.data(), sizeof(float) * nb, cudaMemcpyHostToDevice, s->stream));
     CK(cudaMemsetAsync(s->q3, 0xff, 2 * sizeof(unsigned long long), s->stream));
     k_boundary_keys<<<blocks_for(nb), 256, 0, s->stream>>>(s->grid, d_pos, nb, s->keys, s->vals, s->q3);
     CK_LAUNCH("k_boundary_keys");
@@ -501,8 +492,6 @@ asph_status setup_boundary(asph_simulation* s, const asph_boundary_particle* b, 
     CK(cudaStreamSynchronize(s->stream));
     s->bex[0] = s->h_ctr[0];
     s->bex[1] = s->h_ctr[1];
-    dfree(d_pos);
-    dfree(d_psi);
     if (s->have_bbuf) {
         std::vector<float4> colors(nb, make_float4(0.3f, 0.3f, 0.3f, 0.2f));
         std::vector<float> radii(nb, s->P.base_particle_radius);
@@ -510,7 +499,7 @@ asph_status setup_boundary(asph_simulation* s, const asph_boundary_particle* b, 
         const asph_memory* mr = s->bbuf.radii;
         const asph_memory* mc = s->bbuf.colors;
         if (mp && mp->size >= sizeof(float4) * nb)
-            CK(cudaMemcpyAsync(mp->ptr, pos.data(), sizeof(float4) * nb, cudaMemcpyHostToDevice, s->stream));
+            CK(cudaMemcpyAsync(mp->ptr, d_pos, sizeof(float4) * nb, cudaMemcpyDeviceToDevice, s->stream));
         if (mr && mr->size >= sizeof(float) * nb)
             CK(cudaMemcpyAsync(mr->ptr, radii.data(), sizeof(float) * nb, cudaMemcpyHostToDevice, s->stream));
         if (mc && mc->size >= sizeof(float4) * nb)
@@ -518,6 +507,33 @@ asph_status setup_boundary(asph_simulation* s, const asph_boundary_particle* b, 
         CK(cudaStreamSynchronize(s->stream));
     }
     return ASPH_OK;
+}
+
+// The same from host boundary particles (StaticBoundaryDomain::Particle, position + psi).
+asph_status setup_boundary(asph_simulation* s, const asph_boundary_particle* b, uint32_t nb) {
+    if (nb == 0) return setup_boundary_device(s, nullptr, nullptr, 0);
+    std::vector<float4> pos(nb);
+    std::vector<float> psi(nb);
+    for (uint32_t i = 0; i < nb; i++) {
+        pos[i] = make_float4(b[i].position[0], b[i].position[1], b[i].position[2], b[i].position[3]);
+        psi[i] = b[i].psi;
+    }
+    float4* d_pos = nullptr;
+    float* d_psi = nullptr;
+    asph_status st;
+    if ((st = dalloc(d_pos, nb)) != ASPH_OK) return st;
+    if ((st = dalloc(d_psi, nb)) != ASPH_OK) {
+        dfree(d_pos);
+        return st;
+    }
+    cudaError_t e = cudaMemcpyAsync(d_pos, pos.data(), sizeof(float4) * nb, cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_psi, psi.data(), sizeof(float) * nb, cudaMemcpyHostToDevice, s->stream);
+    st = e == cudaSuccess ? setup_boundary_device(s, d_pos, d_psi, nb) : cuda_fail(e, "boundary upload");
+    cudaStreamSynchronize(s->stream);
+    dfree(d_pos);
+    dfree(d_psi);
+    return st;
 }
 
 asph_status upload_count(asph_simulation* s) {
@@ -1099,18 +1115,25 @@ void asph_memory_release(asph_memory* mem) {
     delete mem;
 }
 
+}  // extern "C"
+
 // ---------------------------------------------------------------------------------------------- simulation
-asph_status asph_simulation_create(const asph_parameters* parameters, const float* positions, uint32_t count,
-                                   const asph_fluid_buffers* fluid_buffers,
-                                   const asph_boundary_buffers* boundary_buffers,
-                                   const asph_boundary_particle* boundary, uint32_t boundary_count,
-                                   const asph_refinement_parameters* refinement, uint32_t max_fluid_capacity,
-                                   uint32_t max_boundary_capacity, asph_simulation** out) {
-    API_ENTRY();
+// createSimulation; the boundary comes from host particles or, when `walls` is given, from walls generated on the
+// device (their count is walls->n; boundary / boundary_count are then unused).
+static asph_status create_impl(const asph_parameters* parameters, const float* positions, uint32_t count,
+                               const asph_fluid_buffers* fluid_buffers, const asph_boundary_buffers* boundary_buffers,
+                               const asph_boundary_particle* boundary, uint32_t boundary_count,
+                               const DeviceWalls* walls, const asph_refinement_parameters* refinement,
+                               uint32_t max_fluid_capacity, uint32_t max_boundary_capacity, asph_simulation** out) {
+    if (walls) {
+        boundary = nullptr;
+        boundary_count = walls->n;
+    }
     if (!parameters || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "parameters and out are required");
     *out = nullptr;
     if (count > 0 && !positions) return fail(ASPH_ERR_INVALID_ARGUMENT, "positions are required");
-    if (boundary_count > 0 && !boundary) return fail(ASPH_ERR_INVALID_ARGUMENT, "boundary particles are required");
+    if (boundary_count > 0 && !boundary && !walls)
+        return fail(ASPH_ERR_INVALID_ARGUMENT, "boundary particles are required");
     const asph_parameters& P = *parameters;
     if (!(P.base_smoothing_radius > 0.0f) || !(P.rest_density > 0.0f) || !(P.speed_of_sound > 0.0f) ||
         !(P.base_particle_mass > 0.0f))
@@ -1244,7 +1267,9 @@ asph_status asph_simulation_create(const asph_parameters* parameters, const floa
     }
     CK(cudaMemsetAsync(s->err, 0, sizeof(uint32_t), s->stream));
     s->bcap = 0;
-    TRY(setup_boundary(s, boundary, boundary_count));
+    TRY(walls ? setup_boundary_device(s, walls->pos, walls->psi, walls->n)
+              : setup_boundary(s, boundary, boundary_count));
+    if (walls) s->launches += walls->launches;
     if (count > 0) {
         float4* d_pos = nullptr;
         TRY(dalloc(d_pos, count));
@@ -1271,6 +1296,38 @@ asph_status asph_simulation_create(const asph_parameters* parameters, const floa
 #undef TRY
     *out = s;
     return ASPH_OK;
+}
+
+extern "C" {
+
+asph_status asph_simulation_create(const asph_parameters* parameters, const float* positions, uint32_t count,
+                                   const asph_fluid_buffers* fluid_buffers,
+                                   const asph_boundary_buffers* boundary_buffers,
+                                   const asph_boundary_particle* boundary, uint32_t boundary_count,
+                                   const asph_refinement_parameters* refinement, uint32_t max_fluid_capacity,
+                                   uint32_t max_boundary_capacity, asph_simulation** out) {
+    API_ENTRY();
+    return create_impl(parameters, positions, count, fluid_buffers, boundary_buffers, boundary, boundary_count,
+                       nullptr, refinement, max_fluid_capacity, max_boundary_capacity, out);
+}
+
+asph_status asph_simulation_create_with_walls(const asph_parameters* parameters, const float* positions,
+                                              uint32_t count, const asph_fluid_buffers* fluid_buffers,
+                                              const asph_boundary_buffers* boundary_buffers, float wall_spacing,
+                                              const asph_refinement_parameters* refinement,
+                                              uint32_t max_fluid_capacity, uint32_t max_boundary_capacity,
+                                              asph_simulation** out) {
+    API_ENTRY();
+    if (!parameters || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "parameters and out are required");
+    *out = nullptr;
+    DeviceWalls w;
+    asph_status st = generate_walls_device(parameters->domain, wall_spacing, parameters->rest_density,
+                                           parameters->base_smoothing_radius, nullptr, w);
+    if (st != ASPH_OK) return st;
+    st = create_impl(parameters, positions, count, fluid_buffers, boundary_buffers, nullptr, 0, &w, refinement,
+                     max_fluid_capacity, std::max(max_boundary_capacity, w.n), out);
+    free_walls(w);
+    return st;
 }
 
 void asph_simulation_destroy(asph_simulation* sim) { destroy(sim); }

@@ -252,6 +252,7 @@ class CRequest(ctypes.Structure):
         ("max_fluid_capacity", ctypes.c_uint32),
         ("delta_time", ctypes.c_float),
         ("steps", ctypes.c_uint32),
+        ("wall_spacing", ctypes.c_float),
     ]
 
 

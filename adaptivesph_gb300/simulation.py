@@ -110,17 +110,18 @@ class StaticBoundaryDomain:
 
     @staticmethod
     def generate(bounds: Domain, particle_spacing: float, fluid_rest_density: float,
-                 fluid_smoothing_radius: float) -> "StaticBoundaryDomain":
+                 fluid_smoothing_radius: float, device: bool = False) -> "StaticBoundaryDomain":
+        """StaticBoundaryDomain::generate; device=True runs it on the GPU (asph_boundary_generate_gpu, bit-identical
+        output)."""
         lib = _lib.load()
+        fn = lib.asph_boundary_generate_gpu if device else lib.asph_boundary_generate
         d = _p.to_c_domain(bounds)
         n = ctypes.c_uint32()
-        _lib.check(lib.asph_boundary_generate(ctypes.byref(d), particle_spacing, fluid_rest_density,
-                                              fluid_smoothing_radius, None, 0, ctypes.byref(n)),
-                   "StaticBoundaryDomain::generate")
+        _lib.check(fn(ctypes.byref(d), particle_spacing, fluid_rest_density, fluid_smoothing_radius, None, 0,
+                      ctypes.byref(n)), "StaticBoundaryDomain::generate")
         arr = (_p.CBoundaryParticle * max(n.value, 1))()
-        _lib.check(lib.asph_boundary_generate(ctypes.byref(d), particle_spacing, fluid_rest_density,
-                                              fluid_smoothing_radius, ctypes.cast(arr, _vp), n.value,
-                                              ctypes.byref(n)), "StaticBoundaryDomain::generate")
+        _lib.check(fn(ctypes.byref(d), particle_spacing, fluid_rest_density, fluid_smoothing_radius,
+                      ctypes.cast(arr, _vp), n.value, ctypes.byref(n)), "StaticBoundaryDomain::generate")
         raw = np.frombuffer(arr, dtype=np.float32).reshape(-1, 5)[: n.value]
         return StaticBoundaryDomain(bounds, raw[:, :4].copy(), raw[:, 4].copy())
 
@@ -384,6 +385,24 @@ def create_simulation(parameters: Parameters, positions: np.ndarray,
     return sim
 
 
+def create_simulation_with_walls(parameters: Parameters, positions: np.ndarray, wall_spacing: float,
+                                 refinement_params: Optional[RefinementParameters], max_fluid_particle_capacity: int,
+                                 max_boundary_particle_capacity: int = 0) -> Simulation:
+    """StaticBoundaryDomain::generate on the GPU followed by createSimulation (asph_simulation_create_with_walls):
+    the walls never pass through host memory and equal those of StaticBoundaryDomain.generate bit for bit."""
+    lib = _lib.load()
+    pos = np.ascontiguousarray(positions, np.float32).reshape(-1, 4)
+    cp = _p.to_c_parameters(parameters)
+    cr = _p.to_c_refinement(refinement_params) if refinement_params is not None else None
+    out = _vp()
+    _lib.check(lib.asph_simulation_create_with_walls(ctypes.byref(cp), _fp(pos), pos.shape[0], None, None,
+                                                     float(wall_spacing), ctypes.byref(cr) if cr is not None else None,
+                                                     int(max_fluid_particle_capacity),
+                                                     int(max_boundary_particle_capacity), ctypes.byref(out)),
+               "createSimulation (walls on the device)")
+    return Simulation(out.value, parameters, refinement_params)
+
+
 class Batch:
     """Independent simulations advanced together (asph_batch_*; no reference counterpart): their steps overlap on
     the device and plain steps replay CUDA graphs. Each simulation's result equals its result when stepped alone.
@@ -446,17 +465,18 @@ class Server:
                    "asph_server_create")
         self._h = h
 
-    def submit(self, parameters: Parameters, positions: np.ndarray, boundary: "StaticBoundaryDomain",
+    def submit(self, parameters: Parameters, positions: np.ndarray, boundary: Optional["StaticBoundaryDomain"],
                refinement: Optional[RefinementParameters], delta_time: float, steps: int,
-               max_fluid_capacity: Optional[int] = None) -> int:
+               max_fluid_capacity: Optional[int] = None, wall_spacing: float = 0.0) -> int:
+        """boundary None with wall_spacing > 0: the walls are generated on the GPU at admission."""
         pos = np.ascontiguousarray(positions, np.float32).reshape(-1, 4)
-        bp, nb = boundary.to_c()
+        bp, nb = boundary.to_c() if boundary is not None else (None, 0)
         cr = _p.to_c_refinement(refinement) if refinement is not None and refinement.enabled else None
         cap = max_fluid_capacity if max_fluid_capacity is not None else pos.shape[0]
         rq = _p.CRequest(_p.to_c_parameters(parameters), _fp(pos), pos.shape[0],
                          ctypes.cast(bp, ctypes.POINTER(_p.CBoundaryParticle)) if nb else None,
                          nb, ctypes.pointer(cr) if cr is not None else None, int(cap),
-                         float(delta_time), int(steps))
+                         float(delta_time), int(steps), float(wall_spacing))
         t = ctypes.c_uint64()
         _lib.check(self._lib.asph_server_submit(self._h, ctypes.byref(rq), ctypes.byref(t)), "asph_server_submit")
         return int(t.value)

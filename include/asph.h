@@ -194,6 +194,17 @@ asph_status asph_boundary_generate(const asph_domain* bounds,
                                    uint32_t capacity,
                                    uint32_t* count);
 
+/* StaticBoundaryDomain::generate on the GPU (StaticBoundaryDomain.cu:76-174 runs on the host in the reference):
+ * the same contract and bit-identical output as asph_boundary_generate (positions from the reference's float
+ * loops, psi summed in the same order); with out == NULL only *count is written (host arithmetic only). */
+asph_status asph_boundary_generate_gpu(const asph_domain* bounds,
+                                       float particle_spacing,
+                                       float fluid_rest_density,
+                                       float fluid_smoothing_radius,
+                                       asph_boundary_particle* out,
+                                       uint32_t capacity,
+                                       uint32_t* count);
+
 /* ---------------------------------------------------------------------------------------------
  * Simulation (cuda/include/cuda/simulation/Simulation.cuh:61-145)
  * ------------------------------------------------------------------------------------------- */
@@ -215,6 +226,21 @@ asph_status asph_simulation_create(const asph_parameters* parameters,
                                    uint32_t max_fluid_capacity,
                                    uint32_t max_boundary_capacity,
                                    asph_simulation** out);
+
+/* StaticBoundaryDomain::generate(domain, wall_spacing, rest_density, base_smoothing_radius) followed by
+ * createSimulation (app/App.cpp:144-172), with the walls generated on the device and handed to the simulation without
+ * a trip through host memory (no reference counterpart for the device path). The walls equal those of
+ * asph_boundary_generate bit for bit, so the simulation equals one created from them. */
+asph_status asph_simulation_create_with_walls(const asph_parameters* parameters,
+                                              const float* positions,
+                                              uint32_t count,
+                                              const asph_fluid_buffers* fluid_buffers,
+                                              const asph_boundary_buffers* boundary_buffers,
+                                              float wall_spacing,
+                                              const asph_refinement_parameters* refinement,
+                                              uint32_t max_fluid_capacity,
+                                              uint32_t max_boundary_capacity,
+                                              asph_simulation** out);
 
 /* Simulation::~Simulation */
 void asph_simulation_destroy(asph_simulation* sim);
@@ -446,6 +472,9 @@ typedef struct asph_request {
     uint32_t max_fluid_capacity;                  /* plain: at least count (adaptive: refinement->max_particle_count) */
     float delta_time;
     uint32_t steps;
+    /* > 0 with boundary_count == 0: walls of this spacing are generated on the GPU at admission
+     * (asph_simulation_create_with_walls) instead of being passed in */
+    float wall_spacing;
 } asph_request;
 
 #define ASPH_REQUEST_QUEUED 0u
