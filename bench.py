@@ -620,6 +620,107 @@ def run_served(args, rank: int, world: int, dist):
     }
 
 
+# ------------------------------------------------------------------------------------------------ conservation
+def _totals_row(sim, frame):
+    t = sim.totals()
+    return {"frame": frame, "count": t["count"], "mass": t["mass"], "momentum": list(t["momentum"]),
+            "kinetic_energy": t["kinetic_energy"]}
+
+
+def _conservation_run(sc, steps, every, adaptive):
+    """FP64 totals of one simulation every `every` steps over `steps` steps, with the refinement reports."""
+    import torch
+
+    from adaptivesph_gb300 import StaticBoundaryDomain, create_simulation
+
+    if sc.boundary_spacing > 0:
+        bd = StaticBoundaryDomain.generate(sc.parameters.domain, sc.boundary_spacing, sc.parameters.rest_density,
+                                           sc.parameters.base_smoothing_radius, device=True)
+    else:
+        bd = StaticBoundaryDomain.empty(sc.parameters.domain)
+    n0 = sc.positions.shape[0]
+    cap = sc.refinement.max_particle_count if adaptive else n0
+    sim = create_simulation(sc.parameters, sc.positions, None, None, bd, sc.refinement if adaptive else None, cap,
+                            max(bd.get_particle_count(), 1))
+    if sc.velocities is not None:
+        st = sim.read_state()
+        st["vel"] = sc.velocities.copy()
+        sim.write_state(st, next_id=n0)
+    rows = [_totals_row(sim, 0)]
+    refinements = []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(1, steps + 1):
+        sim.step_async(sc.dt)
+        if k % every == 0 or k == steps:
+            rows.append(_totals_row(sim, k))
+        if adaptive and (k - 1 == sc.refinement.initial_cooldown or
+                         (k - 1 > sc.refinement.initial_cooldown and (k - 1) % sc.refinement.cooldown == 0)):
+            r = sim.last_refinement()
+            refinements.append({"frame": r["frame"], "merge_pairs": r["merge_pairs"], "splits": r["splits"],
+                                "count_after": r["count_after"]})
+    sim.synchronize()
+    secs = time.perf_counter() - t0
+    errors = sim.device_errors()
+    sim.close()
+    return rows, refinements, secs, errors
+
+
+def _drift_summary(rows, refinements, sc, every):
+    m0 = rows[0]["mass"]
+    P0 = np.array(rows[0]["momentum"])
+    g = np.array(sc.parameters.gravity, np.float64)
+    out = {"mass_initial": m0, "mass_final": rows[-1]["mass"],
+           "mass_drift_rel": (rows[-1]["mass"] - m0) / m0,
+           "kinetic_energy_initial": rows[0]["kinetic_energy"], "kinetic_energy_final": rows[-1]["kinetic_energy"]}
+    splits = sum(r["splits"] for r in refinements)
+    if refinements:
+        # mass changes only where particles split (13 x 0.077 = 1.001 of the parent: +0.001 m_parent per split, the
+        # reference's mass ratios) and by the rounding of merged masses (m1 + m2 in FP32)
+        out["splits"] = splits
+        out["merges"] = sum(r["merge_pairs"] for r in refinements)
+        out["mass_gain_per_split_over_m0"] = ((rows[-1]["mass"] - m0) / splits / sc.parameters.base_particle_mass
+                                              if splits else None)
+        out["split_mass_ratio_excess"] = 13 * 0.077 - 1.0
+    # momentum minus the impulse of gravity on the whole mass: what walls and the domain clamp added (zero, to
+    # rounding, where nothing but pair forces act)
+    t_end = rows[-1]["frame"] * sc.dt
+    wall = np.array(rows[-1]["momentum"]) - P0 - g * m0 * t_end
+    out["momentum_minus_gravity_impulse_final"] = wall.tolist()
+    out["momentum_abs_max_over_run"] = float(max(np.abs(np.array(r["momentum"])).max() for r in rows))
+    return out
+
+
+def run_conservation(args, rank: int, world: int, dist):
+    """FP64 mass, momentum and kinetic energy over --drift-steps steps (default 10,000) of: the 1M adaptive dam break
+    (refinement on: mass changes only at split events, Q-7), the 128k plain dam break (refinement off: the mass is
+    constant) and a periodic Taylor-Green vortex at 64^3 (no gravity, no walls: momentum is conserved up to
+    rounding). Totals every --drift-every steps from fixed-order FP64 reductions on the device."""
+    import torch
+
+    from adaptivesph_gb300 import scenes
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    if rank != 0:
+        return None
+    cases = [("adaptive dam break 1M (100x200x50, dx=0.004 m), velocity criterion", c2_scene(args), True),
+             ("plain dam break 128k (40x80x40, dx=0.01 m)", scenes.c1_plain(), False),
+             ("periodic Taylor-Green vortex 64^3, Re=100, Morris viscosity", scenes.taylor_green(64), False)]
+    results = []
+    for name, sc, adaptive in cases:
+        rows, refs, secs, errors = _conservation_run(sc, args.drift_steps, args.drift_every, adaptive)
+        results.append({"case": name, "steps": args.drift_steps, "dt": sc.dt, "seconds": secs,
+                        "device_errors": errors, "summary": _drift_summary(rows, refs, sc, args.drift_every),
+                        "totals": rows, "refinements": refs})
+    line = {"metric": "FP64 conserved totals over 10k steps", "workload": "conservation",
+            "steps": args.drift_steps, "every": args.drift_every, "n_gpus": 1, "cases": results}
+    if args.out:
+        with open(args.out, "w") as f:
+            json.dump(line, f, indent=1)
+    return {k: v for k, v in line.items() if k != "cases"} | {
+        "cases": [{"case": r["case"], "seconds": r["seconds"], "summary": r["summary"]} for r in results]}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -634,7 +735,10 @@ def main():
                          "the neighbour-count deficit that splits at the free surface")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
-    ap.add_argument("--workload", choices=["adaptive1m", "batched", "served"], default="adaptive1m",
+    ap.add_argument("--drift-steps", type=int, default=10000, help="steps of the conservation workload")
+    ap.add_argument("--drift-every", type=int, default=100, help="steps between FP64 totals (conservation)")
+    ap.add_argument("--out", default="", help="conservation: write the full record (every totals row) to this file")
+    ap.add_argument("--workload", choices=["adaptive1m", "batched", "served", "conservation"], default="adaptive1m",
                     help="adaptive1m: the headline 1M adaptive dam break; batched: the scene mix through asph_batch; "
                          "served: Poisson scene requests through asph_server")
     ap.add_argument("--requests", type=int, default=24, help="requests of the served workload")
@@ -663,7 +767,8 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         tdist.init_process_group("nccl")
         dist = tdist
-    runners = {"batched": run_batched, "served": run_served, "adaptive1m": run_ours}
+    runners = {"batched": run_batched, "served": run_served, "adaptive1m": run_ours,
+               "conservation": run_conservation}
     line = runners[args.workload](args, rank, world, dist)
     if line is not None:
         print(json.dumps(line), flush=True)
