@@ -650,10 +650,12 @@ def _conservation_run(sc, steps, every, adaptive):
     refinements = []
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    rows[0]["seconds"] = 0.0
     for k in range(1, steps + 1):
         sim.step_async(sc.dt)
         if k % every == 0 or k == steps:
-            rows.append(_totals_row(sim, k))
+            rows.append(_totals_row(sim, k))  # the totals read drains the stream: the time is the steps' own
+            rows[-1]["seconds"] = time.perf_counter() - t0
         if adaptive and (k - 1 == sc.refinement.initial_cooldown or
                          (k - 1 > sc.refinement.initial_cooldown and (k - 1) % sc.refinement.cooldown == 0)):
             r = sim.last_refinement()
@@ -707,13 +709,16 @@ def run_conservation(args, rank: int, world: int, dist):
              ("plain dam break 128k (40x80x40, dx=0.01 m)", scenes.c1_plain(), False),
              ("periodic Taylor-Green vortex 64^3, Re=100, Morris viscosity", scenes.taylor_green(64), False)]
     results = []
+    sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    sampler.start()
     for name, sc, adaptive in cases:
         rows, refs, secs, errors = _conservation_run(sc, args.drift_steps, args.drift_every, adaptive)
         results.append({"case": name, "steps": args.drift_steps, "dt": sc.dt, "seconds": secs,
                         "device_errors": errors, "summary": _drift_summary(rows, refs, sc, args.drift_every),
                         "totals": rows, "refinements": refs})
+    clocks = sampler.stop()
     line = {"metric": "FP64 conserved totals over 10k steps", "workload": "conservation",
-            "steps": args.drift_steps, "every": args.drift_every, "n_gpus": 1, "cases": results}
+            "steps": args.drift_steps, "every": args.drift_every, "n_gpus": 1, "clocks": clocks, "cases": results}
     if args.out:
         with open(args.out, "w") as f:
             json.dump(line, f, indent=1)
