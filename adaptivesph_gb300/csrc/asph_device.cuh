@@ -217,12 +217,11 @@ __device__ __forceinline__ float gap1(float p, float lo, float w, float m) {
 // hold a member within reach of p is skipped: reach = Rfix when Rfix > 0, else 2 * (max h of the cell). Culling
 // never skips a member that passes a support test, so sums over the visited members are unchanged.
 // body(begin, end, shx, shy, shz) gets the member range and the periodic image offsets.
-// for_each_cell_coords also gives the body the sub-cell's coordinates before periodic wrapping (usx, usy, usz).
 template <bool kCull, class Body>
-__device__ __forceinline__ void for_each_cell_coords(const GridDev& g, const uint32_t* __restrict__ start,
-                                                     const uint32_t* __restrict__ end, const float* __restrict__ hmax,
-                                                     const float* __restrict__ hmax_ref, uint32_t ex0, uint32_t ex1,
-                                                     float px, float py, float pz, float R, float Rfix, Body&& body) {
+__device__ __forceinline__ void for_each_cell(const GridDev& g, const uint32_t* __restrict__ start,
+                                              const uint32_t* __restrict__ end, const float* __restrict__ hmax,
+                                              const float* __restrict__ hmax_ref, uint32_t ex0, uint32_t ex1,
+                                              float px, float py, float pz, float R, float Rfix, Body&& body) {
     int32_t lo[3], hi[3];
     const float p[3] = {px, py, pz};
     bool ok = true;
@@ -280,22 +279,11 @@ __device__ __forceinline__ void for_each_cell_coords(const GridDev& g, const uin
                                 const float dz = gap1(pz, g.dmin[2] + (float)sz * g.w[2] + shz, g.w[2], m);
                                 if (dx * dx + dy * dy + dz * dz > reach * reach) continue;
                             }
-                            body(b, __ldg(end + lin), shx, shy, shz, sx + 2 * (rx - cx), sy + 2 * (ry - cy),
-                                 sz + 2 * (rz - cz));
+                            body(b, __ldg(end + lin), shx, shy, shz);
                         }
             }
         }
     }
-}
-
-template <bool kCull, class Body>
-__device__ __forceinline__ void for_each_cell(const GridDev& g, const uint32_t* __restrict__ start,
-                                              const uint32_t* __restrict__ end, const float* __restrict__ hmax,
-                                              const float* __restrict__ hmax_ref, uint32_t ex0, uint32_t ex1,
-                                              float px, float py, float pz, float R, float Rfix, Body&& body) {
-    for_each_cell_coords<kCull>(g, start, end, hmax, hmax_ref, ex0, ex1, px, py, pz, R, Rfix,
-                                [&](uint32_t b, uint32_t e, float shx, float shy, float shz, int32_t, int32_t,
-                                    int32_t) { body(b, e, shx, shy, shz); });
 }
 
 // One query walked by a whole warp: the sub-cells of the box [x-R, x+R] are numbered in the canonical order,

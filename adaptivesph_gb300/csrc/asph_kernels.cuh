@@ -65,8 +65,6 @@ struct NbrDev {
     uint32_t* pool_cnt;
     uint32_t pool_slots;
     uint32_t maxe;
-    const uint32_t* tiles;  // first particle of every non-empty reference cell of the step (any order)
-    uint32_t* tiles_ctr;    // [0] number of tiles, [2] next tile to take (work counter of the force pass)
 };
 
 struct ReorderArgs {
@@ -84,8 +82,6 @@ struct ReorderArgs {
     float* hmax_ref;
     uint32_t* heavy;    // queue of heavy particles (query box > kHeavyCells reference cells)
     uint32_t* heavy_n;
-    uint32_t* tiles;    // first particle of every non-empty reference cell (density tiles); may be null
-    uint32_t* tiles_n;
 };
 
 __global__ void k_integrate_keys(StepArgs a, float dt, float pending_half, int has_pending, uint32_t* keys,
@@ -108,7 +104,7 @@ enum DensityKernel { kDensityOrdinary, kDensityHeavy, kDensityOverflow, kDensity
 // the step is replayed from a CUDA graph too.
 cudaError_t launch_density(DensityKernel kind, uint32_t blocks, cudaStream_t stream, int priority, StepArgs a,
                            CellsDev c, BoundaryDev b, NbrDev nl);
-enum ForceKernel { kForcesOrdinary, kForcesHeavy, kForcesRow, kForcesTiles };
+enum ForceKernel { kForcesOrdinary, kForcesHeavy, kForcesRow };
 cudaError_t launch_forces(ForceKernel kind, bool morris, uint32_t blocks, cudaStream_t stream, int priority, StepArgs a,
                           CellsDev c, BoundaryDev b, NbrDev nl);
 // number of reference cells of the query box [x - R, x + R] above which a particle is heavy

@@ -21,7 +21,6 @@
 // whole blocks.
 #include <utility>
 
-#include "../../include/asph.h"
 #include "asph_device.cuh"
 #include "asph_kernels.cuh"
 
@@ -226,9 +225,10 @@ __device__ __forceinline__ ForceCtx force_ctx(const StepArgs& a, uint32_t i) {
 
 // Pressure, viscosity and cohesion terms of fluid neighbour j (Algorithm.cu:56-221).
 template <bool kMorris, bool kSigma = true>
-__device__ __forceinline__ void force_term_vals(const StepArgs& a, const ForceCtx& c, float4 pj, float4 kj, float2 rpj,
-                                                float4 vj, float shx, float shy, float shz, ForceAcc& f) {
+__device__ __forceinline__ void force_term(const StepArgs& a, const ForceCtx& c, uint32_t j, float shx, float shy,
+                                           float shz, ForceAcc& f) {
     const bool periodic = a.grid.periodic;
+    const float4 pj = __ldg(a.ph + j);
     const float xj = periodic ? pj.x + shx : pj.x;
     const float yj = periodic ? pj.y + shy : pj.y;
     const float zj = periodic ? pj.z + shz : pj.z;
@@ -236,6 +236,8 @@ __device__ __forceinline__ void force_term_vals(const StepArgs& a, const ForceCt
     const float r2 = dist2(dx, dy, dz);
     const float twoh = pj.w + pj.w;
     if (r2 > twoh * twoh) return;
+    const float4 kj = __ldg(a.kc + j);
+    const float2 rpj = __ldg(a.rp + j);
     const float r = sqrtf(r2);
     float u[3];
     if (r > 0.0f) {
@@ -256,6 +258,7 @@ __device__ __forceinline__ void force_term_vals(const StepArgs& a, const ForceCt
         for (int q = 0; q < 3; q++) f.ap[q] = fmaf(-sp, u[q], f.ap[q]);
     }
     if (c.visc_on) {
+        const float4 vj = __ldg(a.vm + j);
         const float vd[3] = {c.vi.x - vj.x, c.vi.y - vj.y, c.vi.z - vj.z};
         const float rhoj = rpj.x;
         if (!kMorris) {
@@ -281,20 +284,19 @@ __device__ __forceinline__ void force_term_vals(const StepArgs& a, const ForceCt
     }
 }
 
-// force_term_vals with the neighbour's operands loaded from global memory.
-template <bool kMorris, bool kSigma = true>
-__device__ __forceinline__ void force_term(const StepArgs& a, const ForceCtx& c, uint32_t j, float shx, float shy,
-                                           float shz, ForceAcc& f) {
-    const float4 vj = c.visc_on ? __ldg(a.vm + j) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    force_term_vals<kMorris, kSigma>(a, c, __ldg(a.ph + j), __ldg(a.kc + j), __ldg(a.rp + j), vj, shx, shy, shz, f);
-}
-
 // force_term for two neighbours: the per-pair quantities in packed FP32x2 arithmetic (each half rounds as the
 // scalar operation; divisions and square roots stay scalar), each accumulator updated for j1, then j2.
 template <bool kMorris, bool kPeriodic, bool kSigma = true, bool kAccepted = false>
-__device__ __forceinline__ void force_pair_vals(const StepArgs& a, const ForceCtx& c, float4 p1, float4 k1, float2 rp1,
-                                                float4 v1, float s1x, float s1y, float s1z, float4 p2, float4 k2,
-                                                float2 rp2, float4 v2, float s2x, float s2y, float s2z, ForceAcc& f) {
+__device__ __forceinline__ void force_pair(const StepArgs& a, const ForceCtx& c, uint32_t j1, float s1x, float s1y,
+                                           float s1z, uint32_t j2, float s2x, float s2y, float s2z, ForceAcc& f) {
+    const float4 p1 = __ldg(a.ph + j1), p2 = __ldg(a.ph + j2);
+    const float4 k1 = __ldg(a.kc + j1), k2 = __ldg(a.kc + j2);
+    const float2 rp1 = __ldg(a.rp + j1), rp2 = __ldg(a.rp + j2);
+    float4 v1 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), v2 = v1;
+    if (c.visc_on) {
+        v1 = __ldg(a.vm + j1);
+        v2 = __ldg(a.vm + j2);
+    }
     float2 x = make_float2(p1.x, p2.x), y = make_float2(p1.y, p2.y), z = make_float2(p1.z, p2.z);
     if (kPeriodic) {
         x = __fadd2_rn(x, make_float2(s1x, s2x));
@@ -400,22 +402,6 @@ __device__ __forceinline__ void force_pair_vals(const StepArgs& a, const ForceCt
             f.as[2] = fmaf(ss, uz.y, f.as[2]);
         }
     }
-}
-
-// force_pair_vals with the neighbours' operands loaded from global memory.
-template <bool kMorris, bool kPeriodic, bool kSigma = true, bool kAccepted = false>
-__device__ __forceinline__ void force_pair(const StepArgs& a, const ForceCtx& c, uint32_t j1, float s1x, float s1y,
-                                           float s1z, uint32_t j2, float s2x, float s2y, float s2z, ForceAcc& f) {
-    const float4 p1 = __ldg(a.ph + j1), p2 = __ldg(a.ph + j2);
-    const float4 k1 = __ldg(a.kc + j1), k2 = __ldg(a.kc + j2);
-    const float2 rp1 = __ldg(a.rp + j1), rp2 = __ldg(a.rp + j2);
-    float4 v1 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), v2 = v1;
-    if (c.visc_on) {
-        v1 = __ldg(a.vm + j1);
-        v2 = __ldg(a.vm + j2);
-    }
-    force_pair_vals<kMorris, kPeriodic, kSigma, kAccepted>(a, c, p1, k1, rp1, v1, s1x, s1y, s1z, p2, k2, rp2, v2, s2x,
-                                                           s2y, s2z, f);
 }
 
 // Boundary pressure and friction (BoundaryAlgorithm.cu:53-162) over the cells of lane `lane`.
@@ -749,266 +735,6 @@ __global__ void __launch_bounds__(128, 7) k_density(StepArgs a, CellsDev c, Boun
     a.rp[i] = make_float2(rh, pressure_term(rh, a.phys.rho0, a.phys.B));
 }
 
-// ---------------------------------------------------------------------------------------------- tiles
-// A tile is one reference cell (2x2x2 sub-cells); the 4x4x4 sub-cells around it hold every neighbour its particles can
-// have unless merging grew smoothing lengths. The reorder pass lists the first particle of every non-empty reference
-// cell; persistent blocks take tiles from a device-side counter and stage the window's particle data in shared memory
-// by bulk copies (cp.async.bulk, one per sub-cell and array, completing on an mbarrier with a bounded wait).
-constexpr int kTileThreads = 160;
-constexpr int kTileWindow = 64;     // 4 x 4 x 4 sub-cells
-constexpr uint32_t kBulkSpins = 1u << 22;
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return done != 0u;
-}
-
-// bounded wait for the phase with the given parity; false when the limit ran out
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-    for (uint32_t k = 0; k < kBulkSpins; ++k)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
-}
-
-// global -> shared bulk copy of `bytes` (multiple of 16, both addresses 16-byte aligned), completing on `bar`
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
-}
-
-// orders this thread's earlier generic-proxy accesses of shared memory before its later bulk copies into it
-__device__ __forceinline__ void fence_proxy_async_smem() {
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
-// ------------------------------------------------------------------------------------------------ forces by tiles
-// The force pass of the ordinary particles by the same tiles: the window's positions, velocities and kernel constants
-// staged by bulk copies and the (density, pressure term) pairs by plain loads, in dynamic shared memory; each thread
-// then runs its row exactly as k_forces does (same pairs, same arithmetic, same order), reading a neighbour from the
-// window when its sub-cell is staged. Row entries never straddle sub-cells, so one lookup per entry (a binary search
-// of the staged sub-cells by first member) places all of its members.
-constexpr uint32_t kForceTileCap = 1152;  // staged members: 3 x 16 B + 8 B each, 64.5 KB
-constexpr size_t kForceTileSmem = (size_t)kForceTileCap * (3 * sizeof(float4) + sizeof(float2));
-
-template <bool kMorris, bool kSigma, bool kPeriodic>
-__global__ void __launch_bounds__(kTileThreads, 3) k_forces_tile(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
-    extern __shared__ __align__(16) unsigned char smem_dyn[];
-    float4* s_ph = reinterpret_cast<float4*>(smem_dyn);
-    float4* s_vm = s_ph + kForceTileCap;
-    float4* s_kc = s_vm + kForceTileCap;
-    float2* s_rp = reinterpret_cast<float2*>(s_kc + kForceTileCap);
-    __shared__ uint32_t s_start[kTileWindow], s_cnt[kTileWindow], s_off[kTileWindow];
-    __shared__ uint32_t s_sorted_start[kTileWindow], s_sorted_end[kTileWindow], s_sorted_off[kTileWindow];
-    __shared__ __align__(8) uint64_t s_bar;
-    __shared__ uint32_t s_item, s_first, s_last, s_failed, s_nslots;
-    __shared__ int32_t s_cell[3];
-    const GridDev& g = a.grid;
-    if (threadIdx.x == 0) {
-        mbar_init(&s_bar, 1u);
-        s_failed = 0u;
-        s_nslots = 0u;
-    }
-    __syncthreads();
-    const uint32_t ntiles = nl.tiles_ctr[0];
-    uint32_t parity = 0;
-    for (;;) {
-        if (threadIdx.x == 0) {
-            const uint32_t item = atomicAdd(nl.tiles_ctr + 2, 1u);
-            s_item = item;
-            if (item < ntiles) {
-                const uint32_t i0 = nl.tiles[item];
-                const float4 p = a.ph[i0];
-                uint32_t key, refkey;
-                cell_of(g, p.x, p.y, p.z, key, refkey);
-                s_cell[0] = (int32_t)(compact1by2(key) >> 1);
-                s_cell[1] = (int32_t)(compact1by2(key >> 1) >> 1);
-                s_cell[2] = (int32_t)(compact1by2(key >> 2) >> 1);
-                s_first = i0;
-            }
-        }
-        __syncthreads();
-        if (s_item >= ntiles) break;
-        const int32_t w0[3] = {2 * s_cell[0] - 1, 2 * s_cell[1] - 1, 2 * s_cell[2] - 1};
-        if (threadIdx.x < kTileWindow) {
-            const int w = threadIdx.x;
-            int32_t u[3] = {w0[0] + (w & 3), w0[1] + ((w >> 2) & 3), w0[2] + (w >> 4)};
-            bool ok = true;
-#pragma unroll
-            for (int q = 0; q < 3; q++) {
-                if (kPeriodic) {
-                    if (u[q] < 0) u[q] += g.sgs[q];
-                    else if (u[q] >= g.sgs[q]) u[q] -= g.sgs[q];
-                } else {
-                    ok &= u[q] >= 0 && u[q] < g.sgs[q];
-                }
-            }
-            uint32_t bgn = kEmpty, cnt = 0;
-            if (ok) {
-                const uint32_t lin = (uint32_t)u[0] + (uint32_t)g.sgs[0] * ((uint32_t)u[1] + (uint32_t)g.sgs[1] * (uint32_t)u[2]);
-                bgn = __ldg(c.start + lin);
-                if (bgn != kEmpty) cnt = __ldg(c.end + lin) - bgn;
-            }
-            s_start[w] = bgn;
-            s_cnt[w] = cnt;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            uint32_t off = 0, last = s_first;
-            for (int w = 0; w < kTileWindow; w++) {
-                const uint32_t n = s_cnt[w];
-                if (n > 0u && off + n <= kForceTileCap) {
-                    s_off[w] = off;
-                    off += n;
-                } else {
-                    s_off[w] = kEmpty;
-                }
-                const bool own = (unsigned)((w & 3) - 1) < 2u && (unsigned)(((w >> 2) & 3) - 1) < 2u &&
-                                 (unsigned)((w >> 4) - 1) < 2u;
-                if (own && n > 0u && s_start[w] + n > last) last = s_start[w] + n;
-            }
-            s_last = last;
-            mbar_arrive_expect_tx(&s_bar, off * 48u);
-        }
-        __syncthreads();
-        if (threadIdx.x < kTileWindow) {
-            const int w = threadIdx.x;
-            const uint32_t o = s_off[w];
-            // rank of this staged sub-cell among the staged ones by first member: the sorted list for lookups
-            if (o != kEmpty) {
-                uint32_t rank = 0;
-                for (int q = 0; q < kTileWindow; q++)
-                    rank += (s_off[q] != kEmpty && s_start[q] < s_start[w]) ? 1u : 0u;
-                s_sorted_start[rank] = s_start[w];
-                s_sorted_end[rank] = s_start[w] + s_cnt[w];
-                s_sorted_off[rank] = o;
-                fence_proxy_async_smem();
-                bulk_g2s(s_ph + o, a.ph + s_start[w], s_cnt[w] * 16u, &s_bar);
-                bulk_g2s(s_vm + o, a.vm + s_start[w], s_cnt[w] * 16u, &s_bar);
-                bulk_g2s(s_kc + o, a.kc + s_start[w], s_cnt[w] * 16u, &s_bar);
-            }
-            const unsigned staged = __ballot_sync(0xffffffffu, o != kEmpty);
-            if ((w & 31) == 0) atomicAdd(&s_nslots, (uint32_t)__popc(staged));
-        }
-        // the (density, pressure term) pairs: plain loads (their 8-byte rows need not start on 16 bytes)
-        for (int w = 0; w < kTileWindow; w++) {
-            const uint32_t o = s_off[w];
-            if (o == kEmpty) continue;
-            const uint32_t n = s_cnt[w], st = s_start[w];
-            for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) s_rp[o + k] = __ldg(a.rp + st + k);
-        }
-        if (!mbar_wait_bounded(&s_bar, parity)) atomicOr(&s_failed, 1u);
-        __syncthreads();
-        if (s_failed) {
-            if (threadIdx.x == 0) atomicOr(a.err, ASPH_DEVERR_SPIN_LIMIT);
-            mbar_wait_bounded(&s_bar, parity);
-            return;
-        }
-        parity ^= 1u;
-        const uint32_t nslots = s_nslots;
-        const uint32_t first_i = s_first, last_i = s_last;
-        for (uint32_t i = first_i + threadIdx.x; i < last_i; i += blockDim.x) {
-            const uint32_t cnt = nl.cnt[i];
-            if (cnt > kRowHeavy) continue;  // long row (k_forces_row), overflowed or heavy (k_forces_heavy)
-            const ForceCtx x = force_ctx(a, i);
-            ForceAcc f = {};
-            const uint2* row = nl.ent + (size_t)i * nl.maxe;
-            uint2 next = cnt > 0u ? __ldg(row) : make_uint2(0u, 0u);
-            uint32_t k = 1, first = 0, mask = 0;
-            float shx = 0.0f, shy = 0.0f, shz = 0.0f;
-            // operands of the current entry's members: staged (bias added to the member index) or global
-            bool staged = false;
-            uint32_t bias = 0;
-            auto pull = [&](uint32_t& j, float& sx, float& sy, float& sz, bool& from_smem) -> bool {
-                for (;;) {
-                    if (mask == 0u) {
-                        if (k > cnt) return false;
-                        decode_entry(g, next.x, first, shx, shy, shz);
-                        mask = next.y;
-                        if (k < cnt) next = __ldg(row + k);
-                        k++;
-                        // the staged sub-cell holding this entry's members, if any
-                        uint32_t lo = 0, hi = nslots;
-                        while (lo < hi) {
-                            const uint32_t mid = (lo + hi) >> 1;
-                            if (s_sorted_end[mid] <= first) lo = mid + 1;
-                            else hi = mid;
-                        }
-                        staged = lo < nslots && s_sorted_start[lo] <= first;
-                        bias = staged ? s_sorted_off[lo] - s_sorted_start[lo] : 0u;
-                    }
-                    j = first + (uint32_t)(__ffs(mask) - 1);
-                    mask &= mask - 1u;
-                    sx = shx;
-                    sy = shy;
-                    sz = shz;
-                    from_smem = staged;
-                    if (j != i) {
-                        if (staged) j += bias;
-                        return true;
-                    }
-                }
-            };
-            auto load = [&](uint32_t j, bool sm, float4& p, float4& kk, float2& rp, float4& v) {
-                if (sm) {
-                    p = s_ph[j];
-                    kk = s_kc[j];
-                    rp = s_rp[j];
-                    v = s_vm[j];
-                } else {
-                    p = __ldg(a.ph + j);
-                    kk = __ldg(a.kc + j);
-                    rp = __ldg(a.rp + j);
-                    v = __ldg(a.vm + j);
-                }
-            };
-            for (;;) {
-                uint32_t j1, j2;
-                float s1x, s1y, s1z, s2x, s2y, s2z;
-                bool m1, m2;
-                if (!pull(j1, s1x, s1y, s1z, m1)) break;
-                float4 p1, k1, v1, p2, k2, v2;
-                float2 r1, r2;
-                load(j1, m1, p1, k1, r1, v1);
-                if (!pull(j2, s2x, s2y, s2z, m2)) {
-                    force_term_vals<kMorris, kSigma>(a, x, p1, k1, r1, v1, s1x, s1y, s1z, f);
-                    break;
-                }
-                load(j2, m2, p2, k2, r2, v2);
-                force_pair_vals<kMorris, kPeriodic, kSigma, true>(a, x, p1, k1, r1, v1, s1x, s1y, s1z, p2, k2, r2, v2,
-                                                                  s2x, s2y, s2z, f);
-            }
-            const uint32_t bn = nl.bcnt[i];
-            if (bn == kBoundaryWalk)
-                boundary_forces<1>(a, b, i, x, f, 0);
-            else if (bn != 0u)
-                boundary_forces_rows(a, b, i, x, f, row + cnt, bn);
-            finish_force(a, i, x, f);
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) s_nslots = 0u;
-    }
-}
-
 // Density of the heavy particles: one warp per particle.
 __global__ void __launch_bounds__(128, 2) k_density_heavy(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl,
                                                           const uint32_t* queue, const uint32_t* queue_n, bool pooled) {
@@ -1276,48 +1002,11 @@ cudaError_t launch_density(DensityKernel kind, uint32_t blocks, cudaStream_t str
     return cudaGetLastError();
 }
 
-// The tiled force kernel: persistent blocks, as many as fit; 64.5 KB of dynamic shared memory each.
-template <bool kMorris, bool kSigma, bool kPeriodic>
-cudaError_t launch_forces_tile_v(cudaStream_t stream, StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
-    static int per_sm = 0, sms = 0;
-    auto kernel = k_forces_tile<kMorris, kSigma, kPeriodic>;
-    if (per_sm == 0) {
-        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kForceTileSmem);
-        if (e != cudaSuccess) return e;
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kTileThreads, kForceTileSmem);
-        if (per_sm < 1) per_sm = 1;
-    }
-    kernel<<<(uint32_t)(per_sm * (sms > 0 ? sms : 1)), kTileThreads, kForceTileSmem, stream>>>(a, c, b, nl);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_forces_tile(int variant, cudaStream_t stream, StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
-    switch (variant) {
-        case 0: return launch_forces_tile_v<false, false, false>(stream, a, c, b, nl);
-        case 1: return launch_forces_tile_v<false, false, true>(stream, a, c, b, nl);
-        case 2: return launch_forces_tile_v<false, true, false>(stream, a, c, b, nl);
-        case 3: return launch_forces_tile_v<false, true, true>(stream, a, c, b, nl);
-        case 4: return launch_forces_tile_v<true, false, false>(stream, a, c, b, nl);
-        case 5: return launch_forces_tile_v<true, false, true>(stream, a, c, b, nl);
-        case 6: return launch_forces_tile_v<true, true, false>(stream, a, c, b, nl);
-        default: return launch_forces_tile_v<true, true, true>(stream, a, c, b, nl);
-    }
-}
-
 cudaError_t launch_forces(ForceKernel kind, bool morris, uint32_t blocks, cudaStream_t stream, int priority, StepArgs a,
                           CellsDev c, BoundaryDev b, NbrDev nl) {
     if (kind == kForcesHeavy) {
         if (morris) return launch_with_priority(k_forces_heavy<true>, blocks, stream, priority, a, c, b, nl);
         return launch_with_priority(k_forces_heavy<false>, blocks, stream, priority, a, c, b, nl);
-    }
-    if (kind == kForcesTiles) {
-        const bool sigma = a.phys.sigma_on != 0;
-        const bool periodic = a.grid.periodic != 0;
-        const int variant = (morris ? 4 : 0) | (sigma ? 2 : 0) | (periodic ? 1 : 0);
-        return launch_forces_tile(variant, stream, a, c, b, nl);
     }
     if (kind == kForcesRow) {
         if (morris)

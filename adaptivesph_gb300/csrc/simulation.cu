@@ -172,8 +172,6 @@ struct asph_simulation {
     uint2* pool = nullptr;          // [pool_slots * 32 * kPoolLaneEntries] accepted blocks of heavy particles
     uint32_t* pool_cnt = nullptr;   // [pool_slots * 32]
     uint32_t pool_slots = 0;        // capacity / 128, clamped to [64, kPoolSlots]
-    uint32_t* tiles = nullptr;      // [cap] first particle of every non-empty reference cell (density tiles)
-    uint32_t* tiles_ctr = nullptr;  // [4] tile count, next tile of the density pass, of the force pass
     uint32_t* keys = nullptr;
     uint32_t* vals = nullptr;
     void* sort_mem = nullptr;
@@ -288,7 +286,7 @@ struct asph_simulation {
     NbrDev nbrs() const {
         return NbrDev{nbr_ent,      nbr_cnt,  heavy_idx,    heavy_n,  fheavy_idx,   fheavy_n,
                       dover_idx,    fheavy_n + 1, drow_idx, fheavy_n + 2, frow_idx, fheavy_n + 3,
-                      nbr_bcnt,     pool,     pool_cnt,     pool_slots,   kListEntries, tiles, tiles_ctr};
+                      nbr_bcnt,     pool,     pool_cnt,     pool_slots,   kListEntries};
     }
 
     BoundaryDev boundary() const {
@@ -360,7 +358,7 @@ uint64_t device_bytes_for(uint32_t C, uint32_t sort_items, uint32_t ncells, uint
     b += 2 * c * (sizeof(float4) * 3 + sizeof(float2) + sizeof(float) + sizeof(uint32_t));  // two buffer sets
     b += c * sizeof(float4) * 2;                                           // kernel constants, support operands
     b += c * kListEntries * sizeof(uint2) + c * sizeof(uint32_t) * 2;                      // rows and counts
-    b += c * sizeof(uint32_t) * 6 + sizeof(uint32_t) * 9;                                   // queues, tiles
+    b += c * sizeof(uint32_t) * 5 + sizeof(uint32_t) * 5;                                   // queues
     const uint64_t slots = std::min<uint32_t>(kPoolSlots, std::max<uint32_t>(64u, C / 128u));
     b += slots * 32 * (kPoolLaneEntries * sizeof(uint2) + sizeof(uint32_t));                // heavy pool
     b += (uint64_t)sort_items * sizeof(uint32_t) * 2 + sort_scratch_bytes(sort_items);      // sort
@@ -570,7 +568,6 @@ asph_status build_grid(asph_simulation* s, bool integrate, float dt, bool carry_
     CK(cudaMemsetAsync(s->cell_hmax, 0, sizeof(float) * s->grid.ncells, s->stream));
     CK(cudaMemsetAsync(s->hmax_ref, 0, sizeof(float) * s->refcells_alloc, s->stream));
     CK(cudaMemsetAsync(s->heavy_n, 0, sizeof(uint32_t), s->stream));
-    CK(cudaMemsetAsync(s->tiles_ctr, 0, 4 * sizeof(uint32_t), s->stream));
     k_excluded<<<1, 1, 0, s->stream>>>(s->q3, s->graph_mode ? s->d_count : nullptr, n, s->ex, s->grid.periodic);
     CK_LAUNCH("k_excluded");
     ReorderArgs r;
@@ -588,8 +585,6 @@ asph_status build_grid(asph_simulation* s, bool integrate, float dt, bool carry_
     r.hmax_ref = s->hmax_ref;
     r.heavy = s->heavy_idx;
     r.heavy_n = s->heavy_n;
-    r.tiles = s->tiles;
-    r.tiles_n = s->tiles_ctr;
     const int nxt = 1 - s->cur;
     StepArgs b = s->args(nxt);
     h = s->tic();
@@ -632,7 +627,7 @@ asph_status run_forces(asph_simulation* s) {
     CK(cudaStreamWaitEvent(s->aux, s->ev_main, 0));
     CK(launch_forces(kForcesHeavy, s->phys.morris != 0, heavy_blocks(s->span()), s->aux, s->heavy_priority, a, s->cells(), s->boundary(),
                      s->nbrs()));
-    CK(launch_forces(kForcesTiles, s->phys.morris != 0, blocks_for(s->span()), s->stream, 0, a, s->cells(), s->boundary(),
+    CK(launch_forces(kForcesOrdinary, s->phys.morris != 0, blocks_for(s->span()), s->stream, 0, a, s->cells(), s->boundary(),
                      s->nbrs()));
     CK(launch_forces(kForcesRow, s->phys.morris != 0, heavy_blocks(s->span()), s->stream, 0, a, s->cells(), s->boundary(),
                      s->nbrs()));
@@ -946,8 +941,6 @@ void destroy(asph_simulation* s) {
     dfree(s->dover_idx);
     dfree(s->drow_idx);
     dfree(s->frow_idx);
-    dfree(s->tiles);
-    dfree(s->tiles_ctr);
     dfree(s->pool);
     dfree(s->pool_cnt);
     dfree(s->keys);
@@ -1232,8 +1225,6 @@ static asph_status create_impl(const asph_parameters* parameters, const float* p
     TRY(dalloc(s->dover_idx, C));
     TRY(dalloc(s->drow_idx, C));
     TRY(dalloc(s->frow_idx, C));
-    TRY(dalloc(s->tiles, C));
-    TRY(dalloc(s->tiles_ctr, 4));
     s->pool_slots = std::min<uint32_t>(kPoolSlots, std::max<uint32_t>(64u, C / 128u));
     TRY(dalloc(s->pool, (size_t)s->pool_slots * 32 * kPoolLaneEntries));
     TRY(dalloc(s->pool_cnt, (size_t)s->pool_slots * 32));

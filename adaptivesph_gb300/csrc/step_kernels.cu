@@ -170,12 +170,7 @@ __global__ void __launch_bounds__(256) k_reorder_cells(StepArgs a, ReorderArgs r
     a.pq[k] = make_float4(ph.x, ph.y, ph.z, twoh * twoh);
     if (r.heavy != nullptr && box_cells(a.grid, ph, ph.w + ph.w) > kHeavyCells) r.heavy[atomicAdd(r.heavy_n, 1u)] = k;
     const uint32_t lin = lin_of_key(a.grid, key);
-    if (k == 0 || r.keys_sorted[k - 1] != key) {
-        r.start[lin] = k;
-        // the 8 sub-cells of a reference cell have consecutive Morton keys: key >> 3 is the reference cell's
-        if (r.tiles != nullptr && (k == 0 || (r.keys_sorted[k - 1] >> 3) != (key >> 3)))
-            r.tiles[atomicAdd(r.tiles_n, 1u)] = k;
-    }
+    if (k == 0 || r.keys_sorted[k - 1] != key) r.start[lin] = k;
     if (k + 1 == n || r.keys_sorted[k + 1] != key) r.end[lin] = k + 1;
     // max h of the cell: one atomic per run of equal keys within the warp
     const unsigned peers = __match_any_sync(__activemask(), key);
