@@ -44,8 +44,7 @@ DENSITY_BYTES_PER_PARTICLE = 28.0
 # cell tables 4, reorder 88, density 28, force 60)
 STEP_BYTES_PER_PARTICLE = 332.0
 L2_BYTES = 129e6
-LATE_FRAME = 150  # first frame of the late-frame leg
-LATE_STEPS = 20
+LATE_STEPS = 20  # frames timed by the late-frame leg
 
 
 def measured_peaks():
@@ -269,13 +268,14 @@ def run_ours(args, rank: int, world: int, dist):
     n_end = sim.get_fluid_particles_count()
     frame_end = args.warmup + args.steps
 
-    # ---------------- late frames: the same simulation continued, untimed, to frame LATE_FRAME (merged particles of
+    # ---------------- late frames: the same simulation continued, untimed, to frame --late-frame (merged particles of
     # several h0 exist from about frame 100 on), then LATE_STEPS frames timed like the main leg
     late = None
-    if not args.no_late and frame_end <= LATE_FRAME:
-        for _ in range(LATE_FRAME - frame_end):
+    if not args.no_late and frame_end <= args.late_frame:
+        for _ in range(args.late_frame - frame_end):
             sim.step_async(sc.dt)
         sim.synchronize()
+        sim.enable_timing(True)
         late_counts = []
         ls, le = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
@@ -287,12 +287,15 @@ def run_ours(args, rank: int, world: int, dist):
             le.record(stream)
         torch.cuda.synchronize()
         late_ms = ls.elapsed_time(le)
+        lkt = sim.kernel_times()
+        sim.enable_timing(False)
         late = {"value": float(sum(late_counts)) / (late_ms / 1e3), "unit": UNIT,
-                "ms_per_step": late_ms / LATE_STEPS, "frames": [LATE_FRAME, LATE_FRAME + LATE_STEPS - 1],
+                "ms_per_step": late_ms / LATE_STEPS, "frames": [args.late_frame, args.late_frame + LATE_STEPS - 1],
                 "particles": [late_counts[0], sim.get_fluid_particles_count()],
-                "what": "the same simulation continued untimed to frame 150, then 20 frames timed with the state "
-                        "resident (CUDA events on the simulation's stream); merged particles of several h0 make "
-                        "these frames the slower part of the 2000-step run"}
+                "kernel_ms": {k: {"total_ms": v[0], "launches": v[1]} for k, v in lkt.items()},
+                "what": f"the same simulation continued untimed to frame {args.late_frame}, then {LATE_STEPS} frames "
+                        "timed with the state resident (CUDA events on the simulation's stream); merged particles "
+                        "of several h0 make the later frames of the 2000-step run slower"}
         errors |= sim.device_errors()
     sim.close()
 
@@ -461,11 +464,14 @@ def run_batched(args, rank: int, world: int, dist):
     n_before = [s.get_fluid_particles_count() for s in sims]
     if dist is not None:
         dist.barrier()
+    sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    sampler.start()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     batch.step(dts, args.steps)
     torch.cuda.synchronize()
     batched_s = time.perf_counter() - t0
+    clocks = sampler.stop()
     n_after = [s.get_fluid_particles_count() for s in sims]
     work = float(sum(0.5 * (a + b) for a, b in zip(n_before, n_after))) * args.steps
     stats = batch.stats()
@@ -515,6 +521,7 @@ def run_batched(args, rank: int, world: int, dist):
                        "ms_per_step_p50": float(np.percentile(ps, 50)), "ms_per_step_p99": float(np.percentile(ps, 99))},
         "speedup_vs_sequential": value / seq,
         "batch": stats,
+        "clocks": clocks,
     }
 
 
@@ -529,22 +536,34 @@ def run_served(args, rank: int, world: int, dist):
     arrival order (first come first served, each alone through asph_simulation_update); latency = finish - arrival."""
     import torch
 
-    from adaptivesph_gb300 import Server, StaticBoundaryDomain, create_simulation, scenes
+    from adaptivesph_gb300 import Server, StaticBoundaryDomain, create_simulation_with_walls, scenes
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     reqs = scenes.served_requests(count=args.requests)
-    bds = [StaticBoundaryDomain.generate(sc.parameters.domain, sc.boundary_spacing, sc.parameters.rest_density,
-                                         sc.parameters.base_smoothing_radius) for sc, _ in reqs]
+    # wall generation per request: the host generator against the GPU one (the served path uses the GPU one at
+    # admission, the requests carry only their parameters and fluid positions)
+    host_walls_s, gpu_walls_s, wall_counts = [], [], []
+    for sc, _ in reqs:
+        wargs = (sc.parameters.domain, sc.boundary_spacing, sc.parameters.rest_density,
+                 sc.parameters.base_smoothing_radius)
+        t = time.perf_counter()
+        bd = StaticBoundaryDomain.generate(*wargs)
+        host_walls_s.append(time.perf_counter() - t)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        StaticBoundaryDomain.generate(*wargs, device=True)
+        gpu_walls_s.append(time.perf_counter() - t)
+        wall_counts.append(bd.get_particle_count())
     work = float(sum(sc.positions.shape[0] * steps for sc, steps in reqs))
     budget = int(args.budget_gb * 1e9)
-    # sequential: every request alone, its service time measured; queueing follows from the arrival times
+    # sequential: every request alone (walls generated on the GPU), its service time measured; queueing follows from
+    # the arrival times
     service = []
-    for (sc, steps), bd in zip(reqs, bds):
+    for sc, steps in reqs:
         cap = sc.refinement.max_particle_count if sc.refinement else sc.positions.shape[0]
         torch.cuda.synchronize()
         t = time.perf_counter()
-        sim = create_simulation(sc.parameters, sc.positions, None, None, bd, sc.refinement, cap,
-                                bd.get_particle_count())
+        sim = create_simulation_with_walls(sc.parameters, sc.positions, sc.boundary_spacing, sc.refinement, cap)
         for _ in range(steps):
             sim.update(sc.dt)
         sim.export_host()
@@ -552,6 +571,8 @@ def run_served(args, rank: int, world: int, dist):
         sim.close()
     rng = np.random.default_rng(5)
     results = []
+    sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    sampler.start()
     for rate in args.rates:
         arrivals = np.cumsum(rng.exponential(1.0 / rate, size=len(reqs)))
         # sequential first come first served
@@ -569,8 +590,9 @@ def run_served(args, rank: int, world: int, dist):
             now = time.perf_counter() - t0
             while nxt < len(reqs) and arrivals[nxt] <= now:
                 sc, steps = reqs[nxt]
-                tickets.append(server.submit(sc.parameters, sc.positions, bds[nxt], sc.refinement, sc.dt, steps,
-                                             sc.refinement.max_particle_count if sc.refinement else None))
+                tickets.append(server.submit(sc.parameters, sc.positions, None, sc.refinement, sc.dt, steps,
+                                             sc.refinement.max_particle_count if sc.refinement else None,
+                                             wall_spacing=sc.boundary_spacing))
                 nxt += 1
             left = server.poll(args.poll_steps)
             if left == 0:
@@ -596,6 +618,7 @@ def run_served(args, rank: int, world: int, dist):
                            "latency_s": {"p50": _pct(seq_lat, 50), "p95": _pct(seq_lat, 95),
                                          "p99": _pct(seq_lat, 99)}},
         })
+    clocks = sampler.stop()
     if rank != 0:
         return None
     best = max(r["served"]["particle_steps_per_s"] for r in results)
@@ -617,6 +640,11 @@ def run_served(args, rank: int, world: int, dist):
                    "poll_steps": args.poll_steps, "parallelism": f"replicas x{world}"},
         "speedup_vs_sequential": best / seq_best,
         "rates": results,
+        "walls_per_request": {"particles_mean": float(np.mean(wall_counts)),
+                              "host_s_mean": float(np.mean(host_walls_s)), "gpu_s_mean": float(np.mean(gpu_walls_s)),
+                              "what": "StaticBoundaryDomain::generate per request: host threads against the GPU "
+                                      "kernels (bit-identical walls); the served and sequential runs use the GPU"},
+        "clocks": clocks,
     }
 
 
@@ -735,6 +763,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=10, help="steps of the CPU baseline sample in the GPU arm")
     ap.add_argument("--ref-steps", type=int, default=40, help="most steps the reference arm times")
     ap.add_argument("--no-late", action="store_true", help="skip the late-frame leg")
+    ap.add_argument("--late-frame", type=int, default=150, help="first frame of the late-frame leg")
     ap.add_argument("--criterion", choices=["velocity", "free_surface"], default="velocity",
                     help="split/merge criterion of the 1M adaptive dam break: the reference's velocity criterion, or "
                          "the neighbour-count deficit that splits at the free surface")
