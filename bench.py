@@ -56,14 +56,14 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes per particle of one density launch from the committed ncu summary, if present."""
+def profiled_density():
+    """DRAM bytes per particle and pipe utilisation of one density launch from the committed ncu record, if
+    present (an empty dict otherwise)."""
     p = os.path.join(ROOT, "profiles", "density_traffic.json")
     if os.path.exists(p):
         with open(p) as f:
-            d = json.load(f)
-        return float(d["dram_bytes_per_particle"]), d.get("source", "")
-    return None, None
+            return json.load(f)
+    return {}
 
 
 # ------------------------------------------------------------------------------------------------ clocks
@@ -342,7 +342,8 @@ def run_ours(args, rank: int, world: int, dist):
     mean_n = particle_steps / max(args.steps, 1)
     peak, peak_kind = measured_peaks()
     achieved = DENSITY_BYTES_PER_PARTICLE * mean_n / (avg_density_ms * 1e-3) / 1e9
-    traffic_pp, traffic_src = profiled_traffic()
+    prof = profiled_density()
+    traffic_pp = prof.get("dram_bytes_per_particle")
     line = {
         "metric": METRIC,
         "value": value,
@@ -371,9 +372,14 @@ def run_ours(args, rank: int, world: int, dist):
             "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
             "algorithmic_bytes_per_particle": DENSITY_BYTES_PER_PARTICLE,
             "avg_launch_ms": avg_density_ms,
-            "traffic_source": traffic_src,
-            "note": "the density pass is bound by instruction issue in its candidate scan (57% of issue slots busy, "
-                    "1-3% of DRAM peak in the ncu capture), not by HBM; the HBM fraction is small by construction",
+            "traffic_source": prof.get("source"),
+            "limiter": "instruction issue",
+            "issue": {"issue_slots_busy": prof.get("issue_slots_busy"), "fma_pipe": prof.get("fma_pipe"),
+                      "alu_pipe": prof.get("alu_pipe"), "dram_throughput": prof.get("dram_throughput"),
+                      "source": "the same ncu capture as traffic"},
+            "note": "the density pass is bound by instruction issue in its candidate scan (issue slots and the "
+                    "FMA/ALU pipes above, a few % of DRAM peak), not by HBM; the HBM fraction is small by "
+                    "construction (28 algorithmic bytes per particle against ~1 us of scan work)",
         },
         "step_roofline": {
             "achieved": STEP_BYTES_PER_PARTICLE * value / 1e9,
