@@ -45,6 +45,7 @@ DENSITY_BYTES_PER_PARTICLE = 28.0
 STEP_BYTES_PER_PARTICLE = 332.0
 L2_BYTES = 129e6
 LATE_STEPS = 20  # frames timed by the late-frame leg
+PLAIN_WARMUP = 3  # untimed frames before the plain legs (ours and the reference's CUDA step)
 
 
 def measured_peaks():
@@ -299,6 +300,33 @@ def run_ours(args, rank: int, world: int, dist):
         errors |= sim.device_errors()
     sim.close()
 
+    # ---------------- plain form: the same 1M scene without refinement, frames PLAIN_WARMUP .. PLAIN_WARMUP + K - 1
+    # from the lattice, timed like the main leg; the reference arm times the reference's own CUDA step on the same
+    # frames (its GPU leg), so the two plain numbers compare like for like
+    plain = None
+    if args.plain_steps > 0:
+        simp = create_simulation(sc.parameters, sc.positions, None, None, bd, None, n0, bd.get_particle_count())
+        simp.set_stream(stream.cuda_stream)
+        for _ in range(PLAIN_WARMUP):
+            simp.step_async(sc.dt)
+        simp.synchronize()
+        ps, pe = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            ps.record(stream)
+            for _ in range(args.plain_steps):
+                simp.step_async(sc.dt)
+            pe.record(stream)
+        torch.cuda.synchronize()
+        plain_ms = ps.elapsed_time(pe)
+        errors |= simp.device_errors()
+        plain = {"value": n0 * args.plain_steps / (plain_ms / 1e3), "unit": UNIT,
+                 "ms_per_step": plain_ms / args.plain_steps, "steps": args.plain_steps,
+                 "frames": [PLAIN_WARMUP, PLAIN_WARMUP + args.plain_steps - 1], "particles": n0,
+                 "what": "the same 1M-particle dam break and walls without refinement (the reference's plain "
+                         "SphSimulation step), state resident, CUDA events on the simulation's stream"}
+        simp.close()
+
     # ---------------- end to end through the C ABI with host buffers: the simulation is created from host arrays
     # inside the timed region and every frame's result is exported to pinned host memory; it covers frames
     # 0 .. warmup + steps - 1 (the device-resident run times frames warmup .. warmup + steps - 1)
@@ -399,6 +427,8 @@ def run_ours(args, rank: int, world: int, dist):
     }
     if late is not None:
         line["late"] = late
+    if plain is not None:
+        line["plain"] = plain
     if not args.no_cpu:
         cps, cores, secs, (f0, f1) = cpu_throughput(args, args.cpu_steps, 1)
         line["cpu_baseline"] = {"value": cps, "unit": UNIT, "cores": cores, "kind": "port",
@@ -418,11 +448,12 @@ def run_reference(args, rank: int, world: int):
     import adaptivesph_gb300._lib as product_lib
 
     steps = min(args.steps, args.ref_steps)
-    sc, bpos, _ = build_scene_cpu(args)
+    sc, bpos, bpsi = build_scene_cpu(args)
     cps, cores, secs, (f0, f1) = cpu_throughput(args, steps, args.warmup)
+    ref_gpu = reference_cuda_leg(args, sc, bpos, bpsi) if args.plain_steps > 0 else None
     if product_lib._lib is not None:
         raise RuntimeError("the reference arm must not load the CUDA library")
-    return {
+    line = {
         "impl": "reference",
         "metric": METRIC,
         "value": cps,
@@ -443,6 +474,53 @@ def run_reference(args, rank: int, world: int):
                                    f"untimed), {secs:.1f} s: the oracle's FP64 step (the reference has no CPU path)"},
         "e2e": {"value": cps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if ref_gpu is not None:
+        line["reference_cuda"] = ref_gpu
+    return line
+
+
+def reference_cuda_leg(args, sc, bpos, bpsi):
+    """The reference's own CUDA step on this GPU (oracle/ref_cuda.py: its kernels compiled from its sources for
+    sm_103a, launched in SphSimulation::update's order with its block size and its device synchronisation after
+    every step) on the plain form of the 1M-particle dam break, frames PLAIN_WARMUP .. PLAIN_WARMUP + K - 1: what
+    the GPU arm's `plain` leg is compared with. The reference's refinement pass is not run on the GPU (its in-place
+    compaction races)."""
+    from oracle import ref_cuda
+
+    if not ref_cuda.available():
+        return {"unavailable": "the reference's kernels are built into oracle/_ref where the reference checkout is "
+                               "present, and none were found"}
+    import torch
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    r = ref_cuda.RefCudaSim(sc.parameters, sc.positions, bpos, bpsi)
+    for _ in range(PLAIN_WARMUP):
+        r.step(sc.dt)
+    steps = args.plain_steps
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    sampler = ClockSampler(dev)
+    sampler.start()
+    torch.cuda.synchronize()
+    s.record()
+    for _ in range(steps):
+        r.step(sc.dt)  # ends with the device synchronisation the reference's update() ends with
+    e.record()
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = s.elapsed_time(e)
+    n = r.n
+    rho = r.rho[:n].float()
+    ok = bool(torch.isfinite(rho).all().item())
+    r.close()
+    return {"value": n * steps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps, "steps": steps,
+            "frames": [PLAIN_WARMUP, PLAIN_WARMUP + steps - 1], "particles": n, "boundary_particles": int(bpos.shape[0]),
+            "densities_finite": ok, "clocks": clocks,
+            "what": "the reference's own kernels (cubins built from its sources, C++20, --expt-relaxed-constexpr, "
+                    "ptxas -O3, default FMA contraction) run in SphSimulation::update's order on the plain form of "
+                    "the 1M-particle dam break (no refinement), 256-thread blocks, a device synchronisation after "
+                    "every step; thrust::sort_by_key of the cell indices replaced by torch.sort (both CUB radix "
+                    "sorts); CUDA events around the timed steps"}
 
 
 # ------------------------------------------------------------------------------------------------ batched mix
@@ -773,6 +851,8 @@ def main():
     ap.add_argument("--criterion", choices=["velocity", "free_surface"], default="velocity",
                     help="split/merge criterion of the 1M adaptive dam break: the reference's velocity criterion, or "
                          "the neighbour-count deficit that splits at the free surface")
+    ap.add_argument("--plain-steps", type=int, default=20,
+                    help="frames of the plain-form legs (ours, and the reference's CUDA step in the reference arm)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--drift-steps", type=int, default=10000, help="steps of the conservation workload")
