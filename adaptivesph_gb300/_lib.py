@@ -27,7 +27,8 @@ STATUS_NAMES = {
 }
 
 STAGE_INTEGRATE, STAGE_GRID, STAGE_DENSITY, STAGE_FORCES, STAGE_ALL = 1, 2, 3, 4, 5
-KERNEL_CLASSES = ("integrate", "sort", "reorder", "density", "forces", "refine")
+KERNEL_CLASSES = ("integrate", "sort", "reorder", "density", "forces", "refine", "refine_merge_select",
+                  "refine_merge", "refine_compact", "refine_split_select", "refine_split")
 
 DEVERR_SPIN_LIMIT = 0x1
 DEVERR_NONFINITE = 0x2

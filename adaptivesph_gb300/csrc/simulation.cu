@@ -703,6 +703,7 @@ asph_status refine_enqueue(asph_simulation* s) {
     StepArgs a = s->args(s->cur);
     const uint32_t nbk = blocks_for(n);
     // merge selection
+    int hp = s->tic();
     k_merge_score<<<nbk, 256, 0, s->stream>>>(a, s->cells(), r);
     k_merge_limits<<<1, 1, 0, s->stream>>>(r, n);
     k_select_ids<<<nbk, 256, 0, s->stream>>>(a, s->ctr + kCtrSortN, s->keys, s->vals);
@@ -712,14 +713,18 @@ asph_status refine_enqueue(asph_simulation* s) {
                                     s->stream);
     k_select_scores<<<nbk, 256, 0, s->stream>>>(s->score, s->ctr + kCtrSortN, 0, s->vals, s->keys);
     s->launches += 1 + radix_sort_pairs(s->keys, s->vals, s->ctr + kCtrSortN, n, 32, s->ss, s->err, s->stream);
+    s->toc(hp, ASPH_KERNEL_REFINE_MERGE_SELECT);
     // candidates, pairs + merges
+    hp = s->tic();
     k_cand_init<<<nbk, 256, 0, s->stream>>>(r, n);
     k_mark_eligible<<<nbk, 256, 0, s->stream>>>(r, s->vals);
     k_merge_candidates<<<nbk, 256, 0, s->stream>>>(a, s->cells(), r);
     k_merge_candidates_heavy<<<heavy_blocks(n), 256, 0, s->stream>>>(a, s->cells(), r);
     k_merge_pairs<<<nbk, 256, 0, s->stream>>>(a, r);
     CK_LAUNCH("merge");
+    s->toc(hp, ASPH_KERNEL_REFINE_MERGE);
     // stable compaction into the other buffer set (also carries the cell keys for a split pass that walks cells)
+    hp = s->tic();
     k_compact_count<<<nbk, 256, 0, s->stream>>>(s->flag, n, s->block_counts);
     k_compact_scan<<<1, 1024, 0, s->stream>>>(s->block_counts, nbk, n, r);
     const int nxt = 1 - s->cur;
@@ -738,7 +743,9 @@ asph_status refine_enqueue(asph_simulation* s) {
         k_cells_only<<<nbk, 256, 0, s->stream>>>(s->grid, keys_c, s->ctr + kCtrCount2, s->cell_start, s->cell_end);
         s->launches++;
     }
+    s->toc(hp, ASPH_KERNEL_REFINE_COMPACT);
     // split selection (skipped on the device when nothing was removed)
+    hp = s->tic();
     k_split_score<<<nbk, 256, 0, s->stream>>>(c, s->cells(), r);
     k_split_limits<<<1, 1, 0, s->stream>>>(r, s->cap, s->tpb);
     k_select_ids<<<nbk, 256, 0, s->stream>>>(c, s->ctr + kCtrSortN, s->keys, s->vals);
@@ -748,12 +755,15 @@ asph_status refine_enqueue(asph_simulation* s) {
                                     s->stream);
     k_select_scores<<<nbk, 256, 0, s->stream>>>(s->score, s->ctr + kCtrSortN, 1, s->vals, s->keys);
     s->launches += 1 + radix_sort_pairs(s->keys, s->vals, s->ctr + kCtrSortN, n, 32, s->ss, s->err, s->stream);
+    s->toc(hp, ASPH_KERNEL_REFINE_SPLIT_SELECT);
+    hp = s->tic();
     k_split_apply<<<nbk, 256, 0, s->stream>>>(c, r, s->vals);
     k_refine_finish<<<1, 1, 0, s->stream>>>(r);
     CK_LAUNCH("split");
     s->launches += 2;
     CK(cudaMemcpyAsync(s->d_count, s->ctr + kCtrCountOut, sizeof(uint32_t), cudaMemcpyDeviceToDevice, s->stream));
     CK(cudaMemcpyAsync(s->h_ctr, s->ctr, sizeof(uint32_t) * kCtrNum, cudaMemcpyDeviceToHost, s->stream));
+    s->toc(hp, ASPH_KERNEL_REFINE_SPLIT);
     s->toc(h, ASPH_KERNEL_REFINE);
     CK(cudaEventRecord(s->ev_refine, s->stream));
     s->refine_pending = true;

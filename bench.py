@@ -250,11 +250,13 @@ def run_ours(args, rank: int, world: int, dist):
         dist.barrier()
     torch.cuda.synchronize()
     with torch.cuda.stream(stream):
+        torch.cuda.nvtx.range_push("timed")  # NVTX ranges let a profiler capture just these frames
         start.record(stream)
         for _ in range(args.steps):
             counts.append(sim.get_fluid_particles_count())
             sim.step_async(sc.dt)
         end.record(stream)
+        torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     if dist is not None:
         dist.barrier()
@@ -281,11 +283,13 @@ def run_ours(args, rank: int, world: int, dist):
         ls, le = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         with torch.cuda.stream(stream):
+            torch.cuda.nvtx.range_push("late")
             ls.record(stream)
             for _ in range(LATE_STEPS):
                 late_counts.append(sim.get_fluid_particles_count())
                 sim.step_async(sc.dt)
             le.record(stream)
+            torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize()
         late_ms = ls.elapsed_time(le)
         lkt = sim.kernel_times()

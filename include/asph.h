@@ -414,7 +414,14 @@ asph_status asph_simulation_last_refinement(asph_simulation* sim, asph_refinemen
 #define ASPH_KERNEL_DENSITY 3u
 #define ASPH_KERNEL_FORCES 4u
 #define ASPH_KERNEL_REFINE 5u
-#define ASPH_KERNEL_COUNT 6u
+/* the phases of a refinement pass (each also inside ASPH_KERNEL_REFINE): merge scores and their selection sorts;
+ * candidates, pairing and merges; compaction; split scores and their selection sorts; splits and the read-back */
+#define ASPH_KERNEL_REFINE_MERGE_SELECT 6u
+#define ASPH_KERNEL_REFINE_MERGE 7u
+#define ASPH_KERNEL_REFINE_COMPACT 8u
+#define ASPH_KERNEL_REFINE_SPLIT_SELECT 9u
+#define ASPH_KERNEL_REFINE_SPLIT 10u
+#define ASPH_KERNEL_COUNT 11u
 asph_status asph_simulation_enable_timing(asph_simulation* sim, int enable);
 /* ms[k]: summed event time of kernel class k since enabling; launches[k]: launches timed. Drains the stream. */
 asph_status asph_simulation_kernel_times(asph_simulation* sim, double* ms, uint32_t* launches, uint32_t n);

@@ -83,7 +83,7 @@ def needs_build() -> bool:
     if not os.path.exists(LIB):
         return True
     t = os.path.getmtime(LIB)
-    return any(os.path.getmtime(f) > t for f in _sources() + OWN_HEADERS)
+    return any(os.path.getmtime(f) > t for f in _sources() + OWN_HEADERS + [__file__])
 
 
 def _compile(src: str) -> str:
@@ -105,7 +105,9 @@ def build(force: bool = False):
     with cf.ThreadPoolExecutor(max_workers=len(_sources())) as ex:
         objs = list(ex.map(_compile, _sources()))
     tmp = LIB + ".tmp"
-    r = subprocess.run([os.environ.get("CXX", "g++"), "-shared", "-fopenmp", "-o", tmp, *objs],
+    # -Bsymbolic: the library's own CUDA runtime stand-ins (cudaMalloc, cudaMemcpy, ...) must bind inside it even
+    # when a process has already loaded the real CUDA runtime globally (torch does), which would otherwise interpose
+    r = subprocess.run([os.environ.get("CXX", "g++"), "-shared", "-fopenmp", "-Wl,-Bsymbolic", "-o", tmp, *objs],
                        capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr[-4000:]}")
