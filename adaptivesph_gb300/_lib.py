@@ -106,6 +106,8 @@ SIGNATURES = {
     "asph_batch_destroy": (None, [_vp]),
     "asph_batch_step": (ctypes.c_int, [_vp, _fp, _u32]),
     "asph_batch_stats": (ctypes.c_int, [_vp, P(ctypes.c_uint64), P(ctypes.c_uint64), P(ctypes.c_uint64)]),
+    "asph_batch_set_mode": (ctypes.c_int, [_vp, _u32]),
+    "asph_batch_tuning": (ctypes.c_int, [_vp, _vp]),
     "asph_grid_sort_noalloc": (ctypes.c_int, [P(_p.CParameters), _vp, _u32, _vp, _vp, _vp, _vp, _u32, _vp, _vp]),
     "asph_abi_version": (ctypes.c_uint32, []),
     "asph_status_string": (ctypes.c_char_p, [ctypes.c_int]),

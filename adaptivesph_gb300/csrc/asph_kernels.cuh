@@ -109,6 +109,35 @@ cudaError_t launch_forces(ForceKernel kind, bool morris, uint32_t blocks, cudaSt
                           CellsDev c, BoundaryDev b, NbrDev nl);
 // number of reference cells of the query box [x - R, x + R] above which a particle is heavy
 constexpr int kHeavyCells = 27;
+
+// Segmented passes: one launch runs a density or force pass for up to kSegScenes simulations (the scenes of a
+// batch), from a table of their argument blocks passed by value (the launch's parameter space, read through the
+// constant cache). The ordinary kernels walk a queue of work items, an item being kSegItem consecutive particles of
+// one scene (items numbered scene by scene: item_start[k] .. item_start[k + 1] - 1 for scene k), each CTA taking
+// `chunk` consecutive items per turn, round robin (persistent when the grid is smaller than the queue); the warp
+// kernels stride over each scene's queue in turn. Every particle is summed by the same device code as in the
+// single-simulation kernels, so results are the same bit for bit.
+constexpr uint32_t kSegScenes = 64;
+constexpr uint32_t kSegItem = 128;
+struct SegScene {
+    StepArgs a;
+    CellsDev c;
+    BoundaryDev b;
+    NbrDev nl;
+};
+struct SegLaunch {
+    uint32_t nscenes;
+    uint32_t total_items;
+    uint32_t chunk;
+    uint32_t pad;
+    uint32_t item_start[kSegScenes + 1];
+    SegScene sc[kSegScenes];
+};
+enum SegPass { kSegDensity, kSegDensityHeavy, kSegDensityOverflow, kSegDensityRow, kSegForces, kSegForcesHeavy,
+               kSegForcesRow };
+// ctas: CTAs of the launch; variant flags as for the single kernels
+cudaError_t launch_segmented(SegPass pass, const SegLaunch& L, uint32_t ctas, cudaStream_t stream, int priority,
+                             bool periodic, bool morris, bool sigma);
 __global__ void k_neighbor_counts(StepArgs a, CellsDev c, uint32_t* counts, unsigned long long* total);
 __global__ void k_export(StepArgs a, float pending_half, int has_pending, float4* pos_out, float4* vel_out,
                          float* rho_out, float* rad_out, uint32_t* id_out);

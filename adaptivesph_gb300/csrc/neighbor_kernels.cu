@@ -613,9 +613,12 @@ __device__ __forceinline__ void boundary_forces_rows(const StepArgs& a, const Bo
 }
 
 // Density pass, ordinary particles; heavy particles are queued for k_density_heavy.
+// The bodies of the neighbour kernels are device functions so that the per-simulation kernels and the segmented
+// (multi-scene) kernels run the same code: particle i (ordinary), or the queued particle of warp item w (heavy,
+// long row). The warp-level parts need all 32 lanes of a warp to enter together.
 template <bool kPeriodic>
-__global__ void __launch_bounds__(128, 7) k_density(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void density_ordinary(const StepArgs& a, const CellsDev& c, const BoundaryDev& b,
+                                                 const NbrDev& nl, const uint32_t i) {
     const bool in = i < count_of(a);
     const float4 pi = in ? a.ph[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const float R = pi.w + pi.w;
@@ -735,16 +738,17 @@ __global__ void __launch_bounds__(128, 7) k_density(StepArgs a, CellsDev c, Boun
     a.rp[i] = make_float2(rh, pressure_term(rh, a.phys.rho0, a.phys.B));
 }
 
-// Density of the heavy particles: one warp per particle.
-__global__ void __launch_bounds__(128, 2) k_density_heavy(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl,
-                                                          const uint32_t* queue, const uint32_t* queue_n, bool pooled) {
-    const int lane = threadIdx.x & 31;
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t nh = *queue_n;
+template <bool kPeriodic>
+__global__ void __launch_bounds__(128, 7) k_density(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
+    density_ordinary<kPeriodic>(a, c, b, nl, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// Density of one heavy particle (queue position w, particle i) by one warp.
+__device__ __forceinline__ void density_heavy_item(const StepArgs& a, const CellsDev& c, const BoundaryDev& b,
+                                                   const NbrDev& nl, const uint32_t w, const uint32_t i,
+                                                   const bool pooled, const int lane) {
     const bool periodic = a.grid.periodic;
-    for (uint32_t w = warp; w < nh; w += nwarps) {
-        const uint32_t i = queue[w];
+    {
         const float4 pi = a.ph[i];
         const float R = pi.w + pi.w;
         const bool keep = pooled && w < nl.pool_slots;
@@ -789,11 +793,21 @@ __global__ void __launch_bounds__(128, 2) k_density_heavy(StepArgs a, CellsDev c
     }
 }
 
+// Density of the heavy particles: one warp per particle.
+__global__ void __launch_bounds__(128, 2) k_density_heavy(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl,
+                                                          const uint32_t* queue, const uint32_t* queue_n, bool pooled) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t nh = *queue_n;
+    for (uint32_t w = warp; w < nh; w += nwarps) density_heavy_item(a, c, b, nl, w, queue[w], pooled, lane);
+}
+
 // Force pass, ordinary particles: walks the particle's neighbour list. Heavy particles and particles whose row
 // overflowed are left to k_forces_heavy.
 template <bool kMorris, bool kSigma>
-__global__ void __launch_bounds__(128, 7) k_forces(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void forces_ordinary(const StepArgs& a, const CellsDev& c, const BoundaryDev& b,
+                                                const NbrDev& nl, const uint32_t i) {
     if (i >= count_of(a)) return;
     const uint32_t cnt = nl.cnt[i];
     if (cnt > kRowHeavy) return;  // long row (k_forces_row), overflowed or heavy (k_forces_heavy)
@@ -845,15 +859,16 @@ __global__ void __launch_bounds__(128, 7) k_forces(StepArgs a, CellsDev c, Bound
     finish_force(a, i, x, f);
 }
 
-// Forces of the heavy particles: one warp per particle.
+template <bool kMorris, bool kSigma>
+__global__ void __launch_bounds__(128, 7) k_forces(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
+    forces_ordinary<kMorris, kSigma>(a, c, b, nl, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// Forces of one heavy particle (force-queue particle i) by one warp.
 template <bool kMorris>
-__global__ void __launch_bounds__(128, 2) k_forces_heavy(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
-    const int lane = threadIdx.x & 31;
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t nh = *nl.fheavy_n;
-    for (uint32_t w = warp; w < nh; w += nwarps) {
-        const uint32_t i = nl.fheavy[w];
+__device__ __forceinline__ void forces_heavy_item(const StepArgs& a, const CellsDev& c, const BoundaryDev& b,
+                                                  const NbrDev& nl, const uint32_t i, const int lane) {
+    {
         const ForceCtx x = force_ctx(a, i);
         ForceAcc f = {};
         const uint32_t cnt = nl.cnt[i];
@@ -895,16 +910,22 @@ __global__ void __launch_bounds__(128, 2) k_forces_heavy(StepArgs a, CellsDev c,
     }
 }
 
-// Particles with long rows (kRowHeavy < cnt <= maxe): one warp per particle, row entry e on lane e mod 32, each
-// lane expanding its entries' masks in order; lane sums combined by the butterfly.
-
-__global__ void __launch_bounds__(128, 4) k_density_row(StepArgs a, BoundaryDev b, NbrDev nl) {
+// Forces of the heavy particles: one warp per particle.
+template <bool kMorris>
+__global__ void __launch_bounds__(128, 2) k_forces_heavy(StepArgs a, CellsDev c, BoundaryDev b, NbrDev nl) {
     const int lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t nq = *nl.drow_n;
-    for (uint32_t w = warp; w < nq; w += nwarps) {
-        const uint32_t i = nl.drow[w];
+    const uint32_t nh = *nl.fheavy_n;
+    for (uint32_t w = warp; w < nh; w += nwarps) forces_heavy_item<kMorris>(a, c, b, nl, nl.fheavy[w], lane);
+}
+
+// Particles with long rows (kRowHeavy < cnt <= maxe): one warp per particle, row entry e on lane e mod 32, each
+// lane expanding its entries' masks in order; lane sums combined by the butterfly.
+
+__device__ __forceinline__ void density_row_item(const StepArgs& a, const BoundaryDev& b, const NbrDev& nl,
+                                                 const uint32_t i, const int lane) {
+    {
         const float4 pi = a.ph[i];
         const uint32_t cnt = nl.cnt[i];
         const uint2* row = nl.ent + (size_t)i * nl.maxe;
@@ -920,7 +941,6 @@ __global__ void __launch_bounds__(128, 4) k_density_row(StepArgs a, BoundaryDev 
             }
         }
         rho = warp_sum_butterfly(rho);
-        const float R = pi.w + pi.w;
         float rb = 0.0f;
         if (b.n != 0) rb = warp_sum_butterfly(boundary_density<32>(a, b, i, pi, lane));
         if (lane == 0) {
@@ -932,14 +952,18 @@ __global__ void __launch_bounds__(128, 4) k_density_row(StepArgs a, BoundaryDev 
     }
 }
 
-template <bool kMorris>
-__global__ void __launch_bounds__(128, 4) k_forces_row(StepArgs a, BoundaryDev b, NbrDev nl) {
+__global__ void __launch_bounds__(128, 4) k_density_row(StepArgs a, BoundaryDev b, NbrDev nl) {
     const int lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t nq = *nl.frow_n;
-    for (uint32_t w = warp; w < nq; w += nwarps) {
-        const uint32_t i = nl.frow[w];
+    const uint32_t nq = *nl.drow_n;
+    for (uint32_t w = warp; w < nq; w += nwarps) density_row_item(a, b, nl, nl.drow[w], lane);
+}
+
+template <bool kMorris>
+__device__ __forceinline__ void forces_row_item(const StepArgs& a, const BoundaryDev& b, const NbrDev& nl,
+                                                const uint32_t i, const int lane) {
+    {
         const ForceCtx x = force_ctx(a, i);
         const uint32_t cnt = nl.cnt[i];
         const uint2* row = nl.ent + (size_t)i * nl.maxe;
@@ -965,6 +989,107 @@ __global__ void __launch_bounds__(128, 4) k_forces_row(StepArgs a, BoundaryDev b
         }
         if (lane == 0) finish_force(a, i, x, f);
     }
+}
+
+template <bool kMorris>
+__global__ void __launch_bounds__(128, 4) k_forces_row(StepArgs a, BoundaryDev b, NbrDev nl) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t nq = *nl.frow_n;
+    for (uint32_t w = warp; w < nq; w += nwarps) forces_row_item<kMorris>(a, b, nl, nl.frow[w], lane);
+}
+
+// ------------------------------------------------------------------ segmented (multi-scene) passes
+static_assert(sizeof(SegLaunch) <= 32000, "segmented launch table must fit the kernel parameter space");
+
+// Scene of work item `it`: the last k with item_start[k] <= it (uniform over the CTA).
+__device__ __forceinline__ uint32_t seg_scene_of(const SegLaunch& L, uint32_t it) {
+    uint32_t lo = 0, hi = L.nscenes - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (L.item_start[mid] <= it)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+// Persistent loop of the ordinary segmented kernels: CTA b takes `chunk` consecutive work items at a time, turn by
+// turn (items b*chunk .., then (b + gridDim.x)*chunk .., the queue walked round robin, items scene by scene);
+// body(scene, i) for every particle slot of an item. The item, and so
+// the scene, follows from blockIdx alone, which keeps the scene's argument blocks warp-uniform: the compiler reads
+// them into uniform registers as it does a kernel's own arguments.
+template <class Body>
+__device__ __forceinline__ void seg_items(const SegLaunch& L, Body&& body) {
+    for (uint32_t base = blockIdx.x * L.chunk; base < L.total_items; base += gridDim.x * L.chunk) {
+        const uint32_t end = base + L.chunk < L.total_items ? base + L.chunk : L.total_items;
+        for (uint32_t it = base; it < end; ++it) {
+            const uint32_t k = seg_scene_of(L, it);
+            body(L.sc[k], (it - L.item_start[k]) * kSegItem + threadIdx.x);
+        }
+    }
+}
+
+// Loop of the warp segmented kernels over the scenes: body(scene).
+template <class Body>
+__device__ __forceinline__ void seg_scenes(const SegLaunch& L, Body&& body) {
+    for (uint32_t k = 0; k < L.nscenes; ++k) body(L.sc[k]);
+}
+
+template <bool kPeriodic>
+__global__ void __launch_bounds__(128, 7) k_density_seg(const __grid_constant__ SegLaunch L) {
+    seg_items(L, [&](const SegScene& S, uint32_t i) { density_ordinary<kPeriodic>(S.a, S.c, S.b, S.nl, i); });
+}
+
+template <bool kMorris, bool kSigma>
+__global__ void __launch_bounds__(128, 6) k_forces_seg(const __grid_constant__ SegLaunch L) {
+    seg_items(L, [&](const SegScene& S, uint32_t i) { forces_ordinary<kMorris, kSigma>(S.a, S.c, S.b, S.nl, i); });
+}
+
+// Warp kernels: every warp strides over scene 0's queue, then scene 1's, and so on.
+__global__ void __launch_bounds__(128, 2) k_density_heavy_seg(const __grid_constant__ SegLaunch L, int overflow) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    seg_scenes(L, [&](const SegScene& S) {
+        const uint32_t* q = overflow ? S.nl.dover : S.nl.heavy;
+        const uint32_t nh = *(overflow ? S.nl.dover_n : S.nl.heavy_n);
+        for (uint32_t w = warp; w < nh; w += nwarps) density_heavy_item(S.a, S.c, S.b, S.nl, w, q[w], !overflow, lane);
+    });
+}
+
+__global__ void __launch_bounds__(128, 4) k_density_row_seg(const __grid_constant__ SegLaunch L) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    seg_scenes(L, [&](const SegScene& S) {
+        const uint32_t nq = *S.nl.drow_n;
+        for (uint32_t w = warp; w < nq; w += nwarps) density_row_item(S.a, S.b, S.nl, S.nl.drow[w], lane);
+    });
+}
+
+template <bool kMorris>
+__global__ void __launch_bounds__(128, 2) k_forces_heavy_seg(const __grid_constant__ SegLaunch L) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    seg_scenes(L, [&](const SegScene& S) {
+        const uint32_t nh = *S.nl.fheavy_n;
+        for (uint32_t w = warp; w < nh; w += nwarps) forces_heavy_item<kMorris>(S.a, S.c, S.b, S.nl, S.nl.fheavy[w], lane);
+    });
+}
+
+template <bool kMorris>
+__global__ void __launch_bounds__(128, 4) k_forces_row_seg(const __grid_constant__ SegLaunch L) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    seg_scenes(L, [&](const SegScene& S) {
+        const uint32_t nq = *S.nl.frow_n;
+        for (uint32_t w = warp; w < nq; w += nwarps) forces_row_item<kMorris>(S.a, S.b, S.nl, S.nl.frow[w], lane);
+    });
 }
 
 // The ordinary and the box-heavy kernels of a pass are independent of each other (the heavy queue is filled by the
@@ -1030,6 +1155,43 @@ cudaError_t launch_forces(ForceKernel kind, bool morris, uint32_t blocks, cudaSt
 }
 
 // Per-particle neighbour counts (sumAllNeighbors, cuda/src/algorithm/Algorithm.cu:234-268).
+cudaError_t launch_segmented(SegPass pass, const SegLaunch& L, uint32_t ctas, cudaStream_t stream, int priority,
+                             bool periodic, bool morris, bool sigma) {
+    if (L.nscenes == 0) return cudaSuccess;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(ctas);
+    cfg.blockDim = dim3(128);
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributePriority;
+    attr[0].val.priority = priority;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    switch (pass) {
+        case kSegDensity:
+            return periodic ? cudaLaunchKernelEx(&cfg, k_density_seg<true>, L) : cudaLaunchKernelEx(&cfg, k_density_seg<false>, L);
+        case kSegDensityHeavy:
+            return cudaLaunchKernelEx(&cfg, k_density_heavy_seg, L, 0);
+        case kSegDensityOverflow:
+            return cudaLaunchKernelEx(&cfg, k_density_heavy_seg, L, 1);
+        case kSegDensityRow:
+            return cudaLaunchKernelEx(&cfg, k_density_row_seg, L);
+        case kSegForces:
+            if (morris)
+                return sigma ? cudaLaunchKernelEx(&cfg, k_forces_seg<true, true>, L)
+                             : cudaLaunchKernelEx(&cfg, k_forces_seg<true, false>, L);
+            return sigma ? cudaLaunchKernelEx(&cfg, k_forces_seg<false, true>, L)
+                         : cudaLaunchKernelEx(&cfg, k_forces_seg<false, false>, L);
+        case kSegForcesHeavy:
+            return morris ? cudaLaunchKernelEx(&cfg, k_forces_heavy_seg<true>, L)
+                          : cudaLaunchKernelEx(&cfg, k_forces_heavy_seg<false>, L);
+        case kSegForcesRow:
+            return morris ? cudaLaunchKernelEx(&cfg, k_forces_row_seg<true>, L)
+                          : cudaLaunchKernelEx(&cfg, k_forces_row_seg<false>, L);
+    }
+    return cudaErrorInvalidValue;
+}
+
 __global__ void __launch_bounds__(256, 4) k_neighbor_counts(StepArgs a, CellsDev c, uint32_t* counts,
                                                          unsigned long long* total) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;

@@ -8,8 +8,10 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <chrono>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -261,6 +263,8 @@ struct asph_simulation {
     // bumped by every call that changes what a captured step holds by value or by pointer (grid, cell and boundary
     // tables, parameters, particle arrays); a batch's cached graphs are recaptured when it changes
     uint64_t generation = 0;
+    // unique over the process's simulations (a recycled address never matches an earlier simulation's graphs)
+    uint64_t serial = 0;
     uint32_t span() const { return graph_mode ? grid_n : n; }
 
     StepArgs args(int s) const {
@@ -1130,6 +1134,29 @@ void asph_memory_release(asph_memory* mem) {
 // ---------------------------------------------------------------------------------------------- simulation
 // createSimulation; the boundary comes from host particles or, when `walls` is given, from walls generated on the
 // device (their count is walls->n; boundary / boundary_count are then unused).
+// With the CUDA runtime's lazy loading (the default), a kernel is loaded at its first launch, which then waits for
+// the load; the refinement and read-out kernels first run many frames into a simulation, inside its step loop.
+// They are loaded once per process when the first simulation is created instead.
+static void preload_kernels() {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        const void* kernels[] = {
+            (const void*)k_merge_score,    (const void*)k_split_score,      (const void*)k_select_ids,
+            (const void*)k_select_scores,  (const void*)k_merge_limits,     (const void*)k_cand_init,
+            (const void*)k_mark_eligible,  (const void*)k_merge_candidates, (const void*)k_merge_candidates_heavy,
+            (const void*)k_merge_pairs,    (const void*)k_compact_count,    (const void*)k_compact_scan,
+            (const void*)k_compact_scatter, (const void*)k_split_limits,    (const void*)k_split_apply,
+            (const void*)k_refine_finish,  (const void*)k_cells_only,       (const void*)k_export,
+            (const void*)k_totals,         (const void*)k_density_info,     (const void*)k_reduce_rows,
+            (const void*)k_neighbor_counts};
+        for (const void* k : kernels) {
+            cudaFuncAttributes attr;
+            (void)cudaFuncGetAttributes(&attr, k);
+        }
+        (void)cudaGetLastError();
+    });
+}
+
 static asph_status create_impl(const asph_parameters* parameters, const float* positions, uint32_t count,
                                const asph_fluid_buffers* fluid_buffers, const asph_boundary_buffers* boundary_buffers,
                                const asph_boundary_particle* boundary, uint32_t boundary_count,
@@ -1142,6 +1169,7 @@ static asph_status create_impl(const asph_parameters* parameters, const float* p
     if (!parameters || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "parameters and out are required");
     *out = nullptr;
     if (count > 0 && !positions) return fail(ASPH_ERR_INVALID_ARGUMENT, "positions are required");
+    preload_kernels();
     if (boundary_count > 0 && !boundary && !walls)
         return fail(ASPH_ERR_INVALID_ARGUMENT, "boundary particles are required");
     const asph_parameters& P = *parameters;
@@ -1167,6 +1195,8 @@ static asph_status create_impl(const asph_parameters* parameters, const float* p
     if (P.boundary_mode == ASPH_BOUNDARY_PERIODIC && cap >= (1u << 27))
         return fail(ASPH_ERR_UNSUPPORTED, "a periodic box holds at most 2^27 - 1 particles");
     asph_simulation* s = new (std::nothrow) asph_simulation;
+    static std::atomic<uint64_t> next_serial{1};
+    if (s) s->serial = next_serial.fetch_add(1);
     if (!s) return fail(ASPH_ERR_OUT_OF_MEMORY, "host allocation failed");
     s->P = P;
     if (adaptive) s->R = *refinement;
@@ -2129,10 +2159,454 @@ asph_status advance_scenes(asph_simulation* const* sims, SceneGraph* const* grap
 
 }  // namespace asph
 
+// ------------------------------------------------------------------------------------------------ segmented batches
+// A batch step in which the plain-stepping scenes of a size bucket run their density and force passes as segmented
+// launches: each scene's integrate, sort and reorder on its own stream, then one launch per pass for up to
+// kSegScenes scenes (persistent ordinary kernels walking a queue of 128-particle work items round robin, warp kernels
+// striding over each scene's heavy and long-row queues), instead of one launch per pass and scene. The whole step
+// (forks and joins included) is captured as one CUDA graph keyed by every member's step inputs and replayed.
+// Scenes that refine this frame, take their first step, or sit in a bucket the tuner gave per-scene graphs step
+// as in advance_scenes. Results equal the per-scene path's bit for bit: every particle is summed by the same device
+// code. The autotuner times the choices (per bucket: segmented or per-scene graphs; work items per CTA turn;
+// persistent CTAs per SM or one CTA per turn's items) over the batch's first plain frames and keeps the fastest.
+namespace {
+
+constexpr uint32_t kBuckets = 3;  // particle counts below 16k, below 64k, and above
+uint32_t bucket_of(uint32_t n) { return n < 16384u ? 0u : (n < 65536u ? 1u : 2u); }
+
+struct SegConfig {
+    uint8_t segmented[kBuckets] = {1, 1, 1};
+    uint32_t chunk = 1;       // consecutive work items per CTA turn
+    uint32_t ctas_per_sm = 7; // CTAs of the ordinary kernels per SM (persistent loop); 0: one per `chunk` items
+    bool operator==(const SegConfig& o) const {
+        return std::memcmp(segmented, o.segmented, sizeof(segmented)) == 0 && chunk == o.chunk &&
+               ctas_per_sm == o.ctas_per_sm;
+    }
+};
+
+struct SegGraph {
+    std::vector<uint64_t> key;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<uint64_t> member_launches;
+    uint64_t last_use = 0;
+};
+
+constexpr size_t kSegGraphCache = 8;
+
+}  // namespace
+
+struct SegEngine {
+    cudaStream_t main = nullptr, aux = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_mid = nullptr, ev_aux = nullptr, ev_done = nullptr;
+    std::vector<cudaEvent_t> ev_member;
+    std::vector<SegGraph> cache;
+    uint64_t clock = 0;
+    int priority_hi = 0;
+    uint32_t sms = 0;
+    SegConfig cfg;        // the configuration of the frame being stepped
+    SegConfig tuned_cfg;  // the autotuner's choice
+    uint32_t mode = ASPH_BATCH_AUTO;
+    bool tuned = false;
+    // tuner state: candidate configurations, the frame times measured for each, the candidate being timed
+    std::vector<SegConfig> trials;
+    std::vector<double> trial_ms;
+    size_t trial = 0;
+    uint32_t trial_frames = 0;
+    double trial_acc = 0.0;
+    uint32_t trial_phase = 0;
+    std::vector<std::pair<SegConfig, double>> log;
+    uint64_t seg_steps = 0, seg_captures = 0;
+};
+
+namespace {
+
+void seg_free(SegEngine* E) {
+    if (!E) return;
+    for (SegGraph& g : E->cache)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+    for (cudaEvent_t e : E->ev_member)
+        if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : {E->ev_fork, E->ev_mid, E->ev_aux, E->ev_done})
+        if (e) cudaEventDestroy(e);
+    if (E->main) cudaStreamDestroy(E->main);
+    if (E->aux) cudaStreamDestroy(E->aux);
+    delete E;
+}
+
+asph_status seg_new(size_t members, SegEngine*& out) {
+    out = nullptr;
+    SegEngine* E = new (std::nothrow) SegEngine();
+    if (!E) return fail(ASPH_ERR_OUT_OF_MEMORY, "segmented batch");
+    int lo = 0, hi = 0, dev = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&E->main, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&E->aux, cudaStreamNonBlocking, hi);
+    E->priority_hi = hi;
+    for (cudaEvent_t* ev : {&E->ev_fork, &E->ev_mid, &E->ev_aux, &E->ev_done})
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+    E->ev_member.assign(members, nullptr);
+    for (size_t k = 0; k < members && e == cudaSuccess; k++)
+        e = cudaEventCreateWithFlags(&E->ev_member[k], cudaEventDisableTiming);
+    int sms = 0;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    E->sms = (uint32_t)(sms > 0 ? sms : 1);
+    if (e != cudaSuccess) {
+        seg_free(E);
+        return cuda_fail(e, "segmented batch setup");
+    }
+    out = E;
+    return ASPH_OK;
+}
+
+// Members grouped by kernel variant (periodic box; Morris viscosity; cohesion term), at most kSegScenes a group.
+struct SegGroup {
+    bool periodic, morris, sigma;
+    std::vector<uint32_t> members;
+};
+
+std::vector<SegGroup> seg_groups(asph_simulation* const* sims, const std::vector<uint32_t>& M) {
+    std::vector<SegGroup> out;
+    for (uint32_t k : M) {
+        const asph_simulation* s = sims[k];
+        const bool p = s->grid.periodic != 0, m = s->phys.morris != 0, g = s->phys.sigma_on != 0;
+        SegGroup* hit = nullptr;
+        for (SegGroup& q : out)
+            if (q.periodic == p && q.morris == m && q.sigma == g && q.members.size() < kSegScenes) hit = &q;
+        if (!hit) {
+            out.push_back(SegGroup{p, m, g, {}});
+            hit = &out.back();
+        }
+        hit->members.push_back(k);
+    }
+    return out;
+}
+
+// Enqueues one plain step of every member: their grid stages on their own streams, the segmented passes on the
+// engine's streams, everything ordered after E.main's current work and joined back into E.main. The members'
+// host state advances as run_step's would (cur flips in the grid stage; the caller applies the rest).
+asph_status seg_enqueue(SegEngine& E, asph_simulation* const* sims, const std::vector<uint32_t>& M, const float* dts,
+                        uint32_t& launches_out) {
+    launches_out = 0;
+    CK(cudaEventRecord(E.ev_fork, E.main));
+    for (uint32_t k : M) {
+        asph_simulation* s = sims[k];
+        CK(cudaStreamWaitEvent(s->stream, E.ev_fork, 0));
+        asph_status st = run_step(s, dts[k], ASPH_STAGE_GRID);
+        if (st != ASPH_OK) return st;
+        CK(cudaMemsetAsync(s->fheavy_n, 0, 4 * sizeof(uint32_t), s->stream));
+        CK(cudaEventRecord(E.ev_member[k], s->stream));
+        CK(cudaStreamWaitEvent(E.main, E.ev_member[k], 0));
+    }
+    const std::vector<SegGroup> groups = seg_groups(sims, M);
+    std::vector<SegLaunch> tables(groups.size());
+    for (size_t gi = 0; gi < groups.size(); gi++) {
+        SegLaunch& L = tables[gi];
+        std::memset(&L, 0, sizeof(L));
+        L.nscenes = (uint32_t)groups[gi].members.size();
+        L.chunk = E.cfg.chunk;
+        uint32_t items = 0;
+        for (uint32_t q = 0; q < L.nscenes; q++) {
+            asph_simulation* s = sims[groups[gi].members[q]];
+            L.item_start[q] = items;
+            L.sc[q].a = s->args(s->cur);
+            L.sc[q].c = s->cells();
+            L.sc[q].b = s->boundary();
+            L.sc[q].nl = s->nbrs();
+            items += (s->span() + kSegItem - 1) / kSegItem;
+        }
+        L.item_start[L.nscenes] = items;
+        L.total_items = items;
+    }
+    const uint32_t warp_ctas = E.sms * 2;
+    // ordinary kernels: one CTA per `chunk` items, at most ctas_per_sm per SM (0: no limit)
+    auto ord_ctas = [&](const SegLaunch& L) -> uint32_t {
+        const uint32_t need = (L.total_items + L.chunk - 1) / L.chunk;
+        const uint32_t cap = E.cfg.ctas_per_sm ? E.sms * E.cfg.ctas_per_sm : need;
+        return std::max<uint32_t>(1u, std::min(need, cap));
+    };
+    auto pass = [&](SegPass p, cudaStream_t st, int prio, uint32_t ctas, bool ordinary) -> asph_status {
+        for (size_t gi = 0; gi < groups.size(); gi++) {
+            const SegLaunch& L = tables[gi];
+            const cudaError_t e = launch_segmented(p, L, ordinary ? ord_ctas(L) : ctas, st, prio, groups[gi].periodic,
+                                                   groups[gi].morris, groups[gi].sigma);
+            if (e != cudaSuccess) return cuda_fail(e, "segmented pass");
+            launches_out++;
+        }
+        return ASPH_OK;
+    };
+    asph_status st;
+    // density: box-heavy particles on the high-priority stream beside the ordinary pass
+    CK(cudaEventRecord(E.ev_mid, E.main));
+    CK(cudaStreamWaitEvent(E.aux, E.ev_mid, 0));
+    if ((st = pass(kSegDensityHeavy, E.aux, E.priority_hi, warp_ctas, false)) != ASPH_OK) return st;
+    if ((st = pass(kSegDensity, E.main, 0, 0, true)) != ASPH_OK) return st;
+    if ((st = pass(kSegDensityOverflow, E.main, 0, warp_ctas, false)) != ASPH_OK) return st;
+    if ((st = pass(kSegDensityRow, E.main, 0, warp_ctas, false)) != ASPH_OK) return st;
+    CK(cudaEventRecord(E.ev_mid, E.main));
+    CK(cudaEventRecord(E.ev_aux, E.aux));
+    CK(cudaStreamWaitEvent(E.main, E.ev_aux, 0));
+    // forces
+    CK(cudaStreamWaitEvent(E.aux, E.ev_mid, 0));
+    if ((st = pass(kSegForcesHeavy, E.aux, E.priority_hi, warp_ctas, false)) != ASPH_OK) return st;
+    if ((st = pass(kSegForces, E.main, 0, 0, true)) != ASPH_OK) return st;
+    if ((st = pass(kSegForcesRow, E.main, 0, warp_ctas, false)) != ASPH_OK) return st;
+    CK(cudaEventRecord(E.ev_aux, E.aux));
+    CK(cudaStreamWaitEvent(E.main, E.ev_aux, 0));
+    return ASPH_OK;
+}
+
+std::vector<uint64_t> seg_key(const SegEngine& E, asph_simulation* const* sims, const std::vector<uint32_t>& M,
+                              const float* dts) {
+    std::vector<uint64_t> key;
+    key.reserve(M.size() * 4 + 4);
+    key.push_back(((uint64_t)E.cfg.chunk << 32) | E.cfg.ctas_per_sm);
+    for (uint32_t k : M) {
+        const asph_simulation* s = sims[k];
+        uint32_t dtb, phb;
+        std::memcpy(&dtb, &dts[k], 4);
+        std::memcpy(&phb, &s->pending_half, 4);
+        key.push_back(s->serial);
+        key.push_back(((uint64_t)k << 32) | ((uint64_t)s->cur << 1) | (s->has_pending ? 1u : 0u));
+        key.push_back(((uint64_t)bound_for(s) << 32) | dtb);
+        key.push_back(((uint64_t)phb << 32) | (uint32_t)(s->generation & 0xffffffffu));
+    }
+    return key;
+}
+
+// One plain step of the members through a cached (or newly captured) whole-step graph.
+asph_status seg_step(SegEngine& E, asph_simulation* const* sims, const std::vector<uint32_t>& M, const float* dts,
+                     AdvanceStats& stats) {
+    // a pending refinement read-back is taken where its worst case would exceed the bound a graph is keyed with
+    for (uint32_t k : M) {
+        asph_simulation* s = sims[k];
+        if (s->refine_pending && count_after_refine_bound(s) > bound_for(s)) {
+            asph_status st = refine_finish(s);
+            if (st != ASPH_OK) return st;
+        }
+    }
+    const std::vector<uint64_t> key = seg_key(E, sims, M, dts);
+    SegGraph* hit = nullptr;
+    for (SegGraph& g : E.cache)
+        if (g.exec && g.key == key) hit = &g;
+    if (!hit) {
+        // capture: members' host state is restored afterwards, the replay below applies the step's effects
+        struct Saved {
+            int cur;
+            uint32_t frame;
+            float pending_half;
+            bool has_pending, grid_valid, timing;
+            uint64_t launches;
+        };
+        std::vector<Saved> saved;
+        saved.reserve(M.size());
+        for (uint32_t k : M) {
+            asph_simulation* s = sims[k];
+            saved.push_back(Saved{s->cur, s->frame, s->pending_half, s->has_pending, s->grid_valid, s->timing,
+                                  s->launches});
+            s->timing = false;
+            s->graph_mode = true;
+            s->grid_n = bound_for(s);
+        }
+        cudaGraph_t graph = nullptr;
+        CK(cudaStreamBeginCapture(E.main, cudaStreamCaptureModeThreadLocal));
+        uint32_t seg_launches = 0;
+        const asph_status st = seg_enqueue(E, sims, M, dts, seg_launches);
+        const cudaError_t ce = cudaStreamEndCapture(E.main, &graph);
+        std::vector<uint64_t> member_launches;
+        for (size_t q = 0; q < M.size(); q++) {
+            asph_simulation* s = sims[M[q]];
+            member_launches.push_back(s->launches - saved[q].launches);
+            s->graph_mode = false;
+            s->cur = saved[q].cur;
+            s->frame = saved[q].frame;
+            s->pending_half = saved[q].pending_half;
+            s->has_pending = saved[q].has_pending;
+            s->grid_valid = saved[q].grid_valid;
+            s->timing = saved[q].timing;
+            s->launches = saved[q].launches;
+        }
+        // the segmented launches are counted on the first member
+        if (!member_launches.empty()) member_launches[0] += seg_launches;
+        if (st != ASPH_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return st;
+        }
+        if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture (segmented step)");
+        SegGraph* slot = nullptr;
+        if (E.cache.size() < kSegGraphCache) {
+            E.cache.emplace_back();
+            slot = &E.cache.back();
+        } else {
+            slot = &E.cache[0];
+            for (SegGraph& g : E.cache)
+                if (g.last_use < slot->last_use) slot = &g;
+            if (slot->exec) cudaGraphExecDestroy(slot->exec);
+            slot->exec = nullptr;
+        }
+        const cudaError_t ie =
+            cudaGraphInstantiateWithFlags(&slot->exec, graph, cudaGraphInstantiateFlagUseNodePriority);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) {
+            slot->exec = nullptr;
+            return cuda_fail(ie, "cudaGraphInstantiate (segmented step)");
+        }
+        slot->key = key;
+        slot->member_launches = member_launches;
+        hit = slot;
+        stats.captures++;
+        E.seg_captures++;
+    }
+    hit->last_use = ++E.clock;
+    // the members' earlier work (their own streams) comes first
+    for (uint32_t k : M) {
+        CK(cudaEventRecord(E.ev_member[k], sims[k]->stream));
+        CK(cudaStreamWaitEvent(E.main, E.ev_member[k], 0));
+    }
+    CK(cudaGraphLaunch(hit->exec, E.main));
+    CK(cudaEventRecord(E.ev_done, E.main));
+    for (size_t q = 0; q < M.size(); q++) {
+        asph_simulation* s = sims[M[q]];
+        CK(cudaStreamWaitEvent(s->stream, E.ev_done, 0));
+        s->cur = 1 - s->cur;
+        s->grid_valid = true;
+        s->pending_half = dts[M[q]] / 2.0f;
+        s->has_pending = true;
+        s->frame++;
+        s->launches += hit->member_launches[q];
+    }
+    stats.graph_steps += M.size();
+    E.seg_steps++;
+    return ASPH_OK;
+}
+
+// The candidate configurations, tried one after another over plain frames: the bucket choices first (all
+// segmented, then the largest bucket on per-scene graphs, then the two largest, then none), then the work items per
+// CTA turn and the CTAs per SM with the best bucket choice so far.
+void seg_plan_trials(SegEngine& E) {
+    E.trials.clear();
+    SegConfig c;
+    E.trials.push_back(c);
+    c.segmented[2] = 0;
+    E.trials.push_back(c);
+    c.segmented[1] = 0;
+    E.trials.push_back(c);
+    c.segmented[0] = 0;
+    E.trials.push_back(c);
+    E.trial_ms.assign(E.trials.size(), 0.0);
+    E.trial = 0;
+    E.trial_frames = 0;
+    E.trial_acc = 0.0;
+    E.trial_phase = 0;
+}
+
+}  // namespace
+
+// Lockstep advance of a batch: every scene one frame per round.
+asph_status advance_batch(asph_simulation* const* sims, SceneGraph* const* graphs, SegEngine& E, const float* dts,
+                          size_t count, uint32_t steps, AdvanceStats& stats) {
+    for (size_t k = 0; k < count; k++) {
+        if (!sims[k] || !graphs[k]) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation or graph cache");
+        if (!std::isfinite(dts[k])) return fail(ASPH_ERR_INVALID_ARGUMENT, "delta time must be finite");
+    }
+    if (E.mode == ASPH_BATCH_AUTO && !E.tuned && E.trials.empty()) seg_plan_trials(E);
+    asph_status st;
+    std::vector<uint32_t> M;
+    M.reserve(count);
+    for (uint32_t t = 0; t < steps; t++) {
+        // which configuration this frame runs with: a trial while tuning, then the tuner's choice; segmented mode
+        // puts every bucket on segmented passes (with the tuned work-item and CTA counts once known)
+        const bool tuning = E.mode == ASPH_BATCH_AUTO && !E.tuned;
+        if (tuning) {
+            E.cfg = E.trials[E.trial];
+        } else if (E.mode == ASPH_BATCH_AUTO) {
+            E.cfg = E.tuned_cfg;
+        } else {
+            E.cfg = E.tuned ? E.tuned_cfg : SegConfig{};
+            for (uint32_t q = 0; q < kBuckets; q++) E.cfg.segmented[q] = E.mode == ASPH_BATCH_SEGMENTED ? 1 : 0;
+        }
+        M.clear();
+        // a tuning frame is timed only when every simulation steps plainly in it; it starts with the device idle
+        // and ends when all of its work (per-simulation graphs and the segmented step) has finished
+        bool plain_frame = true;
+        for (size_t k = 0; k < count; k++) {
+            const asph_simulation* s = sims[k];
+            if (refinement_due(s) || s->n == 0 || !s->has_pending) plain_frame = false;
+        }
+        std::chrono::steady_clock::time_point t0;
+        if (tuning && plain_frame) {
+            CK(cudaDeviceSynchronize());
+            t0 = std::chrono::steady_clock::now();
+        }
+        for (size_t k = 0; k < count; k++) {
+            asph_simulation* s = sims[k];
+            const bool seg_ok = E.cfg.segmented[bucket_of(s->n)] != 0;
+            if (refinement_due(s)) {
+                if ((st = refine_finish(s)) != ASPH_OK) return st;
+                if ((st = run_step(s, dts[k], ASPH_STAGE_ALL, true)) != ASPH_OK) return st;
+                stats.eager_steps++;
+            } else if (s->n == 0 || !s->has_pending) {
+                if ((st = refine_finish(s)) != ASPH_OK) return st;
+                if ((st = run_step(s, dts[k], ASPH_STAGE_ALL)) != ASPH_OK) return st;
+                stats.eager_steps++;
+            } else if (seg_ok) {
+                M.push_back((uint32_t)k);
+            } else if ((st = graph_step(s, *graphs[k], dts[k], stats)) != ASPH_OK) {
+                return st;
+            }
+        }
+        if (!M.empty() && (st = seg_step(E, sims, M, dts, stats)) != ASPH_OK) return st;
+        if (tuning && plain_frame) {
+            CK(cudaDeviceSynchronize());
+            const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+            // the first frame of a configuration captures its graphs: the second is timed
+            if (E.trial_frames++ >= 1) E.trial_acc += ms;
+            if (E.trial_frames >= 3) {
+                E.trial_ms[E.trial] = E.trial_acc / 2.0;
+                E.log.emplace_back(E.trials[E.trial], E.trial_ms[E.trial]);
+                E.trial_frames = 0;
+                E.trial_acc = 0.0;
+                if (++E.trial == E.trials.size()) {
+                    size_t best = 0;
+                    for (size_t q = 1; q < E.trials.size(); q++)
+                        if (E.trial_ms[q] < E.trial_ms[best]) best = q;
+                    const SegConfig won = E.trials[best];
+                    if (E.trial_phase == 0 && (won.segmented[0] || won.segmented[1] || won.segmented[2])) {
+                        // second phase: work items per fetch and CTAs per SM around the winner
+                        E.trial_phase = 1;
+                        E.trials.clear();
+                        E.trials.push_back(won);
+                        for (uint32_t ch : {2u, 4u}) {
+                            SegConfig c = won;
+                            c.chunk = ch;
+                            E.trials.push_back(c);
+                        }
+                        SegConfig c = won;
+                        c.ctas_per_sm = 0;  // one CTA per work item (no persistent loop)
+                        E.trials.push_back(c);
+                        E.trial_ms.assign(E.trials.size(), 0.0);
+                        E.trial = 0;
+                    } else {
+                        E.tuned_cfg = won;
+                        E.tuned = true;
+                    }
+                }
+            }
+        }
+    }
+    for (size_t k = 0; k < count; k++)
+        if ((st = refine_finish(sims[k])) != ASPH_OK) return st;
+    CK(cudaStreamSynchronize(E.main));
+    for (size_t k = 0; k < count; k++)
+        if ((st = check_errors(sims[k], true)) != ASPH_OK) return st;
+    return ASPH_OK;
+}
+
 struct asph_batch {
     std::vector<asph_simulation*> sims;
     std::vector<SceneGraph*> graphs;
     AdvanceStats stats;
+    SegEngine* seg = nullptr;
 };
 
 extern "C" {
@@ -2151,6 +2625,13 @@ asph_status asph_batch_create(asph_simulation* const* sims, uint32_t count, asph
     asph_batch* b = new (std::nothrow) asph_batch();
     if (!b) return fail(ASPH_ERR_OUT_OF_MEMORY, "batch");
     b->sims.assign(sims, sims + count);
+    {
+        asph_status st = seg_new(count, b->seg);
+        if (st != ASPH_OK) {
+            asph_batch_destroy(b);
+            return st;
+        }
+    }
     for (uint32_t k = 0; k < count; k++) {
         SceneGraph* g = scene_graph_new();
         if (!g) {
@@ -2166,14 +2647,46 @@ asph_status asph_batch_create(asph_simulation* const* sims, uint32_t count, asph
 void asph_batch_destroy(asph_batch* b) {
     if (!b) return;
     for (SceneGraph* g : b->graphs) scene_graph_free(g);
+    seg_free(b->seg);
     delete b;
 }
 
 asph_status asph_batch_step(asph_batch* b, const float* dts, uint32_t steps) {
     API_ENTRY();
     if (!b || (!b->sims.empty() && !dts)) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
-    std::vector<uint32_t> left(b->sims.size(), steps);
-    return advance_scenes(b->sims.data(), b->graphs.data(), dts, left.data(), b->sims.size(), b->stats);
+    return advance_batch(b->sims.data(), b->graphs.data(), *b->seg, dts, b->sims.size(), steps, b->stats);
+}
+
+asph_status asph_batch_set_mode(asph_batch* b, uint32_t mode) {
+    API_ENTRY();
+    if (!b) return fail(ASPH_ERR_INVALID_ARGUMENT, "null batch");
+    if (mode != ASPH_BATCH_AUTO && mode != ASPH_BATCH_GRAPHS && mode != ASPH_BATCH_SEGMENTED)
+        return fail(ASPH_ERR_INVALID_ARGUMENT, "unknown batch mode");
+    b->seg->mode = mode;
+    return ASPH_OK;
+}
+
+asph_status asph_batch_tuning(const asph_batch* b, asph_batch_tuning_info* out) {
+    API_ENTRY();
+    if (!b || !out) return fail(ASPH_ERR_INVALID_ARGUMENT, "null argument");
+    const SegEngine& E = *b->seg;
+    std::memset(out, 0, sizeof(*out));
+    out->mode = E.mode;
+    out->tuned = E.tuned ? 1u : 0u;
+    const SegConfig& c0 = E.tuned ? E.tuned_cfg : E.cfg;
+    for (uint32_t q = 0; q < kBuckets; q++) out->segmented[q] = c0.segmented[q];
+    out->chunk = c0.chunk;
+    out->ctas_per_sm = c0.ctas_per_sm;
+    out->segmented_steps = E.seg_steps;
+    out->segmented_captures = E.seg_captures;
+    out->trials = (uint32_t)std::min<size_t>(E.log.size(), ASPH_BATCH_MAX_TRIALS);
+    for (uint32_t q = 0; q < out->trials; q++) {
+        const SegConfig& c = E.log[q].first;
+        out->trial_ms[q] = E.log[q].second;
+        out->trial_config[q] = (uint32_t)c.segmented[0] | ((uint32_t)c.segmented[1] << 1) |
+                               ((uint32_t)c.segmented[2] << 2) | (c.chunk << 8) | (c.ctas_per_sm << 16);
+    }
+    return ASPH_OK;
 }
 
 asph_status asph_batch_stats(const asph_batch* b, uint64_t* graph_steps, uint64_t* eager_steps, uint64_t* captures) {

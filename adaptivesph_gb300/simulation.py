@@ -403,18 +403,50 @@ def create_simulation_with_walls(parameters: Parameters, positions: np.ndarray, 
     return Simulation(out.value, parameters, refinement_params)
 
 
+class _TuningInfo(ctypes.Structure):
+    """asph_batch_tuning_info (include/asph.h)."""
+
+    _fields_ = [("mode", ctypes.c_uint32), ("tuned", ctypes.c_uint32), ("segmented", ctypes.c_uint32 * 3),
+                ("chunk", ctypes.c_uint32), ("ctas_per_sm", ctypes.c_uint32), ("trials", ctypes.c_uint32),
+                ("segmented_steps", ctypes.c_uint64), ("segmented_captures", ctypes.c_uint64),
+                ("trial_ms", ctypes.c_double * 16), ("trial_config", ctypes.c_uint32 * 16)]
+
+
+BATCH_MODES = {"auto": 0, "graphs": 1, "segmented": 2}
+
+
 class Batch:
     """Independent simulations advanced together (asph_batch_*; no reference counterpart): their steps overlap on
-    the device and plain steps replay CUDA graphs. Each simulation's result equals its result when stepped alone.
-    The batch does not own the simulations; keep them alive while the batch exists."""
+    the device. Plain frames run as per-simulation graphs or through segmented density and force passes shared by
+    up to 64 simulations (mode "graphs", "segmented", or "auto": an autotuner picks per particle-count bucket). Each
+    simulation's result equals its result when stepped alone, in every mode. The batch does not own the
+    simulations; keep them alive while the batch exists."""
 
-    def __init__(self, simulations: Sequence[Simulation]):
+    def __init__(self, simulations: Sequence[Simulation], mode: str = "auto"):
         self._lib = _lib.load()
         self._sims = list(simulations)
         arr = (_vp * max(len(self._sims), 1))(*[s._h.value for s in self._sims])
         h = _vp()
         _lib.check(self._lib.asph_batch_create(arr, len(self._sims), ctypes.byref(h)), "asph_batch_create")
         self._h = h
+        self.set_mode(mode)
+
+    def set_mode(self, mode: str) -> None:
+        _lib.check(self._lib.asph_batch_set_mode(self._h, BATCH_MODES[mode]), "asph_batch_set_mode")
+
+    def tuning(self) -> Dict[str, object]:
+        t = _TuningInfo()
+        _lib.check(self._lib.asph_batch_tuning(self._h, ctypes.byref(t)), "asph_batch_tuning")
+        names = {v: k for k, v in BATCH_MODES.items()}
+        trials = []
+        for q in range(t.trials):
+            c = t.trial_config[q]
+            trials.append(dict(segmented=[(c >> b) & 1 for b in range(3)], chunk=(c >> 8) & 0xFF,
+                               ctas_per_sm=(c >> 16) & 0xFF, ms_per_frame=float(t.trial_ms[q])))
+        return dict(mode=names.get(t.mode, t.mode), tuned=bool(t.tuned), segmented=list(t.segmented),
+                    chunk=t.chunk, ctas_per_sm=t.ctas_per_sm, segmented_steps=t.segmented_steps,
+                    segmented_captures=t.segmented_captures, trials=trials,
+                    buckets="particle counts below 16384, below 65536, and above")
 
     def step(self, delta_times, steps: int = 1) -> None:
         dts = np.ascontiguousarray(np.broadcast_to(np.asarray(delta_times, np.float32), (len(self._sims),)))

@@ -547,8 +547,29 @@ def run_batched(args, rank: int, world: int, dist):
                                       bd.get_particle_count()))
     setup_s = time.perf_counter() - t0
     dts = [sc.dt for sc in mix]
-    batch = Batch(sims)
+    batch = Batch(sims)  # mode "auto": the autotuner times its candidates over the first plain frames
+    tune_steps = 0
+    while not batch.tuning()["tuned"] and tune_steps < 200:
+        batch.step(dts, 5)
+        tune_steps += 5
     batch.step(dts, args.warmup)
+
+    # each mode over the same number of frames, continuing the same simulations (results are identical in every
+    # mode; only the time differs)
+    modes = {}
+    mode_steps = min(args.steps, 100)
+    for mode in ("graphs", "segmented", "auto"):
+        batch.set_mode(mode)
+        batch.step(dts, 3)  # captures
+        nb = [s.get_fluid_particles_count() for s in sims]
+        torch.cuda.synchronize()
+        tm = time.perf_counter()
+        batch.step(dts, mode_steps)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - tm
+        na = [s.get_fluid_particles_count() for s in sims]
+        modes[mode] = {"value": float(sum(0.5 * (a + b) for a, b in zip(nb, na))) * mode_steps / el,
+                       "ms_per_step": el * 1e3 / mode_steps, "steps": mode_steps}
     n_before = [s.get_fluid_particles_count() for s in sims]
     if dist is not None:
         dist.barrier()
@@ -563,6 +584,7 @@ def run_batched(args, rank: int, world: int, dist):
     n_after = [s.get_fluid_particles_count() for s in sims]
     work = float(sum(0.5 * (a + b) for a, b in zip(n_before, n_after))) * args.steps
     stats = batch.stats()
+    tuning = batch.tuning()
     batch.close()
     # sequential: the same simulations, continuing, one scene at a time
     seq_work, seq_s, per_scene = 0.0, 0.0, []
@@ -609,8 +631,44 @@ def run_batched(args, rank: int, world: int, dist):
                        "ms_per_step_p50": float(np.percentile(ps, 50)), "ms_per_step_p99": float(np.percentile(ps, 99))},
         "speedup_vs_sequential": value / seq,
         "batch": stats,
+        "tuning": tuning,
+        "tuning_steps": tune_steps,
+        "modes": modes,
         "clocks": clocks,
     }
+
+
+def run_batch_one(args, rank: int, world: int, dist):
+    """The 1M-particle dam break without refinement, alone in an asph_batch in mode --batch-mode: 8 frames untimed,
+    then --steps frames timed inside the NVTX range "timed" (a profiler's capture window). Compares the segmented
+    passes with per-simulation graphs on the same particles."""
+    import torch
+
+    from adaptivesph_gb300 import Batch, create_simulation
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    sc, bd = build_scene(args)
+    sc.refinement = None
+    n0 = sc.positions.shape[0]
+    sim = create_simulation(sc.parameters, sc.positions, None, None, bd, None, n0, bd.get_particle_count())
+    batch = Batch([sim], mode=args.batch_mode)
+    batch.step([sc.dt], 8)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    torch.cuda.nvtx.range_push("timed")
+    batch.step([sc.dt], args.steps)
+    torch.cuda.nvtx.range_pop()
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    tuning = batch.tuning()
+    batch.close()
+    sim.close()
+    if rank != 0:
+        return None
+    return {"metric": "particle-steps/s, one scene in a batch", "value": n0 * args.steps / el, "unit": UNIT,
+            "ms_per_step": el * 1e3 / args.steps, "steps": args.steps, "batch_mode": args.batch_mode,
+            "segmented_steps": tuning["segmented_steps"],
+            "config": {"workload": "1M-particle dam break (100x200x50, dx 0.004 m) without refinement, alone in a batch"}}
 
 
 # ------------------------------------------------------------------------------------------------ served
@@ -862,9 +920,13 @@ def main():
     ap.add_argument("--drift-steps", type=int, default=10000, help="steps of the conservation workload")
     ap.add_argument("--drift-every", type=int, default=100, help="steps between FP64 totals (conservation)")
     ap.add_argument("--out", default="", help="conservation: write the full record (every totals row) to this file")
-    ap.add_argument("--workload", choices=["adaptive1m", "batched", "served", "conservation"], default="adaptive1m",
+    ap.add_argument("--workload", choices=["adaptive1m", "batched", "served", "conservation", "batch1m"],
+                    default="adaptive1m",
                     help="adaptive1m: the headline 1M adaptive dam break; batched: the scene mix through asph_batch; "
-                         "served: Poisson scene requests through asph_server")
+                         "served: Poisson scene requests through asph_server; batch1m: the 1M plain dam break alone in "
+                         "a batch (--batch-mode)")
+    ap.add_argument("--batch-mode", choices=["auto", "graphs", "segmented"], default="segmented",
+                    help="batch mode of the batch1m workload")
     ap.add_argument("--requests", type=int, default=24, help="requests of the served workload")
     ap.add_argument("--rates", type=float, nargs="+", default=[5.0, 50.0, 200.0], help="arrival rates (1/s)")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="device-memory budget of the server")
@@ -892,7 +954,7 @@ def main():
         tdist.init_process_group("nccl")
         dist = tdist
     runners = {"batched": run_batched, "served": run_served, "adaptive1m": run_ours,
-               "conservation": run_conservation}
+               "conservation": run_conservation, "batch1m": run_batch_one}
     line = runners[args.workload](args, rank, world, dist)
     if line is not None:
         print(json.dumps(line), flush=True)

@@ -457,6 +457,31 @@ asph_status asph_batch_step(asph_batch* batch, const float* dts, uint32_t steps)
 /* Steps replayed from graphs, steps run eagerly (refinement frames), graph captures so far. */
 asph_status asph_batch_stats(const asph_batch* batch, uint64_t* graph_steps, uint64_t* eager_steps,
                              uint64_t* captures);
+/* How plain frames are stepped. GRAPHS: one captured graph per simulation step, the simulations' graphs
+ * overlapping on their own streams. SEGMENTED: every plain-stepping simulation's grid stage on its own stream, then
+ * its density and force passes inside segmented launches shared by up to 64 simulations (persistent kernels walking
+ * a queue of 128-particle work items), the whole batch step one captured graph. AUTO (the default): an autotuner
+ * times the choices over the batch's first plain frames (per particle-count bucket -- below 16k, below 64k, above --
+ * segmented or per-simulation graphs; work items per CTA turn; persistent CTAs per SM) and keeps the fastest.
+ * Every mode gives every simulation the same result bit for bit. */
+#define ASPH_BATCH_AUTO 0u
+#define ASPH_BATCH_GRAPHS 1u
+#define ASPH_BATCH_SEGMENTED 2u
+asph_status asph_batch_set_mode(asph_batch* batch, uint32_t mode);
+#define ASPH_BATCH_MAX_TRIALS 16u
+typedef struct asph_batch_tuning_info {
+    uint32_t mode;
+    uint32_t tuned;           /* 1 once the autotuner has chosen */
+    uint32_t segmented[3];    /* per bucket: 1 segmented, 0 per-simulation graphs */
+    uint32_t chunk;           /* consecutive work items per CTA turn */
+    uint32_t ctas_per_sm;     /* CTAs per SM of the ordinary segmented kernels (persistent); 0: one CTA per turn */
+    uint32_t trials;          /* configurations timed */
+    uint64_t segmented_steps; /* batch steps run through the segmented graph */
+    uint64_t segmented_captures;
+    double trial_ms[ASPH_BATCH_MAX_TRIALS];        /* wall time of one plain frame of the whole batch */
+    uint32_t trial_config[ASPH_BATCH_MAX_TRIALS];  /* bits 0-2 segmented per bucket, 8-15 chunk, 16-23 CTAs/SM */
+} asph_batch_tuning_info;
+asph_status asph_batch_tuning(const asph_batch* batch, asph_batch_tuning_info* out);
 
 /* ---------------------------------------------------------------------------------------------
  * Serving loop (no reference counterpart): scene requests are submitted at any time, admitted first

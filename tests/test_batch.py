@@ -18,7 +18,10 @@ def _scenes():
     ]
 
 
-def test_batch_matches_alone():
+@pytest.mark.parametrize("mode", ["auto", "graphs", "segmented"])
+def test_batch_matches_alone(mode):
+    """Plain frames as per-simulation graphs, as segmented passes, or as the autotuner switches between them while
+    it times them: every simulation's state equals its state stepped alone, bit for bit."""
     scenes = _scenes()
     alone = [make_pair(sc)[0] for sc in scenes]
     mixed = [make_pair(sc)[0] for sc in scenes]
@@ -26,7 +29,7 @@ def test_batch_matches_alone():
     for _ in range(25):
         for sim, dt in zip(alone, dts):
             sim.update(dt)
-    batch = Batch(mixed)
+    batch = Batch(mixed, mode=mode)
     batch.step(dts, 10)
     batch.step(dts, 15)
     for a, m in zip(alone, mixed):
@@ -35,6 +38,13 @@ def test_batch_matches_alone():
     st = batch.stats()
     assert st["graph_steps"] > 0 and st["eager_steps"] > 0
     assert st["captures"] < st["graph_steps"]
+    tn = batch.tuning()
+    if mode == "segmented":
+        assert tn["segmented_steps"] > 0
+    if mode == "graphs":
+        assert tn["segmented_steps"] == 0
+    if mode == "auto":
+        assert len(tn["trials"]) > 0
     batch.close()
 
 
@@ -76,9 +86,12 @@ def _mix_slice():
     return scenes.batched_mix()[:28]
 
 
-def test_batched_mix_slice_alone_vs_batch_and_oracle():
+@pytest.mark.parametrize("mode", ["segmented", "auto"])
+def test_batched_mix_slice_alone_vs_batch_and_oracle(mode):
     """Each of 28 scenes of the batched mix gives, in one batch with the 27 others, the state it gives alone, bit for
-    bit, over 25 frames (refinement frames 10 and 20 included); the 3 smallest (one adaptive) also match the oracle."""
+    bit, over 25 frames (refinement frames 10 and 20 included); the 3 smallest (one adaptive) also match the oracle.
+    Segmented: every plain frame's density and force passes run as launches shared by the scenes (Morris viscosity,
+    one kernel variant); auto: the autotuner's trial configurations during the same frames."""
     mix = _mix_slice()
     counts = [sc.positions.shape[0] for sc in mix]
     assert min(counts) < 16384 and max(counts) > 65536, "uneven counts wanted"
@@ -88,7 +101,7 @@ def test_batched_mix_slice_alone_vs_batch_and_oracle():
         for _ in range(steps):
             sim.update(sc.dt)
     mixed = [_sim(sc) for sc in mix]
-    batch = Batch(mixed)
+    batch = Batch(mixed, mode=mode)
     batch.step([sc.dt for sc in mix], steps)
     refined = 0
     for a, m, sc in zip(alone, mixed, mix):
