@@ -330,6 +330,33 @@ def run_ours(args, rank: int, world: int, dist):
                  "what": "the same 1M-particle dam break and walls without refinement (the reference's plain "
                          "SphSimulation step), state resident, CUDA events on the simulation's stream"}
         simp.close()
+        # the 128k plain dam break (40x80x40 at dx 0.01 m), the same way
+        from adaptivesph_gb300 import StaticBoundaryDomain, scenes as _scenes
+
+        c1 = _scenes.c1_plain()
+        bd1 = StaticBoundaryDomain.generate(c1.parameters.domain, c1.boundary_spacing, c1.parameters.rest_density,
+                                            c1.parameters.base_smoothing_radius)
+        n1 = c1.positions.shape[0]
+        sim1 = create_simulation(c1.parameters, c1.positions, None, None, bd1, None, n1, bd1.get_particle_count())
+        sim1.set_stream(stream.cuda_stream)
+        for _ in range(PLAIN_WARMUP):
+            sim1.step_async(c1.dt)
+        sim1.synchronize()
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            ps.record(stream)
+            for _ in range(args.plain_steps):
+                sim1.step_async(c1.dt)
+            pe.record(stream)
+        torch.cuda.synchronize()
+        c1_ms = ps.elapsed_time(pe)
+        errors |= sim1.device_errors()
+        plain["c1_128k"] = {"value": n1 * args.plain_steps / (c1_ms / 1e3), "unit": UNIT,
+                            "ms_per_step": c1_ms / args.plain_steps, "particles": n1,
+                            "boundary_particles": bd1.get_particle_count(),
+                            "what": "the 128k plain dam break (40x80x40, dx 0.01 m), frames "
+                                    f"{PLAIN_WARMUP}..{PLAIN_WARMUP + args.plain_steps - 1}"}
+        sim1.close()
 
     # ---------------- end to end through the C ABI with host buffers: the simulation is created from host arrays
     # inside the timed region and every frame's result is exported to pinned host memory; it covers frames
@@ -455,6 +482,17 @@ def run_reference(args, rank: int, world: int):
     sc, bpos, bpsi = build_scene_cpu(args)
     cps, cores, secs, (f0, f1) = cpu_throughput(args, steps, args.warmup)
     ref_gpu = reference_cuda_leg(args, sc, bpos, bpsi) if args.plain_steps > 0 else None
+    if ref_gpu is not None and "unavailable" not in ref_gpu:
+        import oracle
+        from adaptivesph_gb300 import scenes as _scenes
+
+        c1 = _scenes.c1_plain()
+        d1 = c1.parameters.domain
+        bp1, bs1 = oracle.boundary_generate(d1.min, d1.max, c1.boundary_spacing, c1.parameters.rest_density,
+                                            c1.parameters.base_smoothing_radius)
+        ref_gpu["c1_128k"] = reference_cuda_leg(args, c1, bp1, bs1)
+        ref_gpu["c1_128k"]["what"] = "the same, on the 128k plain dam break (40x80x40, dx 0.01 m)"
+        ref_gpu["c1_128k"].pop("clocks", None)
     if product_lib._lib is not None:
         raise RuntimeError("the reference arm must not load the CUDA library")
     line = {
@@ -486,9 +524,9 @@ def run_reference(args, rank: int, world: int):
 def reference_cuda_leg(args, sc, bpos, bpsi):
     """The reference's own CUDA step on this GPU (oracle/ref_cuda.py: its kernels compiled from its sources for
     sm_103a, launched in SphSimulation::update's order with its block size and its device synchronisation after
-    every step) on the plain form of the 1M-particle dam break, frames PLAIN_WARMUP .. PLAIN_WARMUP + K - 1: what
-    the GPU arm's `plain` leg is compared with. The reference's refinement pass is not run on the GPU (its in-place
-    compaction races)."""
+    every step) on the plain form of a scene (the 1M-particle dam break, and the 128k one beside it), frames
+    PLAIN_WARMUP .. PLAIN_WARMUP + K - 1: what the GPU arm's `plain` leg is compared with. The reference's
+    refinement pass is not run on the GPU (its in-place compaction races)."""
     from oracle import ref_cuda
 
     if not ref_cuda.available():
