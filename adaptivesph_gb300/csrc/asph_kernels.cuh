@@ -45,7 +45,7 @@ constexpr uint32_t kPooled = 0x80000000u;
 constexpr uint32_t kBoundaryWalk = 0xffffffffu;
 constexpr uint32_t kPoolLaneEntries = 32;
 constexpr uint32_t kPoolSlots = 8192;
-constexpr uint32_t kListEntries = 256;  // entries per row
+constexpr uint32_t kListEntries = 128;  // entries per row
 constexpr uint32_t kRowHeavy = 96;      // rows longer than this are summed by a warp
 struct NbrDev {
     uint2* ent;

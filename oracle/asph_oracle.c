@@ -474,7 +474,7 @@ float orc_cbrtf(float xf)
 static const float ORC_PI_F = 3.141592653589793f;
 #define ORC_LANES 32       /* lanes of the warp that sums a heavy particle */
 #define ORC_HEAVY_CELLS 27 /* query boxes of more reference cells than this are heavy */
-#define ORC_LIST_ENTRIES 256 /* neighbour-list row length in entries; a particle needing more is summed by cells */
+#define ORC_LIST_ENTRIES 128 /* neighbour-list row length in entries; a particle needing more is summed by cells */
 #define ORC_ROW_HEAVY 96     /* a particle with more row entries than this is summed over its row by a warp */
 
 /* Entries of the particle's neighbour-list row: the candidate cells' members are scanned in blocks of up to 32

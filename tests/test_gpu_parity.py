@@ -246,7 +246,7 @@ def test_refinement_with_large_smoothing_lengths_bitexact():
 
 def test_every_summation_kind_bitexact():
     """A dense lattice (h = 2.6 dx, so sub-cells hold over 100 members) with mostly 3 h0 particles: heavy boxes,
-    overflowed rows (more than 256 entries), long rows and ordinary particles all occur in one pass."""
+    overflowed rows (more than 128 entries), long rows and ordinary particles all occur in one pass."""
     sc = scenes.dam_break((24, 24, 24), 0.02, seed=11, tank=(0.7, 0.7, 0.7), h_ratio=2.6)
     sim, orc = make_pair(sc)
     st = sim.read_state()
