@@ -45,7 +45,7 @@ DENSITY_BYTES_PER_PARTICLE = 28.0
 STEP_BYTES_PER_PARTICLE = 332.0
 L2_BYTES = 129e6
 LATE_STEPS = 20  # frames timed by the late-frame leg
-PLAIN_WARMUP = 3  # untimed frames before the plain legs (ours and the reference's CUDA step)
+PLAIN_WARMUP = 20  # untimed frames before the plain legs (ours and the reference's CUDA step)
 
 
 def measured_peaks():
@@ -541,21 +541,26 @@ def reference_cuda_leg(args, sc, bpos, bpsi):
         r.step(sc.dt)
     steps = args.plain_steps
     s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    marks = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
     sampler = ClockSampler(dev)
     sampler.start()
     torch.cuda.synchronize()
     s.record()
-    for _ in range(steps):
+    marks[0].record()
+    for k in range(steps):
         r.step(sc.dt)  # ends with the device synchronisation the reference's update() ends with
+        marks[k + 1].record()
     e.record()
     torch.cuda.synchronize()
     clocks = sampler.stop()
     ms = s.elapsed_time(e)
+    per_step = sorted(marks[k].elapsed_time(marks[k + 1]) for k in range(steps))
     n = r.n
     rho = r.rho[:n].float()
     ok = bool(torch.isfinite(rho).all().item())
     r.close()
-    return {"value": n * steps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps, "steps": steps,
+    return {"value": n * steps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps,
+            "ms_per_step_median": per_step[len(per_step) // 2], "steps": steps,
             "frames": [PLAIN_WARMUP, PLAIN_WARMUP + steps - 1], "particles": n, "boundary_particles": int(bpos.shape[0]),
             "densities_finite": ok, "clocks": clocks,
             "what": "the reference's own kernels (cubins built from its sources, C++20, --expt-relaxed-constexpr, "
@@ -951,7 +956,7 @@ def main():
     ap.add_argument("--criterion", choices=["velocity", "free_surface"], default="velocity",
                     help="split/merge criterion of the 1M adaptive dam break: the reference's velocity criterion, or "
                          "the neighbour-count deficit that splits at the free surface")
-    ap.add_argument("--plain-steps", type=int, default=20,
+    ap.add_argument("--plain-steps", type=int, default=200,
                     help="frames of the plain-form legs (ours, and the reference's CUDA step in the reference arm)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
@@ -966,7 +971,8 @@ def main():
     ap.add_argument("--batch-mode", choices=["auto", "graphs", "segmented"], default="segmented",
                     help="batch mode of the batch1m workload")
     ap.add_argument("--requests", type=int, default=24, help="requests of the served workload")
-    ap.add_argument("--rates", type=float, nargs="+", default=[5.0, 50.0, 200.0], help="arrival rates (1/s)")
+    ap.add_argument("--rates", type=float, nargs="+", default=[5.0, 10.0, 20.0, 50.0, 100.0, 200.0],
+                    help="arrival rates (1/s)")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="device-memory budget of the server")
     ap.add_argument("--poll-steps", type=int, default=50, help="steps per server poll")
     ap.add_argument("--scenes", type=int, default=256, help="scenes of the batched mix")
