@@ -112,6 +112,32 @@ def test_adaptive_dam_break_1m_late_frames_bitexact():
     assert sim.device_errors() == 0
 
 
+def test_adaptive_dam_break_1m_frame_2000_bitexact():
+    """The 1M adaptive dam break at the end of its stated 2000 steps: the GPU alone to frame 1996, then the oracle
+    takes over the same state and both step to frame 2001 (a refinement frame at 2000 included), bit for bit over all
+    particles."""
+    sc = scenes.c2_adaptive()
+    cap = sc.refinement.max_particle_count
+    sim, orc, bd = _scene_pair(sc, cap)
+    for _ in range(1996):
+        sim.step_async(sc.dt)
+    sim.synchronize()
+    _transfer(sim, orc)
+    refined = False
+    for _ in range(5):
+        sim.step_async(sc.dt)
+        sim.synchronize()
+        if orc.step(sc.dt):
+            refined = True
+            rep, o = sim.last_refinement(), orc.last_report()
+            for key in ("merge_eligible", "merge_pairs", "split_candidates", "splits", "count_after"):
+                assert rep[key] == o[key], (key, rep[key], o[key])
+        assert_state_bitexact(sim.read_state(), orc.arrays())
+    assert refined, "the frames must include a refinement pass"
+    assert sim.device_errors() == 0
+    sim.close()
+
+
 def test_taylor_green_128_cubed_bitexact_and_fp64():
     """The periodic Taylor-Green vortex at 128^3 = 2,097,152 particles (Morris viscosity, Re = 100): two frames
     bit-exact against the oracle over the whole state, then the third frame's densities and accelerations bit-exact
