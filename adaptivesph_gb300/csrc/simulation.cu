@@ -248,6 +248,8 @@ struct asph_simulation {
 
     // timing
     bool timing = false;
+    // plain steps of asph_simulation_step_async replayed from captured graphs (created at the first such step)
+    asph::SceneGraph* own_graph = nullptr;
     struct Ev {
         cudaEvent_t a, b;
         int cls;
@@ -935,6 +937,8 @@ asph_status export_copies(cudaStream_t stream, const ExportStage& x, float* posi
 void destroy(asph_simulation* s) {
     if (!s) return;
     if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->own_graph) scene_graph_free(s->own_graph);
+    s->own_graph = nullptr;
     for (int k = 0; k < 2; k++) {
         dfree(s->set[k].ph);
         dfree(s->set[k].vm);
@@ -1338,6 +1342,22 @@ static asph_status create_impl(const asph_parameters* parameters, const float* p
     return ASPH_OK;
 }
 
+namespace {
+asph_status graph_step(asph_simulation* s, SceneGraph& g, float dt, AdvanceStats& stats);
+}  // namespace
+
+// A plain step (no refinement pass due, a pending half-kick to fuse, particles present) replays a captured graph,
+// which saves the launch gaps of ~20 dependent kernels (at 128k particles a step takes 0.32 ms from a graph against
+// 0.36 ms launched one by one). Not while per-stage timing is on (its events belong to eager launches), not on the
+// legacy or per-thread default stream (they cannot be captured), and not while the caller captures the stream.
+static bool plain_step_graphable(asph_simulation* s) {
+    if (s->n == 0 || !s->has_pending || s->timing || refinement_due(s)) return false;
+    if (s->stream == nullptr || s->stream == cudaStreamLegacy || s->stream == cudaStreamPerThread) return false;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return false;
+    return true;
+}
+
 extern "C" {
 
 asph_status asph_simulation_create(const asph_parameters* parameters, const float* positions, uint32_t count,
@@ -1375,6 +1395,13 @@ void asph_simulation_destroy(asph_simulation* sim) { destroy(sim); }
 asph_status asph_simulation_step_async(asph_simulation* sim, float delta_time) {
     API_ENTRY();
     if (!sim) return fail(ASPH_ERR_INVALID_ARGUMENT, "null simulation");
+    if (plain_step_graphable(sim)) {
+        if (!sim->own_graph && !(sim->own_graph = scene_graph_new()))
+            return fail(ASPH_ERR_OUT_OF_MEMORY, "step graph");
+        if (!std::isfinite(delta_time)) return fail(ASPH_ERR_INVALID_ARGUMENT, "delta time must be finite");
+        AdvanceStats stats;
+        return graph_step(sim, *sim->own_graph, delta_time, stats);
+    }
     return run_step(sim, delta_time, ASPH_STAGE_ALL);
 }
 
@@ -1459,7 +1486,8 @@ asph_status asph_simulation_step_cfl(asph_simulation* sim, float cfl, float dt_m
     }
     if (!(dt < 3.0e38f)) return fail(ASPH_ERR_INVALID_ARGUMENT, "no particles and no dt_max");
     if (dt_used) *dt_used = dt;
-    return asph_simulation_step_async(sim, dt);
+    if (!std::isfinite(dt)) return fail(ASPH_ERR_INVALID_ARGUMENT, "delta time must be finite");
+    return run_step(sim, dt, ASPH_STAGE_ALL);  // eager: dt changes every step, a graph would be captured each time
 }
 
 asph_status asph_simulation_update_domain(asph_simulation* sim, const asph_domain* domain,
