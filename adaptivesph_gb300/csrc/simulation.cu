@@ -1346,12 +1346,16 @@ namespace {
 asph_status graph_step(asph_simulation* s, SceneGraph& g, float dt, AdvanceStats& stats);
 }  // namespace
 
-// A plain step (no refinement pass due, a pending half-kick to fuse, particles present) replays a captured graph,
-// which saves the launch gaps of ~20 dependent kernels (at 128k particles a step takes 0.32 ms from a graph against
-// 0.36 ms launched one by one). Not while per-stage timing is on (its events belong to eager launches), not on the
-// legacy or per-thread default stream (they cannot be captured), and not while the caller captures the stream.
+// A plain step (no refinement pass due, a pending half-kick to fuse, particles present) of a simulation of up to
+// kGraphStepParticles particles replays a captured graph, which saves the launch gaps of ~20 dependent kernels (at
+// 128k particles a step takes 0.32 ms from a graph against 0.36 ms launched one by one). Larger simulations launch
+// eagerly: their device time hides the gaps (1.67 against 1.69 ms per step at 1M), and the two captures (one per
+// buffer parity, ~1 ms each) would cost more than they save over the first hundreds of steps. Not while per-stage
+// timing is on (its events belong to eager launches), not on the legacy or per-thread default stream (they cannot
+// be captured), and not while the caller captures the stream.
+constexpr uint32_t kGraphStepParticles = 262144;
 static bool plain_step_graphable(asph_simulation* s) {
-    if (s->n == 0 || !s->has_pending || s->timing || refinement_due(s)) return false;
+    if (s->n == 0 || s->n > kGraphStepParticles || !s->has_pending || s->timing || refinement_due(s)) return false;
     if (s->stream == nullptr || s->stream == cudaStreamLegacy || s->stream == cudaStreamPerThread) return false;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(s->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return false;
