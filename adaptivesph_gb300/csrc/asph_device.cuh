@@ -301,7 +301,7 @@ __device__ __forceinline__ void for_each_subcell_lane(const GridDev& g, const ui
                                                       const float* __restrict__ hmax,
                                                       const float* __restrict__ hmax_ref, uint32_t ex0, uint32_t ex1,
                                                       float px, float py, float pz, float R, float Rfix, int lane,
-                                                      Body&& body) {
+                                                      Body&& body, uint32_t wi = 0, uint32_t nw = 1) {
     int32_t lo[3], hi[3];
     const float p[3] = {px, py, pz};
     bool ok = true;
@@ -315,9 +315,12 @@ __device__ __forceinline__ void for_each_subcell_lane(const GridDev& g, const ui
     const float m = g.cull_margin;
     const uint32_t grp = (uint32_t)lane >> 3, q = (uint32_t)lane & 7u;
     const int32_t qx = (int32_t)(q & 1u), qy = (int32_t)((q >> 1) & 1u), qz = (int32_t)(q >> 2);
-    for (uint32_t base = 0; base < ncell; base += 32u) {
-        // level 1: reference cell base + lane
-        const uint32_t cell = base + (uint32_t)lane;
+    // with nw warps over one box (wi this warp's index), warp wi takes the reference cells whose index modulo 4 nw is
+    // in [4 wi, 4 wi + 4), 32 of them per round; with one warp that is cells base + lane, base = 0, 32, 64, ...
+    const uint32_t G = 4u * nw;
+    for (uint32_t j0 = 0; G * j0 + 4u * wi < ncell; j0 += 8u) {
+        // level 1: one reference cell per lane
+        const uint32_t cell = G * (j0 + ((uint32_t)lane >> 2)) + 4u * wi + ((uint32_t)lane & 3u);
         float shx = 0.0f, shy = 0.0f, shz = 0.0f;
         int32_t cx = 0, cy = 0, cz = 0;
         bool live = false;

@@ -48,6 +48,7 @@ __device__ float cbrt_newton(float x);
 __global__ void k_merge_score(StepArgs a, CellsDev c, RefineArgs r);
 __global__ void k_split_score(StepArgs a, CellsDev c, RefineArgs r);
 __global__ void k_select_ids(StepArgs a, const uint32_t* n_ptr, uint32_t* keys, uint32_t* vals);
+__global__ void k_select_split_ids(StepArgs a, RefineArgs r, uint32_t* keys, uint32_t* vals);
 __global__ void k_select_scores(const float* score, const uint32_t* n_ptr, int descending, const uint32_t* vals_by_id,
                                 uint32_t* keys);
 __global__ void k_merge_limits(RefineArgs r, uint32_t n);

@@ -221,6 +221,27 @@ __global__ void __launch_bounds__(256, 2) k_split_score(StepArgs a, CellsDev c, 
 }
 
 // Stage A of the selection: (id, index) pairs; stage B keys come from the scores in id order.
+// The split selection's input: only the particles with a positive split score (the split parents are the first
+// `splits` entries of the descending order, and splits <= the positive count), appended at kCtrSortN, which
+// k_split_limits zeroes when there is anything to split; warp-aggregated appends, their order is then fixed by the
+// sort by id. The first `splits` entries after the sorts are the ones a sort of all particles gives.
+__global__ void __launch_bounds__(256) k_select_split_ids(StepArgs a, RefineArgs r, uint32_t* keys, uint32_t* vals) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = (r.ctr[kCtrSplits] > 0u) ? r.ctr[kCtrCount2] : 0u;
+    const bool take = i < n && r.score[i] > 0.0f;
+    const unsigned b = __ballot_sync(0xffffffffu, take);
+    if (b == 0u) return;
+    const int lane = (int)(threadIdx.x & 31u);
+    uint32_t base = 0;
+    if (lane == __ffs(b) - 1) base = atomicAdd(r.ctr + kCtrSortN, (uint32_t)__popc(b));
+    base = __shfl_sync(0xffffffffu, base, __ffs(b) - 1);  // every lane of the warp is here (b is warp-uniform)
+    if (take) {
+        const uint32_t slot = base + (uint32_t)__popc(b & ((1u << lane) - 1u));
+        keys[slot] = a.id[i];
+        vals[slot] = i;
+    }
+}
+
 __global__ void __launch_bounds__(256) k_select_ids(StepArgs a, const uint32_t* n_ptr, uint32_t* keys, uint32_t* vals) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < *n_ptr) {
@@ -295,38 +316,43 @@ __global__ void __launch_bounds__(256, 4) k_merge_candidates(StepArgs a, CellsDe
     r.cand[e] = bj;
 }
 
-// identifyMergeCandidates for the queued large boxes: one warp per particle, the box's sub-cells dealt to the lanes
-// (for_each_subcell_lane). The nearest candidate is the minimum of (r^2, id) over the accepted members, which does not
-// depend on the visiting order, so the warp's reduction gives the sequential scan's result.
-__global__ void __launch_bounds__(256, 4) k_merge_candidates_heavy(StepArgs a, CellsDev c, RefineArgs r) {
+// identifyMergeCandidates for the queued large boxes: one block of 8 warps per particle, the box's reference cells
+// dealt to the warps and their sub-cells to the lanes (for_each_subcell_lane over 8 warps). The nearest candidate is
+// the minimum of (r^2, id) over the accepted members, which does not depend on the visiting order, so the block's
+// reduction gives the sequential scan's result.
+__global__ void __launch_bounds__(256, 2) k_merge_candidates_heavy(StepArgs a, CellsDev c, RefineArgs r) {
+    constexpr uint32_t kWarps = 8;
+    __shared__ float s_best[kWarps];
+    __shared__ uint32_t s_bj[kWarps], s_bid[kWarps];
     const int lane = threadIdx.x & 31;
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t wi = threadIdx.x >> 5;
     const uint32_t nq = r.ctr[kCtrMergeHeavy];
-    for (uint32_t w = warp; w < nq; w += nwarps) {
-        const uint32_t e = r.mqueue[w];
+    for (uint32_t q = blockIdx.x; q < nq; q += gridDim.x) {
+        const uint32_t e = r.mqueue[q];
         const float4 pe = a.ph[e];
         const float he = pe.w;
         float best = 3.402823466e38f;
         uint32_t bj = kNone, bid = 0xffffffffu;
-        for_each_subcell_lane(a.grid, c.start, c.end, c.hmax, c.hmax_ref, c.ex[0], c.ex[1], pe.x, pe.y, pe.z, he, he, lane,
-                              [&](uint32_t jb, uint32_t je, float, float, float) {
-                                for (uint32_t j = jb; j < je; ++j) {
-                                    if (j == e) continue;
-                                    const float4 pj = a.ph[j];
-                                    const float dx = pj.x - pe.x, dy = pj.y - pe.y, dz = pj.z - pe.z;
-                                    const float r2 = dist2(dx, dy, dz);
-                                    const float hm = pj.w < he ? pj.w : he;
-                                    if (r2 < hm * hm && a.vm[j].w < r.max_mass) {
-                                        const uint32_t idj = a.id[j];
-                                        if (r2 < best || (r2 == best && idj < bid)) {
-                                            best = r2;
-                                            bj = j;
-                                            bid = idj;
-                                        }
-                                    }
-                                }
-                            });
+        for_each_subcell_lane(
+            a.grid, c.start, c.end, c.hmax, c.hmax_ref, c.ex[0], c.ex[1], pe.x, pe.y, pe.z, he, he, lane,
+            [&](uint32_t jb, uint32_t je, float, float, float) {
+                for (uint32_t j = jb; j < je; ++j) {
+                    if (j == e) continue;
+                    const float4 pj = a.ph[j];
+                    const float dx = pj.x - pe.x, dy = pj.y - pe.y, dz = pj.z - pe.z;
+                    const float r2 = dist2(dx, dy, dz);
+                    const float hm = pj.w < he ? pj.w : he;
+                    if (r2 < hm * hm && a.vm[j].w < r.max_mass) {
+                        const uint32_t idj = a.id[j];
+                        if (r2 < best || (r2 == best && idj < bid)) {
+                            best = r2;
+                            bj = j;
+                            bid = idj;
+                        }
+                    }
+                }
+            },
+            wi, kWarps);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             const float ob = __shfl_xor_sync(0xffffffffu, best, o);
@@ -338,7 +364,23 @@ __global__ void __launch_bounds__(256, 4) k_merge_candidates_heavy(StepArgs a, C
                 bid = oid;
             }
         }
-        if (lane == 0) r.cand[e] = bj;
+        if (lane == 0) {
+            s_best[wi] = best;
+            s_bj[wi] = bj;
+            s_bid[wi] = bid;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (uint32_t k = 1; k < kWarps; ++k) {
+                if (s_best[k] < best || (s_best[k] == best && s_bid[k] < bid)) {
+                    best = s_best[k];
+                    bj = s_bj[k];
+                    bid = s_bid[k];
+                }
+            }
+            r.cand[e] = bj;
+        }
+        __syncthreads();
     }
 }
 
@@ -491,7 +533,7 @@ __global__ void k_split_limits(RefineArgs r, uint32_t cap, uint32_t tpb) {
     r.ctr[kCtrSplitCand] = ks;
     r.ctr[kCtrSplitBudget] = budget;
     r.ctr[kCtrSplits] = splits;
-    r.ctr[kCtrSortN] = splits > 0u ? n2 : 0u;
+    r.ctr[kCtrSortN] = 0u;  // k_select_split_ids appends the positive-score particles
     r.ctr[kCtrCountOut] = n2 + 12u * splits;
 }
 

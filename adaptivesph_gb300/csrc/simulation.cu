@@ -754,7 +754,7 @@ asph_status refine_enqueue(asph_simulation* s) {
     hp = s->tic();
     k_split_score<<<nbk, 256, 0, s->stream>>>(c, s->cells(), r);
     k_split_limits<<<1, 1, 0, s->stream>>>(r, s->cap, s->tpb);
-    k_select_ids<<<nbk, 256, 0, s->stream>>>(c, s->ctr + kCtrSortN, s->keys, s->vals);
+    k_select_split_ids<<<nbk, 256, 0, s->stream>>>(c, r, s->keys, s->vals);
     CK_LAUNCH("split selection");
     s->launches += 3;
     s->launches += radix_sort_pairs(s->keys, s->vals, s->ctr + kCtrSortN, n, id_bits(s->next_id), s->ss, s->err,
@@ -1151,6 +1151,7 @@ static void preload_kernels() {
             (const void*)k_merge_pairs,    (const void*)k_compact_count,    (const void*)k_compact_scan,
             (const void*)k_compact_scatter, (const void*)k_split_limits,    (const void*)k_split_apply,
             (const void*)k_refine_finish,  (const void*)k_cells_only,       (const void*)k_export,
+            (const void*)k_select_split_ids,
             (const void*)k_totals,         (const void*)k_density_info,     (const void*)k_reduce_rows,
             (const void*)k_neighbor_counts};
         for (const void* k : kernels) {
