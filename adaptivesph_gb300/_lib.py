@@ -34,6 +34,7 @@ DEVERR_SPIN_LIMIT = 0x1
 DEVERR_NONFINITE = 0x2
 DEVERR_SPLIT_CAPACITY = 0x4
 DEVERR_ID_OVERFLOW = 0x8
+DEVERR_ROWS = 0x10
 
 
 class AsphError(RuntimeError):

@@ -65,6 +65,7 @@ struct NbrDev {
     uint32_t* pool_cnt;
     uint32_t pool_slots;
     uint32_t maxe;
+    uint32_t rows;  // particles the rows are allocated for: an index at or above it is flagged, not accessed
 };
 
 struct ReorderArgs {

@@ -619,7 +619,11 @@ __device__ __forceinline__ void boundary_forces_rows(const StepArgs& a, const Bo
 template <bool kPeriodic>
 __device__ __forceinline__ void density_ordinary(const StepArgs& a, const CellsDev& c, const BoundaryDev& b,
                                                  const NbrDev& nl, const uint32_t i) {
-    const bool in = i < count_of(a);
+    bool in = i < count_of(a);
+    if (in && i >= nl.rows) {
+        atomicOr(a.err, 0x10u);  // rows not grown for this count: the particle is skipped, the step flagged
+        in = false;
+    }
     const float4 pi = in ? a.ph[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const float R = pi.w + pi.w;
     bool active = in;
@@ -808,7 +812,7 @@ __global__ void __launch_bounds__(128, 2) k_density_heavy(StepArgs a, CellsDev c
 template <bool kMorris, bool kSigma>
 __device__ __forceinline__ void forces_ordinary(const StepArgs& a, const CellsDev& c, const BoundaryDev& b,
                                                 const NbrDev& nl, const uint32_t i) {
-    if (i >= count_of(a)) return;
+    if (i >= count_of(a) || i >= nl.rows) return;
     const uint32_t cnt = nl.cnt[i];
     if (cnt > kRowHeavy) return;  // long row (k_forces_row), overflowed or heavy (k_forces_heavy)
     const ForceCtx x = force_ctx(a, i);

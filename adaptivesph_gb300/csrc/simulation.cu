@@ -161,7 +161,8 @@ struct asph_simulation {
     int cur = 0;
     float4* kc = nullptr;
     float4* pq = nullptr;  // [cap] x, y, z, (2h)^2 of the current step (StepArgs::pq)
-    uint2* nbr_ent = nullptr;     // [kListEntries * cap] neighbour lists, one row per particle
+    uint2* nbr_ent = nullptr;     // [kListEntries * rows_cap] neighbour lists, one row per particle
+    uint32_t rows_cap = 0;        // particles the rows are allocated for (grown on demand, never above cap)
     uint32_t* nbr_cnt = nullptr;  // [cap]
     uint32_t* nbr_bcnt = nullptr;  // [cap] wall entries of ordinary rows
     uint32_t* heavy_idx = nullptr;  // [cap] queue of heavy particles of the current step
@@ -292,7 +293,7 @@ struct asph_simulation {
     NbrDev nbrs() const {
         return NbrDev{nbr_ent,      nbr_cnt,  heavy_idx,    heavy_n,  fheavy_idx,   fheavy_n,
                       dover_idx,    fheavy_n + 1, drow_idx, fheavy_n + 2, frow_idx, fheavy_n + 3,
-                      nbr_bcnt,     pool,     pool_cnt,     pool_slots,   kListEntries};
+                      nbr_bcnt,     pool,     pool_cnt,     pool_slots,   kListEntries, rows_cap};
     }
 
     BoundaryDev boundary() const {
@@ -355,8 +356,9 @@ void dfree(void* p) {
     if (p) cudaFree(p);
 }
 
-// Device memory a simulation holds: the sizes allocated by asph_simulation_create (the export staging buffer,
-// allocated on the first export, and the optional id lists are not included).
+// Device memory a simulation can hold: the sizes asph_simulation_create allocates, with the neighbour rows at the
+// capacity (they start smaller and grow; the export staging buffer, allocated on the first export, and the optional
+// id lists are not included).
 uint64_t device_bytes_for(uint32_t C, uint32_t sort_items, uint32_t ncells, uint32_t refcells, uint32_t nb,
                           bool adaptive) {
     const uint64_t c = C;
@@ -603,6 +605,34 @@ asph_status build_grid(asph_simulation* s, bool integrate, float dt, bool carry_
     return ASPH_OK;
 }
 
+// Rows for n particles and the growth a refinement pass may add before the next allocation check (the grid bound
+// a captured step is keyed with: n + n/8 + 256, in multiples of 256), never above the capacity.
+uint32_t rows_for(uint32_t n, uint32_t cap) {
+    const uint64_t b = ((uint64_t)n + n / 8 + 256 + 255) / 256 * 256;
+    return (uint32_t)std::min<uint64_t>(b, std::max<uint32_t>(cap, 1u));
+}
+
+// The neighbour rows (128 entries, 1 KB per particle) are allocated for the particles present plus headroom, not
+// for the whole capacity (4x the initial count in the adaptive dam break), and grown when a step needs more: rows
+// are rebuilt every step, so growing drops nothing. Growing waits for the simulation's streams (the old rows may
+// be in use) and bumps the generation, so captured steps holding the old rows are captured again. Never called
+// while a step is being captured (the caller grows the rows first).
+asph_status ensure_rows(asph_simulation* s, uint32_t need) {
+    if (need <= s->rows_cap) return ASPH_OK;
+    if (s->graph_mode) return fail(ASPH_ERR_INVALID_ARGUMENT, "neighbour rows must be grown before a capture");
+    const uint32_t want = rows_for(need + need / 4, s->cap);
+    CK(cudaStreamSynchronize(s->stream));
+    CK(cudaStreamSynchronize(s->aux));
+    dfree(s->nbr_ent);
+    s->nbr_ent = nullptr;
+    s->rows_cap = 0;
+    asph_status st = dalloc(s->nbr_ent, (size_t)kListEntries * want);
+    if (st != ASPH_OK) return st;
+    s->rows_cap = want;
+    s->generation++;
+    return ASPH_OK;
+}
+
 // The ordinary kernel of each neighbour pass runs on the simulation's stream, the heavy-particle kernel on the
 // auxiliary stream, concurrently:
 //   main: k_density ------------(wait heavy density)-- k_forces ------------(wait heavy forces)--
@@ -842,6 +872,7 @@ asph_status run_step(asph_simulation* s, float dt, uint32_t last_stage, bool def
         s->grid_valid = false;
         return ASPH_OK;
     }
+    if (!s->graph_mode && (st = ensure_rows(s, s->span())) != ASPH_OK) return st;
     if ((st = build_grid(s, true, dt, false)) != ASPH_OK) return st;
     if (last_stage < ASPH_STAGE_DENSITY) return ASPH_OK;
     if ((st = run_density(s)) != ASPH_OK) return st;
@@ -1260,7 +1291,8 @@ static asph_status create_impl(const asph_parameters* parameters, const float* p
     }
     TRY(dalloc(s->kc, C));
     TRY(dalloc(s->pq, C));
-    TRY(dalloc(s->nbr_ent, (size_t)kListEntries * C));
+    s->rows_cap = rows_for(count, C);
+    TRY(dalloc(s->nbr_ent, (size_t)kListEntries * s->rows_cap));
     TRY(dalloc(s->nbr_cnt, C));
     TRY(dalloc(s->nbr_bcnt, C));
     TRY(dalloc(s->heavy_idx, C));
@@ -2123,6 +2155,7 @@ asph_status graph_step(asph_simulation* s, SceneGraph& g, float dt, AdvanceStats
         asph_status st = refine_finish(s);
         if (st != ASPH_OK) return st;
         if (!g.exec[parity] || !g.key[parity].replays(key, s->n)) {
+            if ((st = ensure_rows(s, bound_for(s))) != ASPH_OK) return st;
             if ((st = capture_step(s, g, dt)) != ASPH_OK) return st;
             stats.captures++;
         }
@@ -2417,6 +2450,11 @@ asph_status seg_step(SegEngine& E, asph_simulation* const* sims, const std::vect
             asph_status st = refine_finish(s);
             if (st != ASPH_OK) return st;
         }
+    }
+    // rows for the grid bound a capture is keyed with (growing bumps a member's generation, part of the key)
+    for (uint32_t k : M) {
+        asph_status st = ensure_rows(sims[k], bound_for(sims[k]));
+        if (st != ASPH_OK) return st;
     }
     const std::vector<uint64_t> key = seg_key(E, sims, M, dts);
     SegGraph* hit = nullptr;

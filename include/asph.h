@@ -40,6 +40,7 @@ typedef enum asph_status {
 #define ASPH_DEVERR_NONFINITE 0x2u      /* a density or acceleration came out NaN/Inf */
 #define ASPH_DEVERR_SPLIT_CAPACITY 0x4u /* splits were dropped because the fluid capacity was reached (informational) */
 #define ASPH_DEVERR_ID_OVERFLOW 0x8u    /* the 32-bit particle id space is exhausted */
+#define ASPH_DEVERR_ROWS 0x10u          /* a particle lay beyond the allocated neighbour rows; that step is invalid */
 
 /* Simulation::Parameters::Domain (cuda/include/cuda/simulation/Simulation.cuh:66-94) */
 typedef struct asph_domain {
@@ -428,8 +429,9 @@ asph_status asph_simulation_kernel_times(asph_simulation* sim, double* ms, uint3
 /* Number of kernels this library launched on the simulation's stream since create (all classes). */
 asph_status asph_simulation_launch_count(const asph_simulation* sim, uint64_t* out);
 
-/* Device memory a simulation holds, and the same figure for a simulation not yet created (what
- * asph_simulation_create would allocate for these arguments); no reference counterpart. */
+/* Device memory a simulation can hold, and the same figure for a simulation not yet created; no reference
+ * counterpart. Both are the figure at the fluid capacity: the neighbour rows (1 KB per particle) are allocated for
+ * the particles present plus headroom and grown, up to the capacity, by the step that needs more. */
 asph_status asph_simulation_device_bytes(const asph_simulation* sim, uint64_t* out);
 asph_status asph_estimate_device_bytes(const asph_parameters* parameters,
                                        uint32_t count,

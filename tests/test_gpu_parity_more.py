@@ -297,3 +297,37 @@ def test_enable_adaptive_refinement_bitexact():
         assert rep[key] == o[key], (key, rep[key], o[key])
     assert rep["merge_pairs"] + rep["splits"] > 0
     assert_state_bitexact(sim.read_state(), orc.arrays())
+
+
+@pytest.mark.parametrize("path", ["update", "segmented"])
+def test_rows_grow_with_the_particle_count_bitexact(path):
+    """The neighbour rows are allocated for the particles present (plus headroom) and grown on demand: a state of
+    3.8x the created count written into the simulation is stepped through a captured single-simulation step or a
+    segmented batch step; every step equals the oracle's and no particle lies beyond the rows (the kernels flag
+    that in the device error word, which update and step check)."""
+    from adaptivesph_gb300 import Batch
+    sc = small_dam_break()
+    sim, orc = make_pair(sc, capacity=12000)
+    big = small_dam_break(counts=(20, 24, 16))
+    big.parameters = sc.parameters
+    bd = boundary_of(big)
+    o_big = oracle.OracleSim(sc.parameters, big.positions, bd.positions, bd.psi, None, capacity=12000)
+    st = o_big.arrays()
+    n = st["pos"].shape[0]
+    assert n == 7680 and n > 3 * sc.positions.shape[0]
+    sim.write_state(st, frame=3, next_id=n, pending_half=sc.dt / 2)
+    orc.load(st, frame=3, next_id=n, pending_half=sc.dt / 2)
+    if path == "update":
+        for _ in range(6):
+            sim.update(sc.dt)
+            orc.step(sc.dt)
+            assert_state_bitexact(sim.read_state(), orc.arrays())
+    else:
+        batch = Batch([sim], mode="segmented")
+        batch.step([sc.dt], 6)
+        for _ in range(6):
+            orc.step(sc.dt)
+        assert batch.tuning()["segmented_steps"] > 0
+        assert_state_bitexact(sim.read_state(), orc.arrays())
+        batch.close()
+    assert sim.device_errors() == 0
