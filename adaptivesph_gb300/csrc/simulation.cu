@@ -135,6 +135,16 @@ __global__ void k_init_state(StepArgs a, const float4* pos, float r0, float h0, 
     a.id[i] = i;
 }
 
+// Boundary records as the caller passes them (asph_boundary_particle: x, y, z, w, psi; 20 bytes, 4-byte aligned)
+// split into the positions and psi that the boundary setup sorts.
+__global__ void k_boundary_records(const float* rec, uint32_t nb, float4* pos, float* psi) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nb) return;
+    const float* r = rec + 5 * (size_t)i;
+    pos[i] = make_float4(r[0], r[1], r[2], r[3]);
+    psi[i] = r[4];
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------------------------------------ simulation
@@ -163,6 +173,7 @@ struct asph_simulation {
     float4* pq = nullptr;  // [cap] x, y, z, (2h)^2 of the current step (StepArgs::pq)
     uint2* nbr_ent = nullptr;     // [kListEntries * rows_cap] neighbour lists, one row per particle
     uint32_t rows_cap = 0;        // particles the rows are allocated for (grown on demand, never above cap)
+    uint8_t* arena = nullptr;     // one allocation holding the fixed-size buffers (carve_fixed)
     uint32_t* nbr_cnt = nullptr;  // [cap]
     uint32_t* nbr_bcnt = nullptr;  // [cap] wall entries of ordinary rows
     uint32_t* heavy_idx = nullptr;  // [cap] queue of heavy particles of the current step
@@ -518,27 +529,48 @@ asph_status setup_boundary_device(asph_simulation* s, const float4* d_pos, const
 }
 
 // The same from host boundary particles (StaticBoundaryDomain::Particle, position + psi).
+// Whether this device's kernels read pageable host memory coherently through the host's page tables (address
+// translation over NVLink-C2C, as on Grace-Blackwell): creation then reads the caller's arrays in place, one pass
+// at link bandwidth, instead of staging them through a pageable copy. Without translation through the host's page
+// tables (pageable access by page migration) the pages would move to the device, so that case copies.
+bool device_reads_host_in_place(const void* p, size_t align) {
+    if (reinterpret_cast<uintptr_t>(p) % align != 0) return false;
+    int dev = 0, pageable = 0, host_tables = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return pageable == 1 && host_tables == 1;
+}
+
+// The caller's boundary records: read in place (device_reads_host_in_place) or copied as they are, then split into
+// positions and psi on the device.
 asph_status setup_boundary(asph_simulation* s, const asph_boundary_particle* b, uint32_t nb) {
     if (nb == 0) return setup_boundary_device(s, nullptr, nullptr, 0);
-    std::vector<float4> pos(nb);
-    std::vector<float> psi(nb);
-    for (uint32_t i = 0; i < nb; i++) {
-        pos[i] = make_float4(b[i].position[0], b[i].position[1], b[i].position[2], b[i].position[3]);
-        psi[i] = b[i].psi;
-    }
+    static_assert(sizeof(asph_boundary_particle) == 5 * sizeof(float), "boundary records are 5 floats");
     float4* d_pos = nullptr;
     float* d_psi = nullptr;
-    asph_status st;
-    if ((st = dalloc(d_pos, nb)) != ASPH_OK) return st;
-    if ((st = dalloc(d_psi, nb)) != ASPH_OK) {
-        dfree(d_pos);
-        return st;
+    float* d_rec = nullptr;
+    const float* rec = reinterpret_cast<const float*>(b);
+    asph_status st = dalloc(d_pos, nb);
+    if (st == ASPH_OK) st = dalloc(d_psi, nb);
+    cudaError_t e = cudaSuccess;
+    if (st == ASPH_OK && !device_reads_host_in_place(b, alignof(float))) {
+        st = dalloc(d_rec, 5 * (size_t)nb);
+        if (st == ASPH_OK)
+            e = cudaMemcpyAsync(d_rec, b, sizeof(asph_boundary_particle) * nb, cudaMemcpyHostToDevice, s->stream);
+        rec = d_rec;
     }
-    cudaError_t e = cudaMemcpyAsync(d_pos, pos.data(), sizeof(float4) * nb, cudaMemcpyHostToDevice, s->stream);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(d_psi, psi.data(), sizeof(float) * nb, cudaMemcpyHostToDevice, s->stream);
-    st = e == cudaSuccess ? setup_boundary_device(s, d_pos, d_psi, nb) : cuda_fail(e, "boundary upload");
+    if (st == ASPH_OK && e == cudaSuccess) {
+        k_boundary_records<<<blocks_for(nb), 256, 0, s->stream>>>(rec, nb, d_pos, d_psi);
+        e = cudaGetLastError();
+        s->launches++;
+    }
+    if (st == ASPH_OK) st = e == cudaSuccess ? setup_boundary_device(s, d_pos, d_psi, nb) : cuda_fail(e, "boundary upload");
     cudaStreamSynchronize(s->stream);
+    dfree(d_rec);
     dfree(d_pos);
     dfree(d_psi);
     return st;
@@ -970,52 +1002,17 @@ void destroy(asph_simulation* s) {
     if (s->stream) cudaStreamSynchronize(s->stream);
     if (s->own_graph) scene_graph_free(s->own_graph);
     s->own_graph = nullptr;
-    for (int k = 0; k < 2; k++) {
-        dfree(s->set[k].ph);
-        dfree(s->set[k].vm);
-        dfree(s->set[k].acc);
-        dfree(s->set[k].rp);
-        dfree(s->set[k].rad);
-        dfree(s->set[k].id);
-    }
-    dfree(s->kc);
-    dfree(s->pq);
+    dfree(s->arena);  // the fixed-size buffers (carve_fixed)
     dfree(s->nbr_ent);
-    dfree(s->nbr_cnt);
-    dfree(s->nbr_bcnt);
-    dfree(s->heavy_idx);
-    dfree(s->heavy_n);
-    dfree(s->fheavy_idx);
-    dfree(s->fheavy_n);
-    dfree(s->dover_idx);
-    dfree(s->drow_idx);
-    dfree(s->frow_idx);
-    dfree(s->pool);
-    dfree(s->pool_cnt);
-    dfree(s->keys);
-    dfree(s->vals);
-    dfree(s->sort_mem);
     dfree(s->cell_start);
     dfree(s->cell_end);
     dfree(s->cell_hmax);
     dfree(s->hmax_ref);
-    dfree(s->ex);
-    dfree(s->q3);
-    dfree(s->err);
-    dfree(s->d_count);
-    dfree(s->red);
     dfree(s->bpos);
     dfree(s->bfric);
     dfree(s->bstart);
     dfree(s->bend);
     dfree(s->brefflag);
-    dfree(s->score);
-    dfree(s->cand);
-    dfree(s->flag);
-    dfree(s->ctr);
-    dfree(s->slot0);
-    dfree(s->block_counts);
-    dfree(s->rkeys);
     dfree(s->dbg_ids);
     dfree(s->stage);
     if (s->h_ctr) cudaFreeHost(s->h_ctr);
@@ -1193,6 +1190,64 @@ static void preload_kernels() {
     });
 }
 
+// The fixed-size device buffers of a simulation are carved from one allocation: creation made ~35 cudaMalloc calls
+// otherwise, 50-100 us each whatever the size. Each buffer starts on a 256-byte boundary; a first pass with no base
+// measures the total. (The neighbour rows, cell tables and boundary arrays, which are reallocated, stay apart.)
+struct Carver {
+    uint8_t* base = nullptr;
+    size_t used = 0;
+    template <class T>
+    void take(T*& p, size_t count) {
+        used = (used + 255) & ~size_t(255);
+        p = base ? reinterpret_cast<T*>(base + used) : nullptr;
+        used += sizeof(T) * std::max<size_t>(count, 1);
+    }
+};
+
+static void carve_fixed(asph_simulation* s, Carver& c, uint32_t sort_items) {
+    const size_t C = s->cap;
+    for (int k = 0; k < 2; k++) {
+        c.take(s->set[k].ph, C);
+        c.take(s->set[k].vm, C);
+        c.take(s->set[k].acc, C);
+        c.take(s->set[k].rp, C);
+        c.take(s->set[k].rad, C);
+        c.take(s->set[k].id, C);
+    }
+    c.take(s->kc, C);
+    c.take(s->pq, C);
+    c.take(s->nbr_cnt, C);
+    c.take(s->nbr_bcnt, C);
+    c.take(s->heavy_idx, C);
+    c.take(s->heavy_n, 1);
+    c.take(s->fheavy_idx, C);
+    c.take(s->fheavy_n, 4);
+    c.take(s->dover_idx, C);
+    c.take(s->drow_idx, C);
+    c.take(s->frow_idx, C);
+    c.take(s->pool, (size_t)s->pool_slots * 32 * kPoolLaneEntries);
+    c.take(s->pool_cnt, (size_t)s->pool_slots * 32);
+    c.take(s->keys, sort_items);
+    c.take(s->vals, sort_items);
+    uint8_t* mem = nullptr;
+    c.take(mem, sort_scratch_bytes(sort_items));
+    s->sort_mem = mem;
+    c.take(s->ex, 4);
+    c.take(s->q3, 2);
+    c.take(s->err, 1);
+    c.take(s->d_count, 2);
+    c.take(s->red, kRedBytes);
+    if (s->adaptive) {
+        c.take(s->score, C);
+        c.take(s->cand, C);
+        c.take(s->flag, C);
+        c.take(s->ctr, kCtrNum);
+        c.take(s->slot0, 1);
+        c.take(s->block_counts, blocks_for((uint32_t)C));
+        c.take(s->rkeys, 2 * C);
+    }
+}
+
 static asph_status create_impl(const asph_parameters* parameters, const float* positions, uint32_t count,
                                const asph_fluid_buffers* fluid_buffers, const asph_boundary_buffers* boundary_buffers,
                                const asph_boundary_particle* boundary, uint32_t boundary_count,
@@ -1281,57 +1336,22 @@ static asph_status create_impl(const asph_parameters* parameters, const float* p
         return st;                 \
     }
     const uint32_t C = s->cap;
-    for (int k = 0; k < 2; k++) {
-        TRY(dalloc(s->set[k].ph, C));
-        TRY(dalloc(s->set[k].vm, C));
-        TRY(dalloc(s->set[k].acc, C));
-        TRY(dalloc(s->set[k].rp, C));
-        TRY(dalloc(s->set[k].rad, C));
-        TRY(dalloc(s->set[k].id, C));
-    }
-    TRY(dalloc(s->kc, C));
-    TRY(dalloc(s->pq, C));
-    s->rows_cap = rows_for(count, C);
-    TRY(dalloc(s->nbr_ent, (size_t)kListEntries * s->rows_cap));
-    TRY(dalloc(s->nbr_cnt, C));
-    TRY(dalloc(s->nbr_bcnt, C));
-    TRY(dalloc(s->heavy_idx, C));
-    TRY(dalloc(s->heavy_n, 1));
-    TRY(dalloc(s->fheavy_idx, C));
-    TRY(dalloc(s->fheavy_n, 4));
-    TRY(dalloc(s->dover_idx, C));
-    TRY(dalloc(s->drow_idx, C));
-    TRY(dalloc(s->frow_idx, C));
-    s->pool_slots = std::min<uint32_t>(kPoolSlots, std::max<uint32_t>(64u, C / 128u));
-    TRY(dalloc(s->pool, (size_t)s->pool_slots * 32 * kPoolLaneEntries));
-    TRY(dalloc(s->pool_cnt, (size_t)s->pool_slots * 32));
     const uint32_t sort_items = std::max(C, std::max(boundary_count, max_boundary_capacity));
+    s->pool_slots = std::min<uint32_t>(kPoolSlots, std::max<uint32_t>(64u, C / 128u));
+    {
+        Carver plan;
+        carve_fixed(s, plan, sort_items);
+        TRY(dalloc(s->arena, plan.used));
+        Carver take{s->arena};
+        carve_fixed(s, take, sort_items);
+        sort_scratch_bind(s->ss, s->sort_mem, sort_items);
+    }
     s->device_bytes = device_bytes_for(C, sort_items, s->grid.ncells,
                                        (uint32_t)(s->grid.gs[0] * s->grid.gs[1] * s->grid.gs[2]), boundary_count,
                                        adaptive);
-    TRY(dalloc(s->keys, sort_items));
-    TRY(dalloc(s->vals, sort_items));
-    {
-        uint8_t* mem = nullptr;
-        TRY(dalloc(mem, sort_scratch_bytes(sort_items)));
-        s->sort_mem = mem;
-        sort_scratch_bind(s->ss, mem, sort_items);
-    }
-    TRY(dalloc(s->ex, 4));
-    TRY(dalloc(s->q3, 2));
-    TRY(dalloc(s->err, 1));
-    TRY(dalloc(s->d_count, 2));
-    TRY(dalloc(s->red, kRedBytes));
+    s->rows_cap = rows_for(count, C);
+    TRY(dalloc(s->nbr_ent, (size_t)kListEntries * s->rows_cap));
     TRY(alloc_cells(s));
-    if (adaptive) {
-        TRY(dalloc(s->score, C));
-        TRY(dalloc(s->cand, C));
-        TRY(dalloc(s->flag, C));
-        TRY(dalloc(s->ctr, kCtrNum));
-        TRY(dalloc(s->slot0, 1));
-        TRY(dalloc(s->block_counts, blocks_for(C)));
-        TRY(dalloc(s->rkeys, 2 * (size_t)C));
-    }
     e = cudaMallocHost(reinterpret_cast<void**>(&s->h_ctr), sizeof(uint32_t) * 64);
     if (e != cudaSuccess) {
         destroy(s);
@@ -1348,11 +1368,16 @@ static asph_status create_impl(const asph_parameters* parameters, const float* p
               : setup_boundary(s, boundary, boundary_count));
     if (walls) s->launches += walls->launches;
     if (count > 0) {
+        // the caller's positions, read in place where the device reads host memory coherently, else copied first
         float4* d_pos = nullptr;
-        TRY(dalloc(d_pos, count));
-        e = cudaMemcpyAsync(d_pos, positions, sizeof(float4) * count, cudaMemcpyHostToDevice, s->stream);
+        const float4* src = reinterpret_cast<const float4*>(positions);
+        if (!device_reads_host_in_place(positions, alignof(float4))) {
+            TRY(dalloc(d_pos, count));
+            e = cudaMemcpyAsync(d_pos, positions, sizeof(float4) * count, cudaMemcpyHostToDevice, s->stream);
+            src = d_pos;
+        }
         if (e == cudaSuccess) {
-            k_init_state<<<blocks_for(count), 256, 0, s->stream>>>(s->args(s->cur), d_pos, P.base_particle_radius,
+            k_init_state<<<blocks_for(count), 256, 0, s->stream>>>(s->args(s->cur), src, P.base_particle_radius,
                                                                    P.base_smoothing_radius, P.base_particle_mass);
             e = cudaGetLastError();
         }
