@@ -120,6 +120,7 @@ DEBUG_SIGNATURES = {
     "asph_debug_record_refinement": (ctypes.c_int, [_vp, ctypes.c_int]),
     "asph_debug_refinement_ids": (ctypes.c_int, [_vp, _up, _up, _up, _u32]),
     "asph_debug_wait_limit_probe": (ctypes.c_int, [_up]),
+    "asph_debug_host_reads_in_place": (ctypes.c_int, [ctypes.c_int]),
 }
 
 

@@ -533,7 +533,10 @@ asph_status setup_boundary_device(asph_simulation* s, const float4* d_pos, const
 // translation over NVLink-C2C, as on Grace-Blackwell): creation then reads the caller's arrays in place, one pass
 // at link bandwidth, instead of staging them through a pageable copy. Without translation through the host's page
 // tables (pageable access by page migration) the pages would move to the device, so that case copies.
+std::atomic<int> g_host_reads_in_place{1};  // asph_debug_host_reads_in_place: 0 forces the staging copies
+
 bool device_reads_host_in_place(const void* p, size_t align) {
+    if (g_host_reads_in_place.load(std::memory_order_relaxed) == 0) return false;
     if (reinterpret_cast<uintptr_t>(p) % align != 0) return false;
     int dev = 0, pageable = 0, host_tables = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
@@ -2822,6 +2825,13 @@ asph_status asph_estimate_device_bytes(const asph_parameters* parameters, uint32
 }
 
 }  // extern "C"
+
+// Creation reads the caller's positions and boundary records in place where the device reads host memory through
+// the host's page tables; 0 makes it stage them through copies as on other hosts, so that both paths can be
+// compared on one device (test hook, not in asph.h). Returns the previous setting.
+extern "C" int asph_debug_host_reads_in_place(int enable) {
+    return g_host_reads_in_place.exchange(enable ? 1 : 0);
+}
 
 // Failure detection without a fault (test hook, not in asph.h): runs a sort pass whose bounded look-back wait runs
 // out, and returns the error word it left (ASPH_DEVERR_SPIN_LIMIT expected); the context stays usable.

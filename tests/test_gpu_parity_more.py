@@ -331,3 +331,38 @@ def test_rows_grow_with_the_particle_count_bitexact(path):
         assert_state_bitexact(sim.read_state(), orc.arrays())
         batch.close()
     assert sim.device_errors() == 0
+
+
+def test_creation_in_place_and_staged_equal():
+    """Creation reads the positions and wall records in place where the device reads host memory through the
+    host's page tables, and stages them through copies elsewhere (forced here by a test hook) or when the positions
+    are not 16-byte aligned: every way gives the same state and the same trajectory, bit for bit."""
+    from adaptivesph_gb300 import _lib, create_simulation
+    sc = small_dam_break()
+    bd = boundary_of(sc)
+    L = _lib.load()
+
+    def run(pos):
+        sim = create_simulation(sc.parameters, pos, None, None, bd, None, pos.shape[0], bd.get_particle_count())
+        first = sim.read_state()
+        for _ in range(5):
+            sim.update(sc.dt)
+        st = sim.read_state()
+        sim.close()
+        return first, st
+
+    a0, a = run(sc.positions)
+    prev = L.asph_debug_host_reads_in_place(0)
+    try:
+        b0, b = run(sc.positions)
+    finally:
+        L.asph_debug_host_reads_in_place(prev)
+    buf = np.empty(sc.positions.size + 1, np.float32)
+    mis = buf[1:].reshape(-1, 4)
+    mis[:] = sc.positions
+    assert mis.ctypes.data % 16 != 0
+    c0, c = run(mis)
+    for got in (b0, c0):
+        assert_state_bitexact(got, a0)
+    for got in (b, c):
+        assert_state_bitexact(got, a)
