@@ -543,6 +543,20 @@ __device__ __forceinline__ bool for_each_cell_warp(const GridDev& g, const uint3
                     }
                 }
                 uint32_t live = __ballot_sync(0xffffffffu, sb != kEmpty) & 0xffu;
+                // the sub-cells some lane may need, tested against the reference cell's max h (at least each
+                // sub-cell's, so no sub-cell a lane needs is dropped; the exact test below stays as it was): the
+                // loop then visits only those instead of every non-empty one. e2 of octant q is summed as below,
+                // x + y first, so the two tests see the same value.
+                uint32_t may = 0u;
+                if (need) {
+                    const float rr = reach * reach;
+                    const float s00 = q0[0] + q0[1], s10 = q1[0] + q0[1], s01 = q0[0] + q1[1], s11 = q1[0] + q1[1];
+                    may = (s00 + q0[2] <= rr ? 0x01u : 0u) | (s10 + q0[2] <= rr ? 0x02u : 0u) |
+                          (s01 + q0[2] <= rr ? 0x04u : 0u) | (s11 + q0[2] <= rr ? 0x08u : 0u) |
+                          (s00 + q1[2] <= rr ? 0x10u : 0u) | (s10 + q1[2] <= rr ? 0x20u : 0u) |
+                          (s01 + q1[2] <= rr ? 0x40u : 0u) | (s11 + q1[2] <= rr ? 0x80u : 0u);
+                }
+                live &= __reduce_or_sync(0xffffffffu, may);
                 while (live != 0u) {
                     const int q = __ffs(live) - 1;
                     live &= live - 1u;
