@@ -494,22 +494,50 @@ __device__ __forceinline__ bool for_each_cell_warp(const GridDev& g, const uint3
     }
     if (!__any_sync(0xffffffffu, ok)) return true;
     const int64_t span = (int64_t)(uhi[0] - ulo[0] + 1) * (uhi[1] - ulo[1] + 1) * (uhi[2] - ulo[2] + 1);
-    if (span > max_union) return false;
+    if (span > max_union || span > 64) return false;
     const bool periodic = g.periodic;
     const float m = g.cull_margin;
     const int lane = (int)(threadIdx.x & 31u);
+    // The union's reference cells are numbered in walk order, t = ((rz - ulo) * ny + (ry - ulo)) * nx + (rx - ulo);
+    // lane l fetches the max h of cells l and l + 32 up front (0 outside the grid or for an excluded cell), and the
+    // walk takes each cell's from a shuffle instead of a load it would wait for.
+    const int32_t nx = uhi[0] - ulo[0] + 1, ny = uhi[1] - ulo[1] + 1;
+    auto ref_hmax = [&](int32_t t) -> float {
+        if (t >= (int32_t)span) return 0.0f;
+        const int32_t rx = ulo[0] + t % nx, ry = ulo[1] + (t / nx) % ny, rz = ulo[2] + t / (nx * ny);
+        float sh;
+        const int32_t cz = wrap_cell(rz, g.gs[2], g.scale[2], periodic, sh);
+        const int32_t cy = wrap_cell(ry, g.gs[1], g.scale[1], periodic, sh);
+        const int32_t cx = wrap_cell(rx, g.gs[0], g.scale[0], periodic, sh);
+        if (cz < 0 || cz >= g.gs[2] || cy < 0 || cy >= g.gs[1] || cx < 0 || cx >= g.gs[0]) return 0.0f;
+        const uint32_t rk = (uint32_t)cx + (uint32_t)g.gs[0] * ((uint32_t)cy + (uint32_t)g.gs[1] * (uint32_t)cz);
+        if (!periodic && (rk == ex0 || rk == ex1)) return 0.0f;
+        return __ldg(hmax_ref + rk);
+    };
+    const float hr_lo = ref_hmax(lane), hr_hi = ref_hmax(lane + 32);
     for (int32_t rz = ulo[2]; rz <= uhi[2]; ++rz) {
         for (int32_t ry = ulo[1]; ry <= uhi[1]; ++ry) {
             for (int32_t rx = ulo[0]; rx <= uhi[0]; ++rx) {
+                const int32_t t = ((rz - ulo[2]) * ny + (ry - ulo[1])) * nx + (rx - ulo[0]);
+                const float hr = __shfl_sync(0xffffffffu, t < 32 ? hr_lo : hr_hi, t & 31);
+                if (hr <= 0.0f) continue;  // empty, outside the grid or excluded
                 float shz, shy, shx;
                 const int32_t cz = wrap_cell(rz, g.gs[2], g.scale[2], periodic, shz);
                 const int32_t cy = wrap_cell(ry, g.gs[1], g.scale[1], periodic, shy);
                 const int32_t cx = wrap_cell(rx, g.gs[0], g.scale[0], periodic, shx);
-                if (cz < 0 || cz >= g.gs[2] || cy < 0 || cy >= g.gs[1] || cx < 0 || cx >= g.gs[0]) continue;
-                const uint32_t rk = (uint32_t)cx + (uint32_t)g.gs[0] * ((uint32_t)cy + (uint32_t)g.gs[1] * (uint32_t)cz);
-                if (!periodic && (rk == ex0 || rk == ex1)) continue;
-                const float hr = __ldg(hmax_ref + rk);
-                if (hr <= 0.0f) continue;
+                // the eight sub-cells' member ranges and max h, fetched by lanes 0-7 at once, issued before the
+                // reach tests below so that their latency overlaps them (fetched for every octant: the tables
+                // hold every sub-cell, and only the non-empty ones are used)
+                uint32_t sb = kEmpty, se = 0u;
+                float shm = 0.0f;
+                if (lane < 8) {
+                    const int32_t sx = 2 * cx + (lane & 1), sy = 2 * cy + ((lane >> 1) & 1), sz = 2 * cz + (lane >> 2);
+                    const uint32_t lin =
+                        (uint32_t)sx + (uint32_t)g.sgs[0] * ((uint32_t)sy + (uint32_t)g.sgs[1] * (uint32_t)sz);
+                    sb = __ldg(start + lin);
+                    se = __ldg(end + lin);
+                    shm = __ldg(hmax + lin);
+                }
                 bool need = ok && rx >= lo[0] && rx <= hi[0] && ry >= lo[1] && ry <= hi[1] && rz >= lo[2] &&
                             rz <= hi[2];
                 const float reach = 2.0f * hr * 1.00005f;
@@ -529,19 +557,6 @@ __device__ __forceinline__ bool for_each_cell_warp(const GridDev& g, const uint3
                 }
                 need &= d2 <= reach * reach;
                 if (!__any_sync(0xffffffffu, need)) continue;
-                // the eight sub-cells' member ranges and max h, fetched by lanes 0-7 at once
-                uint32_t sb = kEmpty, se = 0u;
-                float shm = 0.0f;
-                if (lane < 8) {
-                    const int32_t sx = 2 * cx + (lane & 1), sy = 2 * cy + ((lane >> 1) & 1), sz = 2 * cz + (lane >> 2);
-                    const uint32_t lin =
-                        (uint32_t)sx + (uint32_t)g.sgs[0] * ((uint32_t)sy + (uint32_t)g.sgs[1] * (uint32_t)sz);
-                    sb = __ldg(start + lin);
-                    if (sb != kEmpty) {
-                        se = __ldg(end + lin);
-                        shm = __ldg(hmax + lin);
-                    }
-                }
                 uint32_t live = __ballot_sync(0xffffffffu, sb != kEmpty) & 0xffu;
                 // the sub-cells some lane may need, tested against the reference cell's max h (at least each
                 // sub-cell's, so no sub-cell a lane needs is dropped; the exact test below stays as it was): the
