@@ -98,13 +98,32 @@ __device__ __forceinline__ bool density_term(const StepArgs& a, float4 pi, uint3
     return true;
 }
 
+// density_term of a neighbour from the particle's row (accepted by the scan's support test on the same operands):
+// the position from pq, as in density_pair<..., true>.
+__device__ __forceinline__ void density_term_accepted(const StepArgs& a, float4 pi, uint32_t j, float shx, float shy,
+                                                      float shz, float& rho) {
+    const float4 pj = __ldg(a.pq + j);
+    const bool periodic = a.grid.periodic;
+    const float xj = periodic ? pj.x + shx : pj.x;
+    const float yj = periodic ? pj.y + shy : pj.y;
+    const float zj = periodic ? pj.z + shz : pj.z;
+    const float dx = xj - pi.x, dy = yj - pi.y, dz = zj - pi.z;
+    const float r2 = dist2(dx, dy, dz);
+    const float4 kj = __ldg(a.kc + j);
+    const float w = kernel_w(sqrtf(r2), kj.x, kj.y);
+    rho = fmaf(kj.w, w, rho);
+}
+
 // density_term for two neighbours, in packed FP32x2 arithmetic (each half rounds as the scalar operation), added in
 // order: j1 then j2. kAccepted: both are members of the particle's row, accepted by the same support test (same
 // operands, same operations) in the scan, so the test is not repeated.
+// With kAccepted the positions come from pq (the same x, y, z; its w, (2h)^2, is then unused), which the density
+// scan has just read for the same candidates, so the loads tend to hit L1.
 template <bool kPeriodic, bool kAccepted = false>
 __device__ __forceinline__ void density_pair(const StepArgs& a, float4 pi, uint32_t j1, float s1x, float s1y,
                                              float s1z, uint32_t j2, float s2x, float s2y, float s2z, float& rho) {
-    const float4 p1 = __ldg(a.ph + j1), p2 = __ldg(a.ph + j2);
+    const float4* pos = kAccepted ? a.pq : a.ph;
+    const float4 p1 = __ldg(pos + j1), p2 = __ldg(pos + j2);
     const float4 k1 = __ldg(a.kc + j1), k2 = __ldg(a.kc + j2);
     float2 x = make_float2(p1.x, p2.x), y = make_float2(p1.y, p2.y), z = make_float2(p1.z, p2.z);
     if (kPeriodic) {
@@ -727,7 +746,7 @@ __device__ __forceinline__ void density_ordinary(const StepArgs& a, const CellsD
             float s1x, s1y, s1z, s2x, s2y, s2z;
             if (!pull(j1, s1x, s1y, s1z)) break;
             if (!pull(j2, s2x, s2y, s2z)) {
-                density_term(a, pi, j1, s1x, s1y, s1z, rho);
+                density_term_accepted(a, pi, j1, s1x, s1y, s1z, rho);
                 break;
             }
             density_pair<periodic, true>(a, pi, j1, s1x, s1y, s1z, j2, s2x, s2y, s2z, rho);
