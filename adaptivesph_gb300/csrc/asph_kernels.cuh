@@ -20,6 +20,7 @@ struct StepArgs {
     uint32_t* id;
     uint32_t* err;
     float4* pq;   // x, y, z, (2h)^2: the support test's operands, written by the reorder kernel for the density scan
+    float4* fr;   // rho, p/rho^2, 1/h, dcoef/h^4: a neighbour's force-pass operands, written by the density pass
 };
 
 // The step's particle count: from the device when the step is replayed from a graph (the count may have changed

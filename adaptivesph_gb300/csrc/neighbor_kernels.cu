@@ -255,8 +255,8 @@ __device__ __forceinline__ void force_term(const StepArgs& a, const ForceCtx& c,
     const float r2 = dist2(dx, dy, dz);
     const float twoh = pj.w + pj.w;
     if (r2 > twoh * twoh) return;
-    const float4 kj = __ldg(a.kc + j);
-    const float2 rpj = __ldg(a.rp + j);
+    const float4 fj = __ldg(a.fr + j);  // rho, p/rho^2, 1/h, dcoef/h^4
+    const float4 vj = __ldg(a.vm + j);  // v, m
     const float r = sqrtf(r2);
     float u[3];
     if (r > 0.0f) {
@@ -269,17 +269,16 @@ __device__ __forceinline__ void force_term(const StepArgs& a, const ForceCtx& c,
         u[1] = 1.0f;
         u[2] = 0.0f;
     }
-    const float dw = kernel_dw(r, kj.x, kj.z);
-    const float mj = kj.w;
+    const float dw = kernel_dw(r, fj.z, fj.w);
+    const float mj = vj.w;
     {
-        const float sp = (mj * dw) * (c.pti + rpj.y);
+        const float sp = (mj * dw) * (c.pti + fj.y);
 #pragma unroll
         for (int q = 0; q < 3; q++) f.ap[q] = fmaf(-sp, u[q], f.ap[q]);
     }
     if (c.visc_on) {
-        const float4 vj = __ldg(a.vm + j);
         const float vd[3] = {c.vi.x - vj.x, c.vi.y - vj.y, c.vi.z - vj.z};
-        const float rhoj = rpj.x;
+        const float rhoj = fj.x;
         if (!kMorris) {
             const float comp = fmaf(vd[2], dz, fmaf(vd[1], dy, vd[0] * dx));
             if (comp < 0.0f) {
@@ -297,6 +296,7 @@ __device__ __forceinline__ void force_term(const StepArgs& a, const ForceCtx& c,
         }
     }
     if (kSigma && c.sigma_on) {
+        const float4 kj = __ldg(a.kc + j);
         const float ss = mj * kernel_w(r, kj.x, kj.y);
 #pragma unroll
         for (int q = 0; q < 3; q++) f.as[q] = fmaf(ss, u[q], f.as[q]);
@@ -309,13 +309,8 @@ template <bool kMorris, bool kPeriodic, bool kSigma = true, bool kAccepted = fal
 __device__ __forceinline__ void force_pair(const StepArgs& a, const ForceCtx& c, uint32_t j1, float s1x, float s1y,
                                            float s1z, uint32_t j2, float s2x, float s2y, float s2z, ForceAcc& f) {
     const float4 p1 = __ldg(a.ph + j1), p2 = __ldg(a.ph + j2);
-    const float4 k1 = __ldg(a.kc + j1), k2 = __ldg(a.kc + j2);
-    const float2 rp1 = __ldg(a.rp + j1), rp2 = __ldg(a.rp + j2);
-    float4 v1 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), v2 = v1;
-    if (c.visc_on) {
-        v1 = __ldg(a.vm + j1);
-        v2 = __ldg(a.vm + j2);
-    }
+    const float4 f1 = __ldg(a.fr + j1), f2 = __ldg(a.fr + j2);  // rho, p/rho^2, 1/h, dcoef/h^4
+    const float4 v1 = __ldg(a.vm + j1), v2 = __ldg(a.vm + j2);  // v, m
     float2 x = make_float2(p1.x, p2.x), y = make_float2(p1.y, p2.y), z = make_float2(p1.z, p2.z);
     if (kPeriodic) {
         x = __fadd2_rn(x, make_float2(s1x, s2x));
@@ -345,14 +340,14 @@ __device__ __forceinline__ void force_pair(const StepArgs& a, const ForceCtx& c,
         uz.y = 0.0f;
     }
     // kernel_dw(r, 1/h, dcoef/h^4)
-    const float2 q = __fmul2_rn(r, make_float2(k1.x, k2.x));
+    const float2 q = __fmul2_rn(r, make_float2(f1.z, f2.z));
     const float2 t = __ffma2_rn(make_float2(-0.5f, -0.5f), q, make_float2(1.0f, 1.0f));
     const float2 t3 = __fmul2_rn(__fmul2_rn(t, t), t);
-    float2 dw = __fmul2_rn(__fmul2_rn(make_float2(k1.z, k2.z), q), t3);
+    float2 dw = __fmul2_rn(__fmul2_rn(make_float2(f1.w, f2.w), q), t3);
     if (q.x > 2.0f) dw.x = 0.0f;
     if (q.y > 2.0f) dw.y = 0.0f;
-    const float2 m = make_float2(k1.w, k2.w);
-    const float2 sp = __fmul2_rn(__fmul2_rn(m, dw), __fadd2_rn(make_float2(c.pti, c.pti), make_float2(rp1.y, rp2.y)));
+    const float2 m = make_float2(v1.w, v2.w);
+    const float2 sp = __fmul2_rn(__fmul2_rn(m, dw), __fadd2_rn(make_float2(c.pti, c.pti), make_float2(f1.y, f2.y)));
     if (ok1) {
         f.ap[0] = fmaf(-sp.x, ux.x, f.ap[0]);
         f.ap[1] = fmaf(-sp.x, uy.x, f.ap[1]);
@@ -367,7 +362,7 @@ __device__ __forceinline__ void force_pair(const StepArgs& a, const ForceCtx& c,
         const float2 vdx = __fadd2_rn(make_float2(c.vi.x, c.vi.x), make_float2(-v1.x, -v2.x));
         const float2 vdy = __fadd2_rn(make_float2(c.vi.y, c.vi.y), make_float2(-v1.y, -v2.y));
         const float2 vdz = __fadd2_rn(make_float2(c.vi.z, c.vi.z), make_float2(-v1.z, -v2.z));
-        const float2 rhoj = make_float2(rp1.x, rp2.x);
+        const float2 rhoj = make_float2(f1.x, f2.x);
         const float2 den = __fadd2_rn(r2, make_float2(c.ei, c.ei));
         if (!kMorris) {
             const float2 comp = __ffma2_rn(vdz, dz, __ffma2_rn(vdy, dy, __fmul2_rn(vdx, dx)));
@@ -408,6 +403,7 @@ __device__ __forceinline__ void force_pair(const StepArgs& a, const ForceCtx& c,
         }
     }
     if (kSigma && c.sigma_on) {
+        const float4 k1 = __ldg(a.kc + j1), k2 = __ldg(a.kc + j2);
         if (ok1) {
             const float ss = m.x * kernel_w(r.x, k1.x, k1.y);
             f.as[0] = fmaf(ss, ux.x, f.as[0]);
@@ -758,7 +754,10 @@ __device__ __forceinline__ void density_ordinary(const StepArgs& a, const CellsD
     nl.bcnt[i] = bn;
     const float rh = rho + rb;
     if (!isfinite(rh)) atomicOr(a.err, 0x2u);
-    a.rp[i] = make_float2(rh, pressure_term(rh, a.phys.rho0, a.phys.B));
+    const float pt = pressure_term(rh, a.phys.rho0, a.phys.B);
+    a.rp[i] = make_float2(rh, pt);
+    const float4 ki = a.kc[i];
+    a.fr[i] = make_float4(rh, pt, ki.x, ki.z);
 }
 
 template <bool kPeriodic>
@@ -810,7 +809,10 @@ __device__ __forceinline__ void density_heavy_item(const StepArgs& a, const Cell
         if (lane == 0) {
             const float rh = rho + rb;
             if (!isfinite(rh)) atomicOr(a.err, 0x2u);
-            a.rp[i] = make_float2(rh, pressure_term(rh, a.phys.rho0, a.phys.B));
+            const float pt = pressure_term(rh, a.phys.rho0, a.phys.B);
+            a.rp[i] = make_float2(rh, pt);
+            const float4 ki = a.kc[i];
+            a.fr[i] = make_float4(rh, pt, ki.x, ki.z);
             nl.fheavy[atomicAdd(nl.fheavy_n, 1u)] = i;
         }
     }
@@ -969,7 +971,10 @@ __device__ __forceinline__ void density_row_item(const StepArgs& a, const Bounda
         if (lane == 0) {
             const float rh = rho + rb;
             if (!isfinite(rh)) atomicOr(a.err, 0x2u);
-            a.rp[i] = make_float2(rh, pressure_term(rh, a.phys.rho0, a.phys.B));
+            const float pt = pressure_term(rh, a.phys.rho0, a.phys.B);
+            a.rp[i] = make_float2(rh, pt);
+            const float4 ki = a.kc[i];
+            a.fr[i] = make_float4(rh, pt, ki.x, ki.z);
             nl.frow[atomicAdd(nl.frow_n, 1u)] = i;
         }
     }

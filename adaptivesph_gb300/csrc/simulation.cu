@@ -171,6 +171,7 @@ struct asph_simulation {
     int cur = 0;
     float4* kc = nullptr;
     float4* pq = nullptr;  // [cap] x, y, z, (2h)^2 of the current step (StepArgs::pq)
+    float4* fr = nullptr;  // [cap] rho, p/rho^2, 1/h, dcoef/h^4 of the current step (StepArgs::fr)
     uint2* nbr_ent = nullptr;     // [kListEntries * rows_cap] neighbour lists, one row per particle
     uint32_t rows_cap = 0;        // particles the rows are allocated for (grown on demand, never above cap)
     uint8_t* arena = nullptr;     // one allocation holding the fixed-size buffers (carve_fixed)
@@ -296,6 +297,7 @@ struct asph_simulation {
         a.kc = kc;
         a.err = err;
         a.pq = pq;
+        a.fr = fr;
         return a;
     }
 
@@ -1219,6 +1221,7 @@ static void carve_fixed(asph_simulation* s, Carver& c, uint32_t sort_items) {
     }
     c.take(s->kc, C);
     c.take(s->pq, C);
+    c.take(s->fr, C);
     c.take(s->nbr_cnt, C);
     c.take(s->nbr_bcnt, C);
     c.take(s->heavy_idx, C);
