@@ -377,7 +377,7 @@ uint64_t device_bytes_for(uint32_t C, uint32_t sort_items, uint32_t ncells, uint
     const uint64_t c = C;
     uint64_t b = 0;
     b += 2 * c * (sizeof(float4) * 3 + sizeof(float2) + sizeof(float) + sizeof(uint32_t));  // two buffer sets
-    b += c * sizeof(float4) * 2;                                           // kernel constants, support operands
+    b += c * sizeof(float4) * 3;                          // kernel constants, support operands, force operands
     b += c * kListEntries * sizeof(uint2) + c * sizeof(uint32_t) * 2;                      // rows and counts
     b += c * sizeof(uint32_t) * 5 + sizeof(uint32_t) * 5;                                   // queues
     const uint64_t slots = std::min<uint32_t>(kPoolSlots, std::max<uint32_t>(64u, C / 128u));
