@@ -191,9 +191,10 @@ struct asph_simulation {
     uint32_t* vals = nullptr;
     void* sort_mem = nullptr;
     SortScratch ss{};
-    uint32_t* cell_start = nullptr;
-    uint32_t* cell_end = nullptr;
+    uint32_t* cell_start = nullptr;  // the five sub-cell tables (start, end, max h; the boundary's start, end)
+    uint32_t* cell_end = nullptr;    // are carved from one allocation, cell_block
     float* cell_hmax = nullptr;
+    uint8_t* cell_block = nullptr;
     uint32_t cells_alloc = 0;
     float* hmax_ref = nullptr;  // [gs.x * gs.y * gs.z] max h per reference cell
     uint32_t refcells_alloc = 0;
@@ -451,18 +452,20 @@ asph_status alloc_cells(asph_simulation* s) {
         s->refcells_alloc = refcells;
     }
     if (s->grid.ncells <= s->cells_alloc) return ASPH_OK;
-    dfree(s->cell_start);
-    dfree(s->cell_end);
-    dfree(s->cell_hmax);
-    dfree(s->bstart);
-    dfree(s->bend);
+    dfree(s->cell_block);
+    s->cell_block = nullptr;
+    s->cell_start = s->cell_end = s->bstart = s->bend = nullptr;
+    s->cell_hmax = nullptr;
     s->cells_alloc = 0;
+    // one allocation for the five tables (each cudaMalloc costs tens of microseconds at creation)
+    const size_t table = ((size_t)s->grid.ncells * sizeof(uint32_t) + 255) / 256 * 256;
     asph_status st;
-    if ((st = dalloc(s->cell_start, s->grid.ncells)) != ASPH_OK) return st;
-    if ((st = dalloc(s->cell_end, s->grid.ncells)) != ASPH_OK) return st;
-    if ((st = dalloc(s->cell_hmax, s->grid.ncells)) != ASPH_OK) return st;
-    if ((st = dalloc(s->bstart, s->grid.ncells)) != ASPH_OK) return st;
-    if ((st = dalloc(s->bend, s->grid.ncells)) != ASPH_OK) return st;
+    if ((st = dalloc(s->cell_block, 5 * table)) != ASPH_OK) return st;
+    s->cell_start = reinterpret_cast<uint32_t*>(s->cell_block);
+    s->cell_end = reinterpret_cast<uint32_t*>(s->cell_block + table);
+    s->cell_hmax = reinterpret_cast<float*>(s->cell_block + 2 * table);
+    s->bstart = reinterpret_cast<uint32_t*>(s->cell_block + 3 * table);
+    s->bend = reinterpret_cast<uint32_t*>(s->cell_block + 4 * table);
     s->cells_alloc = s->grid.ncells;
     return ASPH_OK;
 }
@@ -552,15 +555,23 @@ bool device_reads_host_in_place(const void* p, size_t align) {
 
 // The caller's boundary records: read in place (device_reads_host_in_place) or copied as they are, then split into
 // positions and psi on the device.
-asph_status setup_boundary(asph_simulation* s, const asph_boundary_particle* b, uint32_t nb) {
+// At creation (spare) the other buffer set, not yet used, holds the unsorted positions and psi when they fit.
+asph_status setup_boundary(asph_simulation* s, const asph_boundary_particle* b, uint32_t nb, bool spare = false) {
     if (nb == 0) return setup_boundary_device(s, nullptr, nullptr, 0);
     static_assert(sizeof(asph_boundary_particle) == 5 * sizeof(float), "boundary records are 5 floats");
     float4* d_pos = nullptr;
     float* d_psi = nullptr;
     float* d_rec = nullptr;
     const float* rec = reinterpret_cast<const float*>(b);
-    asph_status st = dalloc(d_pos, nb);
-    if (st == ASPH_OK) st = dalloc(d_psi, nb);
+    const bool own = !(spare && nb <= s->cap);
+    asph_status st = ASPH_OK;
+    if (own) {
+        st = dalloc(d_pos, nb);
+        if (st == ASPH_OK) st = dalloc(d_psi, nb);
+    } else {
+        d_pos = s->set[1 - s->cur].ph;
+        d_psi = s->set[1 - s->cur].rad;
+    }
     cudaError_t e = cudaSuccess;
     if (st == ASPH_OK && !device_reads_host_in_place(b, alignof(float))) {
         st = dalloc(d_rec, 5 * (size_t)nb);
@@ -576,8 +587,10 @@ asph_status setup_boundary(asph_simulation* s, const asph_boundary_particle* b, 
     if (st == ASPH_OK) st = e == cudaSuccess ? setup_boundary_device(s, d_pos, d_psi, nb) : cuda_fail(e, "boundary upload");
     cudaStreamSynchronize(s->stream);
     dfree(d_rec);
-    dfree(d_pos);
-    dfree(d_psi);
+    if (own) {
+        dfree(d_pos);
+        dfree(d_psi);
+    }
     return st;
 }
 
@@ -1009,19 +1022,14 @@ void destroy(asph_simulation* s) {
     s->own_graph = nullptr;
     dfree(s->arena);  // the fixed-size buffers (carve_fixed)
     dfree(s->nbr_ent);
-    dfree(s->cell_start);
-    dfree(s->cell_end);
-    dfree(s->cell_hmax);
+    dfree(s->cell_block);  // the five sub-cell tables
     dfree(s->hmax_ref);
     dfree(s->bpos);
     dfree(s->bfric);
-    dfree(s->bstart);
-    dfree(s->bend);
     dfree(s->brefflag);
     dfree(s->dbg_ids);
     dfree(s->stage);
-    if (s->h_ctr) cudaFreeHost(s->h_ctr);
-    if (s->h_small) cudaFreeHost(s->h_small);
+    if (s->h_ctr) cudaFreeHost(s->h_ctr);  // h_small lies in the same allocation
     for (auto& e : s->events) {
         cudaEventDestroy(e.a);
         cudaEventDestroy(e.b);
@@ -1358,20 +1366,17 @@ static asph_status create_impl(const asph_parameters* parameters, const float* p
     s->rows_cap = rows_for(count, C);
     TRY(dalloc(s->nbr_ent, (size_t)kListEntries * s->rows_cap));
     TRY(alloc_cells(s));
-    e = cudaMallocHost(reinterpret_cast<void**>(&s->h_ctr), sizeof(uint32_t) * 64);
+    // the pinned read-back words: 64 counters, then 16 64-bit values, in one allocation
+    e = cudaMallocHost(reinterpret_cast<void**>(&s->h_ctr), sizeof(uint32_t) * 64 + sizeof(uint64_t) * 16);
     if (e != cudaSuccess) {
         destroy(s);
         return cuda_fail(e, "cudaMallocHost");
     }
-    e = cudaMallocHost(reinterpret_cast<void**>(&s->h_small), sizeof(uint64_t) * 16);
-    if (e != cudaSuccess) {
-        destroy(s);
-        return cuda_fail(e, "cudaMallocHost");
-    }
+    s->h_small = reinterpret_cast<decltype(s->h_small)>(s->h_ctr + 64);
     CK(cudaMemsetAsync(s->err, 0, sizeof(uint32_t), s->stream));
     s->bcap = 0;
     TRY(walls ? setup_boundary_device(s, walls->pos, walls->psi, walls->n)
-              : setup_boundary(s, boundary, boundary_count));
+              : setup_boundary(s, boundary, boundary_count, true));
     if (walls) s->launches += walls->launches;
     if (count > 0) {
         // the caller's positions, read in place where the device reads host memory coherently, else copied first
